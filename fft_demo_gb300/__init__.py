@@ -1,0 +1,168 @@
+"""fft_demo_gb300: tensor-core FFT / FFT convolution for one GB300 (sm_103a).
+
+Python host mirror of the C ABI in include/tcfft_gb300.h. The compute path is
+the in-tree CUDA library libtcfft_gb300.so; there is no CPU fallback: if the
+library is missing or no sm_103 device is present, calls raise.
+
+torch is used only for device memory and streams (tensors are passed to the
+C ABI as raw device pointers).
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libtcfft_gb300.so")
+
+# tcfftStatus
+OK, INVALID_SIZE, UNSUPPORTED, ALLOC_FAILED, LAUNCH_FAILED, TIMEOUT, CAPACITY, INVALID_VALUE, \
+    NO_DEVICE = range(9)
+# tcfftPrecision
+FP16, SPLIT_FP32 = 0, 1
+# tcfftDirection
+FORWARD, INVERSE = -1, 1
+
+_lib = None
+
+
+class TcfftError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        name = status_string(status) if _lib is not None else str(status)
+        super().__init__("%s%s" % (name, (": " + what) if what else ""))
+
+
+def lib():
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libtcfft_gb300.so not built; run __graft_entry__.build() "
+                              "or python fft_demo_gb300/build.py")
+        _lib = ctypes.CDLL(LIB_PATH)
+        _declare(_lib)
+    return _lib
+
+
+def _declare(L):
+    vp, i, ll, f = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong, ctypes.c_float
+    sig = {
+        "tcfft_plan_1d": (i, [ctypes.POINTER(vp), ll, ll, i]),
+        "tcfft_plan_2d": (i, [ctypes.POINTER(vp), i, i, ll, i]),
+        "tcfft_workspace_bytes": (i, [vp, ctypes.POINTER(ctypes.c_size_t)]),
+        "tcfft_exec": (i, [vp, vp, vp, i, f, vp]),
+        "tcfft_exec_digitrev": (i, [vp, vp, vp, ctypes.POINTER(i), i, vp]),
+        "tcfft_check": (i, [vp, vp]),
+        "tcfft_destroy": (i, [vp]),
+        "tcfft_get_last_error": (i, []),
+        "tcfft_status_string": (ctypes.c_char_p, [i]),
+        "tcfft_last_launch_count": (i, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+
+
+def status_string(s):
+    return lib().tcfft_status_string(int(s)).decode()
+
+
+def _check(status, what=""):
+    if status != OK:
+        raise TcfftError(status, what)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        import torch
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def last_launch_count():
+    return lib().tcfft_last_launch_count()
+
+
+class Plan:
+    """A 1D or 2D batched C2C plan (tcfftCreate / tcfftCreate_2d equivalent).
+
+    Data are torch tensors on the GPU: FP16 plans take interleaved complex
+    half (shape [..., 2], dtype float16, or complex32 viewed as such); split
+    plans take interleaved complex float32.
+    """
+
+    def __init__(self, n=None, batch=1, precision=FP16, shape2d=None):
+        self._h = ctypes.c_void_p()
+        self.precision = precision
+        self.batch = int(batch)
+        if shape2d is not None:
+            nx, ny = shape2d
+            self.dims, self.nx, self.ny, self.n = 2, int(nx), int(ny), int(nx) * int(ny)
+            _check(lib().tcfft_plan_2d(ctypes.byref(self._h), self.nx, self.ny, self.batch,
+                                       precision), "plan_2d(%d, %d, %d)" % (nx, ny, batch))
+        else:
+            self.dims, self.n = 1, int(n)
+            _check(lib().tcfft_plan_1d(ctypes.byref(self._h), self.n, self.batch, precision),
+                   "plan_1d(%d, %d)" % (n, batch))
+
+    @property
+    def elem_bytes(self):
+        return 4 if self.precision == FP16 else 8
+
+    def workspace_bytes(self):
+        b = ctypes.c_size_t()
+        _check(lib().tcfft_workspace_bytes(self._h, ctypes.byref(b)))
+        return b.value
+
+    def _validate(self, t):
+        need = self.n * self.batch * self.elem_bytes
+        if not t.is_cuda or t.numel() * t.element_size() != need or not t.is_contiguous():
+            raise TcfftError(INVALID_VALUE, "tensor must be contiguous CUDA with %d bytes" % need)
+
+    def exec(self, x, out=None, direction=FORWARD, scale=1.0, stream=None):
+        """out = scale * FFT(x); out=None -> in place."""
+        self._validate(x)
+        if out is None:
+            out = x
+        self._validate(out)
+        _check(lib().tcfft_exec(self._h, _ptr(x), _ptr(out), int(direction), float(scale),
+                                _stream_ptr(stream)), "exec")
+        return out
+
+    def exec_digitrev(self, x, radices, out=None, stream=None):
+        """Forward FFT of input in the reference's digit-reversed order."""
+        self._validate(x)
+        if out is None:
+            out = x
+        self._validate(out)
+        arr = (ctypes.c_int * max(1, len(radices)))(*radices)
+        _check(lib().tcfft_exec_digitrev(self._h, _ptr(x), _ptr(out), arr, len(radices),
+                                         _stream_ptr(stream)), "exec_digitrev")
+        return out
+
+    def check(self, stream=None):
+        """Synchronise and raise if a kernel of this plan flagged an error."""
+        _check(lib().tcfft_check(self._h, _stream_ptr(stream)), "check")
+
+    def destroy(self):
+        if self._h:
+            lib().tcfft_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+def plan_1d(n, batch=1, precision=FP16):
+    return Plan(n=n, batch=batch, precision=precision)
+
+
+def plan_2d(nx, ny, batch=1, precision=FP16):
+    return Plan(batch=batch, precision=precision, shape2d=(nx, ny))

@@ -1,0 +1,58 @@
+// Registry of instantiated pass kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "fft_tile.cuh"
+
+namespace tcfft {
+
+// Pass kinds (how lines sit in global memory and which way vectors run).
+enum PassKind : int {
+  kPassRow = 0,   // lines contiguous; load and store along the line
+  kPassCol = 1,   // lines = adjacent columns; load and store across lines
+  kPassRowT = 2,  // load along the line, store across lines (transposing)
+  kNumPassKinds = 3
+};
+
+// Tile-size variants: Mt = butterflies per radix-16 stage in one tile.
+enum TileSel : int { kTileSmall = 0 /* Mt = 128 */, kTileBig = 1 /* Mt = 1024 */, kNumTileSel = 2 };
+
+constexpr int kMinLogL = 4;
+constexpr int kMaxLogL = 14;
+
+struct PassKernel {
+  const void* fn = nullptr;
+  int smem = 0;
+  int G = 0;   // lines per tile
+  int Mt = 0;  // butterflies per stage per tile
+};
+
+// sign: 0 = forward, 1 = inverse
+const PassKernel& pass_kernel(int kind, int logL, int tile, int sign);
+
+// Filled by the instantiation units.
+void register_row_kernels(PassKernel (&tab)[kMaxLogL + 1][kNumTileSel][2]);
+void register_col_kernels(PassKernel (&tab)[kMaxLogL + 1][kNumTileSel][2]);
+void register_rowt_kernels(PassKernel (&tab)[kMaxLogL + 1][kNumTileSel][2]);
+
+template <int L, int Mt>
+constexpr int tile_lines() {
+  return Mt * 16 / L;
+}
+
+template <int L, int Mt, bool LINE_MINOR, bool IN_VEC_L, bool OUT_VEC_L>
+void fill_entry(PassKernel (&tab)[kMaxLogL + 1][kNumTileSel][2], int tile) {
+  constexpr int G = tile_lines<L, Mt>();
+  constexpr int LOG = ilog2c(L);
+  const int smem = pass_smem_bytes<L, G>();
+  PassKernel f, i;
+  f.fn = reinterpret_cast<const void*>(&fft_pass_f16<L, G, LINE_MINOR, IN_VEC_L, OUT_VEC_L, -1>);
+  i.fn = reinterpret_cast<const void*>(&fft_pass_f16<L, G, LINE_MINOR, IN_VEC_L, OUT_VEC_L, +1>);
+  f.smem = i.smem = smem;
+  f.G = i.G = G;
+  f.Mt = i.Mt = Mt;
+  tab[LOG][tile][0] = f;
+  tab[LOG][tile][1] = i;
+}
+
+}  // namespace tcfft

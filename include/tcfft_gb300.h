@@ -1,0 +1,94 @@
+/*
+ * tcfft_gb300 -- tensor-core FFT and FFT convolution for one GB300 (sm_103a).
+ *
+ * Thin C ABI: plain pointers, sizes and integer enums; no CUDA or C++ types.
+ * Device buffers are raw device pointers; `stream` is a cudaStream_t passed as
+ * void* (NULL = legacy default stream). Every call returns a tcfftStatus.
+ *
+ * Data formats
+ *   TCFFT_FP16        interleaved complex half (re, im) = 4 bytes / element,
+ *                     the format of the reference's half2 buffers.
+ *   TCFFT_SPLIT_FP32  interleaved complex float (re, im) = 8 bytes / element,
+ *                     computed with hi+lo FP16 operands on the tensor cores.
+ *
+ * Transforms are unnormalised (as the reference's); tcfft_exec's `scale`
+ * multiplies every output (pass 1.0f/N for a normalised inverse).
+ *
+ * Entry points replace (file:line in yuelingfan/fft_demo):
+ *   tcfft_plan_1d   tcfftCreate       tcfft_half.cu:1235  (plan + tables)
+ *   tcfft_exec      tcfftExec         tcfft_half.cu:1177  (launch chain)
+ *   tcfft_destroy   (none: the reference leaks its plans, tcfft_half.cu:1340)
+ *   tcfft_plan_2d   tcfftCreate_2d    tcfft_half_2d.cu:1151
+ *                   TensorCoreFFTCreate tensorcore_fft_conv2d_kernel.cu:1557
+ *   tcfft_exec      tcfftExec_2d      tcfft_half_2d.cu:1128
+ *                   TensorCoreFFTExec tensorcore_fft_conv2d_kernel.cu:1495,1526
+ *   tcfft_exec_digitrev  tcfftExec on the digit-reversed input that setup()
+ *                   prepares (tcfft_half.cu:1376-1394, gen_rev :1351)
+ */
+#ifndef TCFFT_GB300_H
+#define TCFFT_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum tcfftStatus {
+  TCFFT_OK = 0,
+  TCFFT_INVALID_SIZE = 1,   /* size not a supported power of two / too large */
+  TCFFT_UNSUPPORTED = 2,    /* valid request this build cannot do */
+  TCFFT_ALLOC_FAILED = 3,   /* device allocation failed */
+  TCFFT_LAUNCH_FAILED = 4,  /* a CUDA launch or call failed */
+  TCFFT_TIMEOUT = 5,        /* a bounded device wait gave up */
+  TCFFT_CAPACITY = 6,       /* request exceeds an admission / memory cap */
+  TCFFT_INVALID_VALUE = 7,  /* null pointer, bad enum, misaligned buffer */
+  TCFFT_NO_DEVICE = 8       /* no usable sm_103 device */
+} tcfftStatus;
+
+typedef enum tcfftPrecision { TCFFT_FP16 = 0, TCFFT_SPLIT_FP32 = 1 } tcfftPrecision;
+
+typedef enum tcfftDirection { TCFFT_FORWARD = -1, TCFFT_INVERSE = 1 } tcfftDirection;
+
+typedef struct tcfftPlanImpl *tcfftPlan;
+
+/* Batched 1D C2C plan: `batch` sequences of n points, back to back.
+ * n = 2^k, 16 <= n <= 2^24. */
+tcfftStatus tcfft_plan_1d(tcfftPlan *plan, long long n, long long batch, int precision);
+
+/* Batched 2D C2C plan over [batch][nx][ny] arrays (ny contiguous).
+ * nx, ny = 2^k in [16, 4096]. */
+tcfftStatus tcfft_plan_2d(tcfftPlan *plan, int nx, int ny, long long batch, int precision);
+
+/* Bytes of device workspace the plan holds (allocated at plan time). */
+tcfftStatus tcfft_workspace_bytes(tcfftPlan plan, size_t *bytes);
+
+/* out = scale * FFT_direction(in). in == out is allowed. Buffers must be
+ * 16-byte aligned device memory. Asynchronous on `stream`. */
+tcfftStatus tcfft_exec(tcfftPlan plan, const void *in, void *out, int direction, float scale,
+                       void *stream);
+
+/* Forward transform of input stored in the digit-reversed order of the
+ * reference's setup() for a radix list `radices[0..n_radices-1]`
+ * (product == n; n_radices == 0 means natural order). Output natural order,
+ * in place allowed. 1D FP16 plans only. */
+tcfftStatus tcfft_exec_digitrev(tcfftPlan plan, const void *in, void *out, const int *radices,
+                                int n_radices, void *stream);
+
+/* Synchronise `stream` and report any error a kernel of this plan flagged
+ * (e.g. TCFFT_TIMEOUT from a bounded wait). Clears the flag. */
+tcfftStatus tcfft_check(tcfftPlan plan, void *stream);
+
+tcfftStatus tcfft_destroy(tcfftPlan plan);
+
+/* Last status returned on this thread, and a readable name for a status. */
+tcfftStatus tcfft_get_last_error(void);
+const char *tcfft_status_string(tcfftStatus status);
+
+/* Number of kernel launches the last tcfft_exec* call on this thread made. */
+int tcfft_last_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TCFFT_GB300_H */

@@ -1,0 +1,22 @@
+#!/usr/bin/env bash
+# Builds pieces of the reference (yuelingfan/fft_demo) from its own sources,
+# where they lie, into oracle/_ref/. Used only to pin the oracle's
+# restatements on this machine (the sources are absent on GPU hosts):
+#   libref_tcfft1d.so  <- tcfft_half.cu     (gen_rev, tcfftCreate host logic)
+#   libref_tcfft2d.so  <- tcfft_half_2d.cu  (gen_rev_2d)
+# The two files define clashing kernel templates, so they become separate
+# libraries. Nothing here is copied; nvcc reads the reference tree read-only.
+set -euo pipefail
+REF=${REF:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT="$HERE/_ref"
+if [ ! -f "$REF/tcfft_half.cu" ]; then
+  echo "reference sources not found at $REF; skipping" >&2
+  exit 0
+fi
+mkdir -p "$OUT"
+NVFLAGS="-std=c++17 -O1 -shared -Xcompiler -fPIC -gencode arch=compute_103a,code=sm_103a -I$REF -I$REF/include"
+nvcc $NVFLAGS "$REF/tcfft_half.cu" -o "$OUT/libref_tcfft1d.so" -lcudart &
+nvcc $NVFLAGS "$REF/tcfft_half_2d.cu" -o "$OUT/libref_tcfft2d.so" -lcudart &
+wait
+echo "built: $(ls "$OUT")"

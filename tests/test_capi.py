@@ -1,0 +1,67 @@
+"""CPU tests of the C-ABI library: it builds, loads and exports every symbol
+the public headers declare. No compute calls (no GPU here)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    inc = os.path.join(REPO, "include")
+    for f in os.listdir(inc):
+        if not f.endswith(".h"):
+            continue
+        text = open(os.path.join(inc, f)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(tcfft_[a-z0-9_]+)\s*\(", text):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def built_lib():
+    from fft_demo_gb300 import build as b
+    path = b.build()
+    return ctypes.CDLL(path)
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    syms = declared_symbols()
+    assert len(syms) >= 10
+    missing = [s for s in syms if not hasattr(built_lib, s)]
+    assert not missing, missing
+
+
+def test_status_strings(built_lib):
+    import fft_demo_gb300 as t
+    assert t.status_string(t.OK) == "TCFFT_OK"
+    assert t.status_string(t.TIMEOUT) == "TCFFT_TIMEOUT"
+    assert t.status_string(99) == "TCFFT_UNKNOWN"
+
+
+def test_argument_validation_without_device(built_lib):
+    import fft_demo_gb300 as t
+    L = t.lib()
+    h = ctypes.c_void_p()
+    # size / value checks happen before any device call
+    assert L.tcfft_plan_1d(ctypes.byref(h), 1000, 1, t.FP16) == t.INVALID_SIZE
+    assert L.tcfft_plan_1d(ctypes.byref(h), 8, 1, t.FP16) == t.INVALID_SIZE
+    assert L.tcfft_plan_1d(ctypes.byref(h), 1024, 0, t.FP16) == t.INVALID_SIZE
+    assert L.tcfft_plan_1d(ctypes.byref(h), 1024, 1, 7) == t.INVALID_VALUE
+    assert L.tcfft_plan_1d(None, 1024, 1, t.FP16) == t.INVALID_VALUE
+    assert L.tcfft_plan_2d(ctypes.byref(h), 100, 64, 1, t.FP16) == t.INVALID_SIZE
+    assert L.tcfft_exec(None, None, None, -1, 1.0, None) == t.INVALID_VALUE
+    assert L.tcfft_get_last_error() == t.INVALID_VALUE
+
+
+def test_no_device_is_reported(built_lib):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import fft_demo_gb300 as t
+    h = ctypes.c_void_p()
+    assert t.lib().tcfft_plan_1d(ctypes.byref(h), 1024, 4, t.FP16) == t.NO_DEVICE
