@@ -1,0 +1,374 @@
+"""Benchmark: large batched 1D FFT (plain FP16) on one GB300.
+
+Workload ("large-1d-fp16"): forward C2C FFTs of N = 4096, 65536 and 1048576
+points, each over a 1 GiB FP16 array (batch = 65536, 4096, 256), inputs
+i.i.d. uniform[-1, 1] (seeded). One step = one forward transform of each of
+the three arrays. Metric: GFLOP/s with the 5 N log2 N convention, summed over
+the three transforms; the JSON line also carries the HBM roofline fraction of
+the dominant kernel and an end-to-end number through the public API with the
+inputs copied from pinned host memory and the results copied back.
+
+--impl reference: the reference's CPU validation path (FFTW) is absent, so
+the FP64 oracle FFT (oracle/liborc.so, OpenMP over the batch) is timed on the
+host cores on a bounded sample of the same workload.
+
+Multi-GPU (torchrun, WORLD_SIZE > 1): every rank transforms its own arrays
+(weak scaling, no collective on the data path); rank 0 prints the line.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+SIZES = [(4096, 65536), (65536, 4096), (1 << 20, 256)]  # (N, batch): 1 GiB FP16 each
+METRIC = "FFT GFLOP/s (5N log2 N), batched 1D FP16, 1 GiB per size"
+
+
+def flops(n, batch):
+    return 5.0 * n * math.log2(n) * batch
+
+
+def load_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, value):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_fft_sample(seconds_target=12.0, threads=0):
+    """FP64 oracle FFT on the host over a bounded sample of the workload."""
+    import numpy as np
+    import pyoracle as orc
+    orc.build()
+    nt = threads if threads > 0 else orc.max_threads()
+    rng = np.random.default_rng(1)
+    total_flops, total_t = 0.0, 0.0
+    per = seconds_target / len(SIZES)
+    detail = []
+    for n, batch in SIZES:
+        b = max(1, min(batch, (1 << 22) // n))  # 4 Mi points per trial
+        x = (rng.uniform(-1, 1, (b, n)) + 1j * rng.uniform(-1, 1, (b, n)))
+        buf = orc.to_interleaved(x)
+        lib = orc.lib()
+        t_size, f_size, reps = 0.0, 0.0, 0
+        while t_size < per:
+            t0 = time.perf_counter()
+            lib.orc_fft1d(orc._p(buf), n, b, -1, nt)
+            dt = time.perf_counter() - t0
+            t_size += dt
+            f_size += flops(n, b)
+            reps += 1
+        total_flops += f_size
+        total_t += t_size
+        detail.append("N=%d x %d seqs x %d reps" % (n, b, reps))
+    return total_flops / total_t / 1e9, nt, "; ".join(detail)
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    import numpy as np
+    import pyoracle as orc
+    orc.build()
+    nt = orc.max_threads()
+    lib = orc.lib()
+    rng = np.random.default_rng(1)
+    bufs = []
+    for n, batch in SIZES:
+        b = max(1, min(batch, (1 << 21) // n))  # 2 Mi points per size per step
+        x = rng.uniform(-1, 1, (b, n)) + 1j * rng.uniform(-1, 1, (b, n))
+        bufs.append((n, b, orc.to_interleaved(x)))
+
+    def step():
+        f = 0.0
+        for n, b, buf in bufs:
+            lib.orc_fft1d(orc._p(buf), n, b, -1, nt)
+            f += flops(n, b)
+        return f
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    fl = 0.0
+    for _ in range(args.steps):
+        fl += step()
+    dt = time.perf_counter() - t0
+    value = fl / dt / 1e9
+    sample = "; ".join("N=%d x %d seqs" % (n, b) for n, b, _ in bufs)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic uniform[-1,1], seed 1",
+        "config": {"workload": "large-1d-fp16", "sizes": [[n, b] for n, b in SIZES],
+                   "sample_per_step": sample},
+        "cpu_baseline": {"value": value, "unit": "GFLOP/s", "cores": nt, "kind": "port",
+                         "sample": sample + " per step (FP64 oracle FFT; FFTW absent)"},
+        "e2e": {"value": value, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world, rank, local = dist_init()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+
+    import numpy as np
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    import fft_demo_gb300 as tc
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream()
+    peak_gbs, peak_kind = load_peaks()
+
+    plans, xs, ys = [], [], []
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1234 + rank)
+    for n, batch in SIZES:
+        plans.append(tc.plan_1d(n, batch, tc.FP16))
+        x = (torch.rand((batch, n, 2), device=dev, generator=gen) * 2 - 1).half()
+        xs.append(x)
+        ys.append(torch.empty_like(x))
+
+    step_flops = sum(flops(n, b) for n, b in SIZES)
+    step_bytes = sum(2.0 * n * b * 4 for n, b in SIZES)
+
+    launches = [0]
+
+    def step():
+        for p, x, y in zip(plans, xs, ys):
+            p.exec(x, y, direction=tc.FORWARD, stream=stream)
+            launches[0] += tc.last_launch_count()
+
+    for _ in range(args.warmup):
+        step()
+    for p in plans:
+        p.check()
+
+    # --- per-transform device time (CUDA events on the launching stream) ---
+    per_kernel = []
+    for (n, b), p, x, y in zip(SIZES, plans, xs, ys):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 5
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            p.exec(x, y, direction=tc.FORWARD, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        nl = tc.last_launch_count()
+        ms = e0.elapsed_time(e1) / reps
+        per_kernel.append({"n": n, "batch": b, "launches": nl, "ms": ms,
+                           "alg_bytes": 2.0 * n * b * 4, "gflops": flops(n, b) / ms / 1e6})
+
+    # --- timed region: K steps ---
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    barrier(world)
+    torch.cuda.synchronize()
+    launches[0] = 0
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clocks = sampler.stop()
+    ms_total = ev0.elapsed_time(ev1)
+    for p in plans:
+        p.check()
+    ms_total = max_over_ranks(world, ms_total)
+    ms_step = ms_total / args.steps
+    value = step_flops * world / (ms_step * 1e-3) / 1e9
+    gpu_launches = launches[0]
+
+    # --- end to end through the public API with host buffers ---
+    host_in = [torch.empty(x.shape, dtype=x.dtype, pin_memory=True) for x in xs]
+    host_out = [torch.empty(x.shape, dtype=x.dtype, pin_memory=True) for x in xs]
+    for hi, x in zip(host_in, xs):
+        hi.copy_(x)
+    h2d = sum(h.numel() * h.element_size() for h in host_in)
+    d2h = h2d
+
+    def e2e_step():
+        for p, hi, ho, x, y in zip(plans, host_in, host_out, xs, ys):
+            x.copy_(hi, non_blocking=True)
+            p.exec(x, y, direction=tc.FORWARD, stream=stream)
+            ho.copy_(y, non_blocking=True)
+
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_steps = max(2, args.steps // 2)
+    barrier(world)
+    t0 = time.perf_counter()
+    q0 = torch.cuda.Event(enable_timing=True)
+    q1 = torch.cuda.Event(enable_timing=True)
+    q0.record(stream)
+    for _ in range(e2e_steps):
+        e2e_step()
+    q1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(world, q0.elapsed_time(q1)) / e2e_steps
+    e2e_value = step_flops * world / (e2e_ms * 1e-3) / 1e9
+
+    # --- roofline of the dominant transform ---
+    dom = max(per_kernel, key=lambda k: k["ms"])
+    achieved = dom["alg_bytes"] / (dom["ms"] * 1e-3) / 1e9
+    traffic = None
+    tr_path = os.path.join(REPO, "profiles", "traffic.json")
+    if os.path.exists(tr_path):
+        try:
+            traffic = json.load(open(tr_path)).get(str(dom["n"]))
+        except Exception:
+            traffic = None
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, cores, sample = cpu_fft_sample()
+        cpu = {"value": v, "unit": "GFLOP/s", "cores": cores, "kind": "port",
+               "sample": sample + " (FP64 oracle FFT, OpenMP over the batch)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "GFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f16",
+            "data": "synthetic uniform[-1,1] (seeded), inputs larger than L2 (1 GiB per size)",
+            "config": {"workload": "large-1d-fp16", "sizes": [[n, b] for n, b in SIZES],
+                       "precision": "fp16 storage, fp32 accumulate", "l2": "inputs > L2",
+                       "step_bytes_algorithmic": step_bytes},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
+                         "frac": achieved / peak_gbs, "traffic": traffic,
+                         "kernel": "N=%d transform (%d launch%s)" % (
+                             dom["n"], dom["launches"], "es" if dom["launches"] > 1 else ""),
+                         "peak_kind": peak_kind},
+            "per_transform": per_kernel,
+            "hbm_frac_step": step_bytes / (ms_step * 1e-3) / 1e9 / peak_gbs,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": "GFLOP/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": gpu_launches,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    for p in plans:
+        p.destroy()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

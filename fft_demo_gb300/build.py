@@ -17,7 +17,7 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libtcfft_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+NVFLAGS = ["-O3", "-lineinfo", "-std=c++20", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
            "-I" + os.path.join(REPO, "include"), "-I" + CSRC]
 
 

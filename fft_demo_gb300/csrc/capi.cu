@@ -30,32 +30,52 @@ tcfftStatus ret(tcfftStatus s) {
   return s;
 }
 
-PassKernel g_tab[kNumPassKinds][kMaxLogL + 1][kNumTileSel][2];
-int g_occ[kNumPassKinds][kMaxLogL + 1][kNumTileSel][2];
+PassTable g_tab[kNumPrec][kNumPassKinds];
+int g_occ[kNumPrec][kNumPassKinds][kMaxLogL + 1][kNumTileSel][2];
 std::once_flag g_once;
 cudaError_t g_init_err = cudaSuccess;
 int g_num_sms = 0;
 
 void init_registry() {
-  register_row_kernels(g_tab[kPassRow]);
-  register_col_kernels(g_tab[kPassCol]);
-  register_rowt_kernels(g_tab[kPassRowT]);
+  register_row_kernels(g_tab[kPrecF16][kPassRow]);
+  register_col_kernels(g_tab[kPrecF16][kPassCol]);
+  register_rowt_kernels(g_tab[kPrecF16][kPassRowT]);
+  register_split_row_kernels(g_tab[kPrecSplit][kPassRow]);
+  register_split_col_kernels(g_tab[kPrecSplit][kPassCol]);
+  register_split_rowt_kernels(g_tab[kPrecSplit][kPassRowT]);
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+  for (int pr = 0; pr < kNumPrec && e == cudaSuccess; ++pr)
   for (int k = 0; k < kNumPassKinds && e == cudaSuccess; ++k)
     for (int l = 0; l <= kMaxLogL && e == cudaSuccess; ++l)
       for (int t = 0; t < kNumTileSel && e == cudaSuccess; ++t)
         for (int s = 0; s < 2 && e == cudaSuccess; ++s) {
-          PassKernel& pk = g_tab[k][l][t][s];
+          PassKernel& pk = g_tab[pr][k][l][t][s];
           if (!pk.fn) continue;
           e = cudaFuncSetAttribute(pk.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, pk.smem);
           if (e != cudaSuccess) break;
+          e = cudaFuncSetAttribute(pk.fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                   cudaSharedmemCarveoutMaxShared);
+          if (e != cudaSuccess) break;
           int occ = 0;
           e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pk.fn, kPassThreads, pk.smem);
-          // TMEM: 512 columns per SM, a CTA holds Mt/4 columns.
-          const int tmem_limit = 512 / (pk.Mt / 4);
-          g_occ[k][l][t][s] = occ < tmem_limit ? occ : tmem_limit;
+          if (e != cudaSuccess) break;
+          // Own bound from the resources a CTA holds (registers, shared memory,
+          // threads); the larger of this and the runtime's answer is used.
+          cudaFuncAttributes fa;
+          e = cudaFuncGetAttributes(&fa, pk.fn);
+          if (e != cudaSuccess) break;
+          const int regs_per_warp = ((fa.numRegs * 32 + 255) / 256) * 256;
+          const int by_regs = 65536 / (regs_per_warp * (kPassThreads / 32));
+          const int by_smem = (228 * 1024) / (pk.smem + static_cast<int>(fa.sharedSizeBytes) + 1024);
+          const int by_threads = 2048 / kPassThreads;
+          int own = by_regs < by_smem ? by_regs : by_smem;
+          own = own < by_threads ? own : by_threads;
+          if (own > occ) occ = own;
+          // TMEM: 512 columns per SM; a CTA holds Mt/4 (FP16) or Mt/2 (split) columns.
+          const int tmem_limit = 512 / (pk.Mt / (pr == kPrecF16 ? 4 : 2));
+          g_occ[pr][k][l][t][s] = occ < tmem_limit ? occ : tmem_limit;
         }
   g_init_err = e;
 }
@@ -133,15 +153,16 @@ void free_plan(tcfftPlanImpl* p) {
 }
 
 // Launch one pass; grid = persistent CTAs (at most the co-resident count).
-tcfftStatus launch_pass(int kind, int logL, int tile, int sign_idx, const PassArgs& args,
+template <class IO>
+tcfftStatus launch_pass(int prec, int kind, int logL, int tile, int sign_idx, const IO& io, const PassCore& core,
                         cudaStream_t stream) {
-  const PassKernel& pk = g_tab[kind][logL][tile][sign_idx];
+  const PassKernel& pk = g_tab[prec][kind][logL][tile][sign_idx];
   if (!pk.fn) return TCFFT_UNSUPPORTED;
-  const long long ntiles = (args.total_lines + pk.G - 1) / pk.G;
-  long long grid = static_cast<long long>(g_num_sms) * g_occ[kind][logL][tile][sign_idx];
+  const long long ntiles = (io.total_lines + pk.G - 1) / pk.G;
+  long long grid = static_cast<long long>(g_num_sms) * g_occ[prec][kind][logL][tile][sign_idx];
   if (grid < 1) grid = 1;
   if (grid > ntiles) grid = ntiles;
-  void* kargs[] = {const_cast<PassArgs*>(&args)};
+  void* kargs[] = {const_cast<IO*>(&io), const_cast<PassCore*>(&core)};
   cudaError_t e = cudaLaunchKernel(pk.fn, dim3(static_cast<unsigned>(grid)), dim3(kPassThreads), kargs,
                                    static_cast<size_t>(pk.smem), stream);
   if (e != cudaSuccess) return TCFFT_LAUNCH_FAILED;
@@ -151,22 +172,90 @@ tcfftStatus launch_pass(int kind, int logL, int tile, int sign_idx, const PassAr
 
 // Tile size for a contiguous-line pass: small tiles when big ones would
 // leave SMs idle.
-int pick_row_tile(int logL, long long lines) {
-  const PassKernel& small = g_tab[kPassRow][logL][kTileSmall][0];
-  const PassKernel& big = g_tab[kPassRow][logL][kTileBig][0];
+int pick_row_tile(int prec, int logL, long long lines) {
+  const PassKernel& small = g_tab[prec][kPassRow][logL][kTileSmall][0];
+  const PassKernel& big = g_tab[prec][kPassRow][logL][kTileBig][0];
   if (!small.fn) return kTileBig;
   const long long big_tiles = (lines + big.G - 1) / big.G;
   return big_tiles >= 2ll * g_num_sms ? kTileBig : kTileSmall;
 }
 
-PassArgs base_args(tcfftPlanImpl* p, int sign_idx, int logL, float scale) {
-  PassArgs a;
-  std::memset(&a, 0, sizeof(a));
-  a.tw = p->tw[sign_idx][logL];
-  a.bmat = reinterpret_cast<const uint32_t*>(p->bmat[sign_idx]);
-  a.scale = scale;
-  a.err = p->err;
-  return a;
+PassCore make_core(tcfftPlanImpl* p, int sign_idx, int logL) {
+  PassCore c;
+  c.tw = p->tw[sign_idx][logL];
+  c.bmat = reinterpret_cast<const uint32_t*>(p->bmat[sign_idx]);
+  c.err = p->err;
+  return c;
+}
+
+template <class IO, class E>
+IO make_io(const void* in, void* out, long long total_lines, int lps_log2, float scale) {
+  IO io;
+  std::memset(&io, 0, sizeof(io));
+  io.in = static_cast<const E*>(in);
+  io.out = static_cast<E*>(out);
+  io.total_lines = total_lines;
+  io.lps_log2 = lps_log2;
+  io.scale = scale;
+  return io;
+}
+
+// The three pass shapes of a transform, for either storage precision.
+template <template <bool, bool> class IOT, class E>
+tcfftStatus exec_passes(tcfftPlanImpl* p, int prec, const void* in, void* out, int sg, float scale,
+                        cudaStream_t st) {
+  tcfftStatus s = TCFFT_OK;
+  if (p->dims == 1 && p->log_n1 == 0) {
+    const int logL = ilog2ll(p->n);
+    auto io = make_io<IOT<true, true>, E>(in, out, p->batch, 0, scale);
+    io.in_seq = io.out_seq = p->n;
+    io.in_elem = io.out_elem = 1;
+    io.in_contig = io.out_contig = true;
+    io.contig_len = p->n;
+    s = launch_pass(prec, kPassRow, logL, pick_row_tile(prec, logL, p->batch), sg, io, make_core(p, sg, logL), st);
+  } else if (p->dims == 1) {
+    const long long n1 = 1ll << p->log_n1, n2 = 1ll << p->log_n2;
+    // pass 1: length-n1 FFTs down the columns of [n1][n2], times W_N^{n2*k1}
+    auto a = make_io<IOT<false, false>, E>(in, p->ws, p->batch * n2, p->log_n2, 1.0f);
+    a.in_seq = a.out_seq = p->n;
+    a.in_line = a.out_line = 1;
+    a.in_elem = a.out_elem = n2;
+    a.otw.hi = p->otw_hi[sg];
+    a.otw.lo = p->otw_lo[sg];
+    a.otw.shift = p->otw_shift;
+    a.otw.logn = p->otw_logn;
+    s = launch_pass(prec, kPassCol, p->log_n1, kTileBig, sg, a, make_core(p, sg, p->log_n1), st);
+    if (s == TCFFT_OK) {
+      // pass 2: length-n2 FFTs along the rows, row k1 -> X[k1 + n1*k2]
+      auto b = make_io<IOT<true, false>, E>(p->ws, out, p->batch * n1, p->log_n1, scale);
+      b.in_seq = b.out_seq = p->n;
+      b.in_line = n2;
+      b.in_elem = 1;
+      b.out_line = 1;
+      b.out_elem = n1;
+      b.in_contig = true;  // rows k1 of consecutive sequences follow each other
+      b.contig_len = n2;
+      s = launch_pass(prec, kPassRowT, p->log_n2, kTileBig, sg, b, make_core(p, sg, p->log_n2), st);
+    }
+  } else {
+    const int lx = ilog2ll(p->nx), ly = ilog2ll(p->ny);
+    // rows: length ny, contiguous
+    auto a = make_io<IOT<true, true>, E>(in, out, p->batch * p->nx, 0, 1.0f);
+    a.in_seq = a.out_seq = p->ny;
+    a.in_elem = a.out_elem = 1;
+    a.in_contig = a.out_contig = true;
+    a.contig_len = p->ny;
+    s = launch_pass(prec, kPassRow, ly, pick_row_tile(prec, ly, a.total_lines), sg, a, make_core(p, sg, ly), st);
+    if (s == TCFFT_OK) {
+      // columns: length nx, stride ny, in place
+      auto b = make_io<IOT<false, false>, E>(out, out, p->batch * p->ny, ly, scale);
+      b.in_seq = b.out_seq = p->n;
+      b.in_line = b.out_line = 1;
+      b.in_elem = b.out_elem = p->ny;
+      s = launch_pass(prec, kPassCol, lx, kTileBig, sg, b, make_core(p, sg, lx), st);
+    }
+  }
+  return s;
 }
 
 __global__ void digitrev_gather_kernel(const half2* __restrict__ in, half2* __restrict__ out,
@@ -187,6 +276,36 @@ __global__ void digitrev_gather_kernel(const half2* __restrict__ in, half2* __re
   out[i] = in[b * n + pos];
 }
 
+// Storage position of natural index l under a digit-reversal radix list
+// (inverse of the reference's gen_rev permutation).
+__device__ __forceinline__ long long digitrev_pos(long long l, long long n, const int* rad, int nrad) {
+  long long rest = l, span = n, pos = 0;
+  for (int k = nrad - 1; k >= 0; --k) {
+    const int r = rad[k];
+    const long long d = rest % r;
+    rest /= r;
+    span /= r;
+    pos += d * span;
+  }
+  return pos;
+}
+
+struct Radix9 {
+  int r[9];
+};
+
+__global__ void digitrev_gather_2d_kernel(const half2* __restrict__ in, half2* __restrict__ out, int nx, int ny,
+                                          long long total, Radix9 rx, int nrx, Radix9 ry, int nry) {
+  const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
+  if (i >= total) return;
+  const long long plane = static_cast<long long>(nx) * ny;
+  const long long b = i / plane;
+  const int row = static_cast<int>((i % plane) / ny), col = static_cast<int>(i % ny);
+  const long long pr = nrx > 0 ? digitrev_pos(row, nx, rx.r, nrx) : row;
+  const long long pc = nry > 0 ? digitrev_pos(col, ny, ry.r, nry) : col;
+  out[i] = in[b * plane + pr * ny + pc];
+}
+
 }  // namespace
 
 extern "C" {
@@ -196,7 +315,8 @@ tcfftStatus tcfft_plan_1d(tcfftPlan* plan, long long n, long long batch, int pre
   *plan = nullptr;
   if (!is_pow2(n) || n < 16 || n > (1ll << 24) || batch < 1) return ret(TCFFT_INVALID_SIZE);
   if (precision != TCFFT_FP16 && precision != TCFFT_SPLIT_FP32) return ret(TCFFT_INVALID_VALUE);
-  if (precision == TCFFT_SPLIT_FP32) return ret(TCFFT_UNSUPPORTED);
+  // split precision: single pass up to 2^13, two passes up to 2^11 x 2^11
+  if (precision == TCFFT_SPLIT_FP32 && n > (1ll << 22)) return ret(TCFFT_INVALID_SIZE);
   tcfftStatus s = ensure_init();
   if (s != TCFFT_OK) return ret(s);
   tcfftPlanImpl* p = new (std::nothrow) tcfftPlanImpl();
@@ -208,12 +328,14 @@ tcfftStatus tcfft_plan_1d(tcfftPlan* plan, long long n, long long batch, int pre
   const int logn = ilog2ll(n);
   s = common_tables(p);
   if (s == TCFFT_OK) {
-    if (logn <= kMaxLogL) {
+    const int single_max = precision == TCFFT_FP16 ? kMaxLogL : 13;
+    const int pass_max = precision == TCFFT_FP16 ? 12 : 11;
+    if (logn <= single_max) {
       s = ensure_twiddle(p, logn);
     } else {
-      // column pass length 2^a (<= 2^12), row pass length 2^(logn - a) (<= 2^12)
+      // column pass length 2^a, row pass length 2^(logn - a), both <= 2^pass_max
       int a = logn / 2 < 10 ? logn / 2 : 10;
-      if (logn - a > 12) a = logn - 12;
+      if (logn - a > pass_max) a = logn - pass_max;
       p->log_n1 = a;
       p->log_n2 = logn - a;
       s = ensure_twiddle(p, p->log_n1);
@@ -233,7 +355,7 @@ tcfftStatus tcfft_plan_1d(tcfftPlan* plan, long long n, long long batch, int pre
           s = TCFFT_LAUNCH_FAILED;
       }
       if (s == TCFFT_OK) {
-        p->ws_bytes = static_cast<size_t>(n) * static_cast<size_t>(batch) * 4u;
+        p->ws_bytes = static_cast<size_t>(n) * static_cast<size_t>(batch) * (precision == TCFFT_FP16 ? 4u : 8u);
         if (cudaMalloc(&p->ws, p->ws_bytes) != cudaSuccess) s = TCFFT_ALLOC_FAILED;
       }
     }
@@ -253,7 +375,7 @@ tcfftStatus tcfft_plan_2d(tcfftPlan* plan, int nx, int ny, long long batch, int 
   if (!is_pow2(nx) || !is_pow2(ny) || nx < 16 || ny < 16 || nx > 4096 || ny > 4096 || batch < 1)
     return ret(TCFFT_INVALID_SIZE);
   if (precision != TCFFT_FP16 && precision != TCFFT_SPLIT_FP32) return ret(TCFFT_INVALID_VALUE);
-  if (precision == TCFFT_SPLIT_FP32) return ret(TCFFT_UNSUPPORTED);
+  if (precision == TCFFT_SPLIT_FP32 && (nx > 2048 || ny > 8192)) return ret(TCFFT_INVALID_SIZE);
   tcfftStatus s = ensure_init();
   if (s != TCFFT_OK) return ret(s);
   tcfftPlanImpl* p = new (std::nothrow) tcfftPlanImpl();
@@ -290,71 +412,11 @@ tcfftStatus tcfft_exec(tcfftPlan p, const void* in, void* out, int direction, fl
     return ret(TCFFT_INVALID_VALUE);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int sg = direction == TCFFT_FORWARD ? 0 : 1;
-  tcfftStatus s = TCFFT_OK;
-  if (p->dims == 1 && p->log_n1 == 0) {
-    const int logL = ilog2ll(p->n);
-    PassArgs a = base_args(p, sg, logL, scale);
-    a.in = in;
-    a.out = out;
-    a.total_lines = p->batch;
-    a.lines_per_seq = 1;
-    a.in_seq_stride = a.out_seq_stride = p->n;
-    a.in_elem_stride = a.out_elem_stride = 1;
-    s = launch_pass(kPassRow, logL, pick_row_tile(logL, p->batch), sg, a, st);
-  } else if (p->dims == 1) {
-    const long long n1 = 1ll << p->log_n1, n2 = 1ll << p->log_n2;
-    // pass 1: length-n1 FFTs down the columns of [n1][n2], times W_N^{n2*k1}
-    PassArgs a = base_args(p, sg, p->log_n1, 1.0f);
-    a.in = in;
-    a.out = p->ws;
-    a.total_lines = p->batch * n2;
-    a.lines_per_seq = n2;
-    a.in_seq_stride = a.out_seq_stride = p->n;
-    a.in_line_stride = a.out_line_stride = 1;
-    a.in_elem_stride = a.out_elem_stride = n2;
-    a.otw_hi = p->otw_hi[sg];
-    a.otw_lo = p->otw_lo[sg];
-    a.otw_shift = p->otw_shift;
-    a.otw_logn = p->otw_logn;
-    s = launch_pass(kPassCol, p->log_n1, kTileBig, sg, a, st);
-    if (s == TCFFT_OK) {
-      // pass 2: length-n2 FFTs along the rows, row k1 -> X[k1 + n1*k2]
-      PassArgs b = base_args(p, sg, p->log_n2, scale);
-      b.in = p->ws;
-      b.out = out;
-      b.total_lines = p->batch * n1;
-      b.lines_per_seq = n1;
-      b.in_seq_stride = b.out_seq_stride = p->n;
-      b.in_line_stride = n2;
-      b.in_elem_stride = 1;
-      b.out_line_stride = 1;
-      b.out_elem_stride = n1;
-      s = launch_pass(kPassRowT, p->log_n2, kTileBig, sg, b, st);
-    }
-  } else {
-    const int lx = ilog2ll(p->nx), ly = ilog2ll(p->ny);
-    // rows: length ny, contiguous
-    PassArgs a = base_args(p, sg, ly, 1.0f);
-    a.in = in;
-    a.out = out;
-    a.total_lines = p->batch * p->nx;
-    a.lines_per_seq = 1;
-    a.in_seq_stride = a.out_seq_stride = p->ny;
-    a.in_elem_stride = a.out_elem_stride = 1;
-    s = launch_pass(kPassRow, ly, pick_row_tile(ly, a.total_lines), sg, a, st);
-    if (s == TCFFT_OK) {
-      // columns: length nx, stride ny, in place
-      PassArgs b = base_args(p, sg, lx, scale);
-      b.in = out;
-      b.out = out;
-      b.total_lines = p->batch * p->ny;
-      b.lines_per_seq = p->ny;
-      b.in_seq_stride = b.out_seq_stride = p->n;
-      b.in_line_stride = b.out_line_stride = 1;
-      b.in_elem_stride = b.out_elem_stride = p->ny;
-      s = launch_pass(kPassCol, lx, kTileBig, sg, b, st);
-    }
-  }
+  tcfftStatus s;
+  if (p->precision == TCFFT_FP16)
+    s = exec_passes<IoHalf, half2>(p, kPrecF16, in, out, sg, scale, st);
+  else
+    s = exec_passes<IoFloat, float2>(p, kPrecSplit, in, out, sg, scale, st);
   return ret(s);
 }
 
@@ -396,6 +458,50 @@ tcfftStatus tcfft_exec_digitrev(tcfftPlan p, const void* in, void* out, const in
   const int launches_before = n_radices > 0 ? 1 : 0;
   tcfftStatus s = tcfft_exec(p, src, out, TCFFT_FORWARD, 1.0f, stream);
   g_last_launches += launches_before;
+  return ret(s);
+}
+
+tcfftStatus tcfft_exec_digitrev_2d(tcfftPlan p, const void* in, void* out, const int* radices_x, int n_radices_x,
+                                   const int* radices_y, int n_radices_y, void* stream) {
+  g_last_launches = 0;
+  if (!p || !in || !out || n_radices_x < 0 || n_radices_x > 9 || n_radices_y < 0 || n_radices_y > 9 ||
+      (n_radices_x > 0 && !radices_x) || (n_radices_y > 0 && !radices_y))
+    return ret(TCFFT_INVALID_VALUE);
+  if (p->dims != 2 || p->precision != TCFFT_FP16) return ret(TCFFT_UNSUPPORTED);
+  Radix9 rx{}, ry{};
+  long long px = 1, py = 1;
+  for (int i = 0; i < n_radices_x; ++i) {
+    if (radices_x[i] < 2) return ret(TCFFT_INVALID_VALUE);
+    rx.r[i] = radices_x[i];
+    px *= radices_x[i];
+  }
+  for (int i = 0; i < n_radices_y; ++i) {
+    if (radices_y[i] < 2) return ret(TCFFT_INVALID_VALUE);
+    ry.r[i] = radices_y[i];
+    py *= radices_y[i];
+  }
+  if ((n_radices_x > 0 && px != p->nx) || (n_radices_y > 0 && py != p->ny)) return ret(TCFFT_INVALID_SIZE);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const void* src = in;
+  if (n_radices_x > 0 || n_radices_y > 0) {
+    void* dst = out;
+    if (in == out) {
+      if (!p->perm_ws &&
+          cudaMalloc(&p->perm_ws, static_cast<size_t>(p->n) * static_cast<size_t>(p->batch) * 4u) != cudaSuccess)
+        return ret(TCFFT_ALLOC_FAILED);
+      dst = p->perm_ws;
+    }
+    const long long total = p->n * p->batch;
+    const int threads = 256;
+    digitrev_gather_2d_kernel<<<static_cast<unsigned>((total + threads - 1) / threads), threads, 0, st>>>(
+        static_cast<const half2*>(in), static_cast<half2*>(dst), p->nx, p->ny, total, rx, n_radices_x, ry,
+        n_radices_y);
+    if (cudaGetLastError() != cudaSuccess) return ret(TCFFT_LAUNCH_FAILED);
+    src = dst;
+  }
+  const int before = src != in ? 1 : 0;
+  tcfftStatus s = tcfft_exec(p, src, out, TCFFT_FORWARD, 1.0f, stream);
+  g_last_launches += before;
   return ret(s);
 }
 

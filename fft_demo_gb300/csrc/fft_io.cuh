@@ -1,0 +1,123 @@
+// Global-memory IO policies for the pass kernel.
+//
+// A policy tells the pass kernel where line `line`, element `l` lives and how
+// to convert it. Lines are numbered 0..total_lines-1; line -> (sequence,
+// line-in-sequence) uses lines_per_seq = 2^lps_log2. Vector accesses move four
+// complex elements: four consecutive elements of one line ("_l") or the same
+// element of four adjacent lines ("_g", lines adjacent in memory).
+//
+// Interface used by fft_pass_f16:
+//   IN_VEC_L / OUT_VEC_L, Raw, total_lines,
+//   Raw  fetch_l(line, l0, ok) / fetch_g(line0, l, ok)   (issue global loads)
+//   void decode_l(raw, line, l0, v[4]) / decode_g(...)   (to FP32)
+//   void store_row16(line, j, J, v[16])   (outputs l = j + c*J, c = 0..15)
+#pragma once
+#include <cuda_fp16.h>
+#include <cstdint>
+
+#include "fft_tile.cuh"
+
+namespace tcfft {
+
+__device__ __forceinline__ uint4 ldg_nc_v4(const void* p) {
+  uint4 r;
+  asm volatile("ld.global.nc.v4.u32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+               : "l"(p));
+  return r;
+}
+
+__device__ __forceinline__ void stg_v4(void* p, uint4 v) {
+  asm volatile("st.global.v4.u32 [%0], {%1,%2,%3,%4};" ::"l"(p), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
+               : "memory");
+}
+
+__device__ __forceinline__ uint4 pack_h2x4(const float2 (&x)[4]) {
+  uint4 r;
+  __half2 h0 = __floats2half2_rn(x[0].x, x[0].y), h1 = __floats2half2_rn(x[1].x, x[1].y);
+  __half2 h2 = __floats2half2_rn(x[2].x, x[2].y), h3 = __floats2half2_rn(x[3].x, x[3].y);
+  r.x = *reinterpret_cast<uint32_t*>(&h0);
+  r.y = *reinterpret_cast<uint32_t*>(&h1);
+  r.z = *reinterpret_cast<uint32_t*>(&h2);
+  r.w = *reinterpret_cast<uint32_t*>(&h3);
+  return r;
+}
+
+// Outer (four-step) twiddle W_N^{(x*y) mod N} from two FP32 tables:
+// W_N^e = hi[e >> shift] * lo[e & (2^shift - 1)].
+struct OuterTwiddle {
+  const float2* hi = nullptr;
+  const float2* lo = nullptr;
+  int shift = 0;
+  int logn = 0;
+  __device__ __forceinline__ float2 operator()(long long x, long long y) const {
+    const unsigned long long e =
+        (static_cast<unsigned long long>(x) * static_cast<unsigned long long>(y)) & ((1ull << logn) - 1ull);
+    return cmulf(__ldg(hi + (e >> shift)), __ldg(lo + (e & ((1ull << shift) - 1ull))));
+  }
+};
+
+// Interleaved complex half in and out, arbitrary strides (in elements).
+template <bool IN_L, bool OUT_L>
+struct IoHalf {
+  static constexpr bool IN_VEC_L = IN_L;
+  static constexpr bool OUT_VEC_L = OUT_L;
+  using Raw = uint4;
+
+  const half2* in;
+  half2* out;
+  long long total_lines;
+  int lps_log2;
+  long long in_seq, in_line, in_elem;
+  long long out_seq, out_line, out_elem;
+  OuterTwiddle otw;  // applied on store when otw.hi != nullptr: W_N^{li * l}
+  float scale;
+  // Tile contiguity: element (line, l) at in + line * L + l (resp. out), so a
+  // tile of lines moves as one bulk copy. Set by the host.
+  bool in_contig, out_contig;
+  long long contig_len;  // L
+
+  __device__ __forceinline__ const half2* tile_src(long long line0) const { return in + line0 * contig_len; }
+  __device__ __forceinline__ half2* tile_dst(long long line0) const { return out + line0 * contig_len; }
+
+  __device__ __forceinline__ long long in_base(long long line) const {
+    return (line >> lps_log2) * in_seq + (line & ((1ll << lps_log2) - 1)) * in_line;
+  }
+  __device__ __forceinline__ long long out_base(long long line) const {
+    return (line >> lps_log2) * out_seq + (line & ((1ll << lps_log2) - 1)) * out_line;
+  }
+  __device__ __forceinline__ Raw fetch_l(long long line, int l0, bool ok) const {
+    if (!ok || line >= total_lines) return make_uint4(0, 0, 0, 0);
+    return ldg_nc_v4(in + in_base(line) + l0);
+  }
+  __device__ __forceinline__ Raw fetch_g(long long line0, int l, bool ok) const {
+    if (!ok || line0 >= total_lines) return make_uint4(0, 0, 0, 0);
+    return ldg_nc_v4(in + in_base(line0) + static_cast<long long>(l) * in_elem);
+  }
+  __device__ __forceinline__ void decode_l(const Raw& r, long long, int, float2 (&v)[4]) const {
+    unpack_h2x4(r, v);
+  }
+  __device__ __forceinline__ void decode_g(const Raw& r, long long, int, float2 (&v)[4]) const {
+    unpack_h2x4(r, v);
+  }
+  // Outputs l = j + c*J (c = 0..15) of one line. The outer twiddle
+  // W_N^{li*l} is formed as W_N^{li*j} * (W_N^{li*J})^c (FP32 recurrence).
+  __device__ __forceinline__ void store_row16(long long line, int j, int J, float2 (&v)[16]) const {
+    half2* p = out + out_base(line);
+    if (otw.hi) {
+      const long long li = line & ((1ll << lps_log2) - 1);
+      float2 w = otw(li, j);
+      const float2 step = otw(li, J);
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        v[c] = cmulf(v[c], w);
+        w = cmulf(w, step);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 16; ++c)
+      p[static_cast<long long>(j + c * J) * out_elem] = __floats2half2_rn(v[c].x * scale, v[c].y * scale);
+  }
+};
+
+}  // namespace tcfft

@@ -1,0 +1,466 @@
+// Split-precision pass kernel: FP32 data, tensor-core arithmetic on FP16
+// (hi, lo) pairs.
+//
+// Every value v held in shared memory is stored as two FP16 numbers with a
+// per-tile power-of-two scale 2^sigma:
+//     v * 2^sigma = hi + lo * 2^-11,  hi = fp16(v * 2^sigma),
+//                                     lo = fp16((v * 2^sigma - hi) * 2^11)
+// and so is the DFT matrix B = B_hi + B_lo * 2^-11. Each radix-16 stage forms
+//     D_main = A_hi * B_hi                      (TMEM columns  0..31)
+//     D_corr = A_hi * B_lo + A_lo * B_hi        (TMEM columns 32..63)
+// and the epilogue takes A*B = D_main + 2^-11 * D_corr in FP32 (the dropped
+// A_lo * B_lo term is 2^-22 relative). sigma is chosen per tile from the
+// input's largest magnitude (largest value -> <= 2^14 after the radix-T
+// stage); each radix-16 stage scales its output by 2^-4 (its largest possible
+// growth is 16), so no FP16 operand overflows and typical values stay far
+// above FP16's subnormal range.
+#pragma once
+#include "fft_io.cuh"
+#include "fft_tile.cuh"
+
+namespace tcfft {
+
+struct SplitPlanes {
+  uint8_t *rh, *ih, *rl, *il;
+};
+
+__device__ __forceinline__ void split_f(float v, __half& hi, __half& lo) {
+  hi = __float2half_rn(v);
+  lo = __float2half_rn((v - __half2float(hi)) * 2048.0f);
+}
+
+__device__ __forceinline__ void st_pair_split(const SplitPlanes& P, uint32_t off, float2 v) {
+  __half a, b, c, d;
+  split_f(v.x, a, b);
+  split_f(v.y, c, d);
+  *reinterpret_cast<__half*>(P.rh + off) = a;
+  *reinterpret_cast<__half*>(P.rl + off) = b;
+  *reinterpret_cast<__half*>(P.ih + off) = c;
+  *reinterpret_cast<__half*>(P.il + off) = d;
+}
+
+// four consecutive m in one K row (8-byte aligned)
+__device__ __forceinline__ void st_quad_split(const SplitPlanes& P, uint32_t off, const float2 (&x)[4]) {
+  __half rh[4], rl[4], ih[4], il[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    split_f(x[q].x, rh[q], rl[q]);
+    split_f(x[q].y, ih[q], il[q]);
+  }
+  *reinterpret_cast<uint2*>(P.rh + off) = *reinterpret_cast<uint2*>(rh);
+  *reinterpret_cast<uint2*>(P.rl + off) = *reinterpret_cast<uint2*>(rl);
+  *reinterpret_cast<uint2*>(P.ih + off) = *reinterpret_cast<uint2*>(ih);
+  *reinterpret_cast<uint2*>(P.il + off) = *reinterpret_cast<uint2*>(il);
+}
+
+__device__ __forceinline__ float max_abs4(const float2 (&v)[4]) {
+  float m = 0.f;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) m = fmaxf(m, fmaxf(fabsf(v[q].x), fabsf(v[q].y)));
+  return m;
+}
+
+template <int L, int G, bool LINE_MINOR, int s, class IO>
+__device__ __forceinline__ void split_stage_epilogue(const SplitPlanes& P, const float2* __restrict__ tw,
+                                                     uint32_t tbase, int warp, int lane, const IO& io,
+                                                     long long line0, float out_scale) {
+  using Sh = LineShape<L>;
+  using Tl = Tile<L, G, LINE_MINOR>;
+  constexpr int J = Sh::J;
+  constexpr int NG = Tl::Mt / 128;
+  constexpr int Ns = Sh::T << (4 * s);
+  constexpr bool LAST = (s == Sh::S - 1);
+#pragma unroll 1
+  for (int grp = warp >> 2; grp < NG; grp += kPassThreads / 128) {
+    const uint32_t taddr = tbase + (static_cast<uint32_t>(32 * (warp & 3)) << 16) + grp * 64u;
+    uint32_t dm[32], dc[32];
+    tmem_ld_x32(taddr, dm);
+    tmem_ld_x32(taddr + 32u, dc);
+    tmem_ld_wait();
+    const int m = grp * 128 + 32 * (warp & 3) + lane;
+    int g, j;
+    Tl::unpos(m, g, j);
+    float2 v[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c)
+      v[c] = make_float2(fmaf(__uint_as_float(dc[c]), 1.0f / 2048.0f, __uint_as_float(dm[c])),
+                         fmaf(__uint_as_float(dc[16 + c]), 1.0f / 2048.0f, __uint_as_float(dm[16 + c])));
+    if constexpr (LAST) {
+      const long long line = line0 + g;
+      if (line < io.total_lines) {
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+          v[c].x *= out_scale;
+          v[c].y *= out_scale;
+        }
+        io.store_row16(line, j, J, v);
+      }
+    } else {
+      const int a = j / Ns, b = j % Ns;
+      const int lp0 = a * 16 * Ns + b;
+      const int rp = lp0 / J;
+      const int jp0 = lp0 % J;
+      const int e0 = rp * b * (L / (256 * Ns));
+      const int de = rp * (L / 256);
+      const uint32_t krow = (static_cast<uint32_t>(rp) >> 3) * Tl::KSTRIDE + (rp & 7) * 128u;
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        const float2 w = __ldg(tw + e0 + c * de);
+        float2 x = cmulf(v[c], w);
+        x.x *= 0.0625f;  // 2^-4 per stage
+        x.y *= 0.0625f;
+        const uint32_t mp = static_cast<uint32_t>(Tl::pos(g, jp0 + c * Ns));
+        const uint32_t off = krow + (mp >> 6) * 1024u + ((((mp & 63u) >> 3) ^ (rp & 7)) << 4) + (mp & 7u) * 2u;
+        st_pair_split(P, off, x);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Split-precision pass kernel. Same geometry rules as fft_pass_f16, with
+// G * L / 16 in {128, 256, 512} (4 planes + 64 TMEM columns per 128 rows).
+// ---------------------------------------------------------------------------
+template <int L, int G, bool LINE_MINOR, int SIGN, class IO>
+__global__ void __launch_bounds__(kPassThreads, 2) fft_pass_split(const IO io, const PassCore core) {
+  using Sh = LineShape<L>;
+  using Tl = Tile<L, G, LINE_MINOR>;
+  constexpr int T = Sh::T;
+  constexpr int S = Sh::S;
+  constexpr int J = Sh::J;
+  constexpr int Mt = Tl::Mt;
+  constexpr int NG = Mt / 128;
+  constexpr uint32_t PLANE = Tl::PLANE;
+  constexpr uint32_t KSTRIDE = Tl::KSTRIDE;
+  constexpr uint32_t TMEM_COLS = NG * 64;
+  static_assert(Mt % 128 == 0 && Mt <= 512, "tile size");
+  static_assert(TMEM_COLS >= 32 && (TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM columns");
+  static_assert(G % 4 == 0 || IO::IN_VEC_L, "line-vectorised loads need G % 4 == 0");
+  constexpr uint32_t IDESC = make_idesc_f16_f32(128, 32, true, false);
+
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~static_cast<uintptr_t>(1023));
+  SplitPlanes P{smem, smem + PLANE, smem + 2 * PLANE, smem + 3 * PLANE};
+  uint8_t* bhi = smem + 4 * PLANE;  // 2 KB
+  uint8_t* blo = bhi + 2048;        // 2 KB
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(blo + 2048);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(blo + 2048 + 16);
+  int* smax = reinterpret_cast<int*>(blo + 2048 + 32);
+
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5;
+  const int lane = tid & 31;
+
+  for (int i = tid; i < 1024; i += kPassThreads) reinterpret_cast<uint32_t*>(bhi)[i] = __ldg(core.bmat + i);
+  if (tid == 0) mbar_init(mbar, 1);
+  if (warp == 0) {
+    tmem_alloc(tslot, TMEM_COLS);
+    tmem_relinquish();
+  }
+  fence_proxy_async_smem();
+  tc_fence_before_sync();
+  __syncthreads();
+  tc_fence_after_sync();
+  const uint32_t tbase = *tslot;
+  uint32_t phase = 0;
+  bool timed_out = false;
+
+  const long long ntiles = (io.total_lines + G - 1) / G;
+  constexpr int U = T >= 8 ? 1 : 8 / T;
+
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long long line0 = tile * G;
+    if (tid == 0) *smax = 0;
+    __syncthreads();
+
+    // ---- pass A: largest magnitude in the tile (data stays in L1/L2) ----
+    float lmax = 0.f;
+    if constexpr (IO::IN_VEC_L) {
+      constexpr int ITEMS = G * (L / 4);
+#pragma unroll 1
+      for (int base = tid; base < ITEMS; base += kPassThreads * 8) {
+        typename IO::Raw raw[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int it = base + u * kPassThreads;
+          raw[u] = io.fetch_l(line0 + it / (L / 4), (it % (L / 4)) * 4, it < ITEMS);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          float2 v[4];
+          io.decode_l(raw[u], 0, 0, v);
+          lmax = fmaxf(lmax, max_abs4(v));
+        }
+      }
+    } else {
+      constexpr int GQ = G / 4;
+      constexpr int ITEMS = GQ * L;
+#pragma unroll 1
+      for (int base = tid; base < ITEMS; base += kPassThreads * 8) {
+        typename IO::Raw raw[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int it = base + u * kPassThreads;
+          raw[u] = io.fetch_g(line0 + (it % GQ) * 4, it / GQ, it < ITEMS);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          float2 v[4];
+          io.decode_g(raw[u], 0, 0, v);
+          lmax = fmaxf(lmax, max_abs4(v));
+        }
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+    if (lane == 0) atomicMax(smax, __float_as_int(lmax));
+    __syncthreads();
+    const float tmax = __int_as_float(*smax) * static_cast<float>(T);
+    // sigma: largest value after the radix-T stage maps to <= 2^14
+    int sigma = 0;
+    if (tmax > 0.f && isfinite(tmax)) {
+      int ex;
+      frexpf(tmax, &ex);  // tmax = f * 2^ex, f in [0.5, 1)
+      sigma = 14 - ex;
+    }
+    const float in_scale = ldexpf(1.0f, sigma);
+    const float out_scale = ldexpf(1.0f, -(sigma - 4 * (S - 1)));
+
+    // ---- pass B: load, scale, radix-T stage, twiddle, split ----
+    if constexpr (IO::IN_VEC_L) {
+      constexpr int QPL = (L / T) / 4;
+      constexpr int ITEMS = G * QPL;
+#pragma unroll 1
+      for (int base = tid; base < ITEMS; base += kPassThreads * U) {
+        typename IO::Raw raw[U][T];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int it = base + u * kPassThreads;
+#pragma unroll
+          for (int r = 0; r < T; ++r)
+            raw[u][r] = io.fetch_l(line0 + it / QPL, (it % QPL) * 4 + r * (L / T), it < ITEMS);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int it = base + u * kPassThreads;
+          if (it >= ITEMS) break;
+          const int g = it / QPL;
+          const int j0 = (it % QPL) * 4;
+          float2 v[T][4];
+#pragma unroll
+          for (int r = 0; r < T; ++r) {
+            io.decode_l(raw[u][r], line0 + g, j0 + r * (L / T), v[r]);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              v[r][q].x *= in_scale;
+              v[r][q].y *= in_scale;
+            }
+          }
+          if constexpr (T == 1) {
+            if constexpr (!LINE_MINOR && J >= 4) {
+              st_quad_split(P, Tl::off(g, j0), v[0]);
+            } else {
+#pragma unroll
+              for (int q = 0; q < 4; ++q) st_pair_split(P, Tl::off(g, j0 + q), v[0][q]);
+            }
+          } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              float2 t[T];
+#pragma unroll
+              for (int r = 0; r < T; ++r) t[r] = v[r][q];
+              small_dft<T, SIGN>(t);
+              const int j = j0 + q;
+#pragma unroll
+              for (int c = 0; c < T; ++c) {
+                const int lp = j * T + c;
+                const int rp = lp / J, jp = lp % J;
+                const float2 w = __ldg(core.tw + rp * (jp % T) * (L / (16 * T)));
+                st_pair_split(P, Tl::off(g, lp), cmulf(t[c], w));
+              }
+            }
+          }
+        }
+      }
+    } else {
+      constexpr int GQ = G / 4;
+      constexpr int ITEMS = GQ * (L / T);
+#pragma unroll 1
+      for (int base = tid; base < ITEMS; base += kPassThreads * U) {
+        typename IO::Raw raw[U][T];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int it = base + u * kPassThreads;
+#pragma unroll
+          for (int r = 0; r < T; ++r) raw[u][r] = io.fetch_g(line0 + (it % GQ) * 4, it / GQ + r * (L / T), it < ITEMS);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int it = base + u * kPassThreads;
+          if (it >= ITEMS) break;
+          const int j = it / GQ;
+          const int g0 = (it % GQ) * 4;
+          float2 v[T][4];
+#pragma unroll
+          for (int r = 0; r < T; ++r) {
+            io.decode_g(raw[u][r], line0 + g0, j + r * (L / T), v[r]);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              v[r][q].x *= in_scale;
+              v[r][q].y *= in_scale;
+            }
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            float2 t[T];
+#pragma unroll
+            for (int r = 0; r < T; ++r) t[r] = v[r][q];
+            small_dft<T, SIGN>(t);
+#pragma unroll
+            for (int r = 0; r < T; ++r) v[r][q] = t[r];
+          }
+#pragma unroll
+          for (int c = 0; c < T; ++c) {
+            const int lp = j * T + c;
+            float2 x[4] = {v[c][0], v[c][1], v[c][2], v[c][3]};
+            if constexpr (T > 1) {
+              const int rp = lp / J, jp = lp % J;
+              const float2 w = __ldg(core.tw + rp * (jp % T) * (L / (16 * T)));
+#pragma unroll
+              for (int q = 0; q < 4; ++q) x[q] = cmulf(x[q], w);
+            }
+            if constexpr (LINE_MINOR) {
+              st_quad_split(P, Tl::off(g0, lp), x);
+            } else {
+#pragma unroll
+              for (int q = 0; q < 4; ++q) st_pair_split(P, Tl::off(g0 + q, lp), x[q]);
+            }
+          }
+        }
+      }
+    }
+    fence_proxy_async_smem();
+    tc_fence_before_sync();
+    __syncthreads();
+
+    auto run_stage = [&](auto s_const) {
+      constexpr int s = decltype(s_const)::value;
+      if (timed_out) return;
+      if (tid == 0) {
+        tc_fence_after_sync();
+        const uint32_t arh = smem_u32(P.rh), aih = smem_u32(P.ih), arl = smem_u32(P.rl), ail = smem_u32(P.il);
+        const uint64_t bh0 = make_sdesc(smem_u32(bhi), 128u, 512u, kLayoutNone);
+        const uint64_t bh1 = make_sdesc(smem_u32(bhi) + 256u, 128u, 512u, kLayoutNone);
+        const uint64_t bl0 = make_sdesc(smem_u32(blo), 128u, 512u, kLayoutNone);
+        const uint64_t bl1 = make_sdesc(smem_u32(blo) + 256u, 128u, 512u, kLayoutNone);
+#pragma unroll
+        for (int grp = 0; grp < NG; ++grp) {
+          const uint32_t o = grp * 2048u;
+          const uint64_t a_rh = make_sdesc(arh + o, 1024u, KSTRIDE, kLayoutSw128);
+          const uint64_t a_ih = make_sdesc(aih + o, 1024u, KSTRIDE, kLayoutSw128);
+          const uint64_t a_rl = make_sdesc(arl + o, 1024u, KSTRIDE, kLayoutSw128);
+          const uint64_t a_il = make_sdesc(ail + o, 1024u, KSTRIDE, kLayoutSw128);
+          const uint32_t dmain = tbase + grp * 64u, dcorr = dmain + 32u;
+          umma_f16(dmain, a_rh, bh0, IDESC, 0u);
+          umma_f16(dmain, a_ih, bh1, IDESC, 1u);
+          umma_f16(dcorr, a_rh, bl0, IDESC, 0u);
+          umma_f16(dcorr, a_ih, bl1, IDESC, 1u);
+          umma_f16(dcorr, a_rl, bh0, IDESC, 1u);
+          umma_f16(dcorr, a_il, bh1, IDESC, 1u);
+        }
+        umma_commit(mbar);
+      }
+      bool to = !mbar_wait_bounded(mbar, phase & 1u);
+      if (to && lane == 0) atomicOr(core.err, kErrMmaTimeout);
+      phase++;
+      if (__syncthreads_or(to)) {
+        timed_out = true;
+        return;
+      }
+      tc_fence_after_sync();
+      split_stage_epilogue<L, G, LINE_MINOR, s, IO>(P, core.tw, tbase, warp, lane, io, line0, out_scale);
+      fence_proxy_async_smem();
+      tc_fence_before_sync();
+      __syncthreads();
+    };
+    [&]<int... Is>(std::integer_sequence<int, Is...>) {
+      (run_stage(std::integral_constant<int, Is>{}), ...);
+    }(std::make_integer_sequence<int, S>{});
+    if (timed_out) break;
+  }
+
+  tc_fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tbase, TMEM_COLS);
+}
+
+template <int L, int G>
+constexpr int split_smem_bytes() {
+  return 4 * (G * L / 16) * 32 + 4096 + 64 + 1024;
+}
+
+// Interleaved complex float in and out, arbitrary strides (in elements).
+template <bool IN_L, bool OUT_L>
+struct IoFloat {
+  static constexpr bool IN_VEC_L = IN_L;
+  static constexpr bool OUT_VEC_L = OUT_L;
+  struct Raw {
+    uint4 a, b;
+  };
+
+  const float2* in;
+  float2* out;
+  long long total_lines;
+  int lps_log2;
+  long long in_seq, in_line, in_elem;
+  long long out_seq, out_line, out_elem;
+  OuterTwiddle otw;
+  float scale;
+  bool in_contig, out_contig;  // not used by the split kernel (direct loads / stores)
+  long long contig_len;
+
+  __device__ __forceinline__ long long in_base(long long line) const {
+    return (line >> lps_log2) * in_seq + (line & ((1ll << lps_log2) - 1)) * in_line;
+  }
+  __device__ __forceinline__ long long out_base(long long line) const {
+    return (line >> lps_log2) * out_seq + (line & ((1ll << lps_log2) - 1)) * out_line;
+  }
+  __device__ __forceinline__ Raw fetch_l(long long line, int l0, bool ok) const {
+    Raw r{make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
+    if (!ok || line >= total_lines) return r;
+    const float2* p = in + in_base(line) + l0;
+    r.a = ldg_nc_v4(p);
+    r.b = ldg_nc_v4(p + 2);
+    return r;
+  }
+  __device__ __forceinline__ Raw fetch_g(long long line0, int l, bool ok) const {
+    Raw r{make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
+    if (!ok || line0 >= total_lines) return r;
+    const float2* p = in + in_base(line0) + static_cast<long long>(l) * in_elem;
+    r.a = ldg_nc_v4(p);
+    r.b = ldg_nc_v4(p + 2);
+    return r;
+  }
+  __device__ __forceinline__ static void unpack(const Raw& r, float2 (&v)[4]) {
+    v[0] = make_float2(__uint_as_float(r.a.x), __uint_as_float(r.a.y));
+    v[1] = make_float2(__uint_as_float(r.a.z), __uint_as_float(r.a.w));
+    v[2] = make_float2(__uint_as_float(r.b.x), __uint_as_float(r.b.y));
+    v[3] = make_float2(__uint_as_float(r.b.z), __uint_as_float(r.b.w));
+  }
+  __device__ __forceinline__ void decode_l(const Raw& r, long long, int, float2 (&v)[4]) const { unpack(r, v); }
+  __device__ __forceinline__ void decode_g(const Raw& r, long long, int, float2 (&v)[4]) const { unpack(r, v); }
+  // Outer twiddle taken exactly from the tables per element (FP32 accuracy).
+  __device__ __forceinline__ void store_row16(long long line, int j, int J, float2 (&v)[16]) const {
+    float2* p = out + out_base(line);
+    const long long li = line & ((1ll << lps_log2) - 1);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      float2 x = v[c];
+      if (otw.hi) x = cmulf(x, otw(li, j + c * J));
+      p[static_cast<long long>(j + c * J) * out_elem] = make_float2(x.x * scale, x.y * scale);
+    }
+  }
+};
+
+}  // namespace tcfft

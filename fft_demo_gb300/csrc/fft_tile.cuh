@@ -5,11 +5,12 @@
 // (sequence, line, element) strides. One CTA owns a tile of G lines in shared
 // memory and runs the whole length-L transform on it:
 //
-//   load   : global -> registers -> shared. A radix-T first stage
-//            (T = L / 16^S in {1,2,4,8}) runs here on the CUDA cores in FP32,
-//            followed by the twiddle of the first radix-16 stage.
-//   stages : S radix-16 stages. Each is one batch of tcgen05 MMAs
-//            D[m][n] = sum_k A[m][k] B[k][n] with
+//   load   : global -> registers -> shared, 8 x 16-byte loads in flight per
+//            thread. A radix-T first stage (T = L / 16^S in {1,2,4,8}) runs
+//            here on the CUDA cores in FP32, followed by the twiddle of the
+//            first radix-16 stage.
+//   stages : S radix-16 stages (unrolled at compile time). Each is one batch
+//            of tcgen05 MMAs D[m][n] = sum_k A[m][k] B[k][n] with
 //              A = the tile in MN-major 128B-swizzled layout: K row r (0..15)
 //                  holds input r of every butterfly m; real and imaginary
 //                  parts are separate planes (two K=16 MMAs),
@@ -19,8 +20,8 @@
 //            The epilogue reads D (tcgen05.ld), applies the next stage's
 //            twiddle in FP32, rounds once to FP16 and scatters into the next
 //            stage's positions (Stockham autosort order).
-//   store  : shared -> global in natural order, with an optional outer
-//            twiddle (four-step) and scale.
+//   store  : shared -> global in natural order through the IO policy (outer
+//            four-step twiddle, scale, crop, pointwise product ...).
 //
 // Method (radix-16 DFT stages on tensor cores, twiddles between stages,
 // radix-2/4/8 tail on CUDA cores) follows tcfft_half.cu:70-1175 of
@@ -29,6 +30,7 @@
 #pragma once
 #include <cuda_fp16.h>
 #include <cstdint>
+#include <utility>
 
 #include "tc_ptx.cuh"
 
@@ -36,8 +38,15 @@ namespace tcfft {
 
 constexpr int kPassThreads = 256;
 
+__device__ __forceinline__ void unpack_h2x4(const uint4& r, float2 (&v)[4]) {
+  v[0] = __half22float2(*reinterpret_cast<const __half2*>(&r.x));
+  v[1] = __half22float2(*reinterpret_cast<const __half2*>(&r.y));
+  v[2] = __half22float2(*reinterpret_cast<const __half2*>(&r.z));
+  v[3] = __half22float2(*reinterpret_cast<const __half2*>(&r.w));
+}
+
 // Error word bits set by kernels (read back by the host after a launch).
-enum : int { kErrMmaTimeout = 1, kErrBadArgs = 2 };
+enum : int { kErrMmaTimeout = 1, kErrBadArgs = 2, kErrQueueTimeout = 4 };
 
 __host__ __device__ constexpr int ilog2c(long long x) { return x <= 1 ? 0 : 1 + ilog2c(x / 2); }
 
@@ -51,60 +60,18 @@ struct LineShape {
   static_assert(L >= 16, "L >= 16");
 };
 
-struct PassArgs {
-  const void* in;
-  void* out;
-  long long total_lines;    // lines in the whole pass
-  long long lines_per_seq;  // lines per sequence (line index -> (seq, line))
-  long long in_seq_stride, in_line_stride, in_elem_stride;  // in elements
-  long long out_seq_stride, out_line_stride, out_elem_stride;
-  const float2* tw;        // W_L^e (this direction), e in [0, L)
-  const uint32_t* bmat;    // 2 KB image of B for this direction
-  // Outer (four-step) twiddle applied on store: W_N^{(line % lines_per_seq) * l}
-  // factored as otw_hi[e >> otw_shift] * otw_lo[e & ((1 << otw_shift) - 1)],
-  // e = product mod N (N = 2^otw_logn). Null = none.
-  const float2* otw_hi;
-  const float2* otw_lo;
-  int otw_shift;
-  int otw_logn;
-  float scale;  // applied on store (1.0f = none)
+// Per-pass constants shared by every IO policy.
+struct PassCore {
+  const float2* tw;      // W_L^e (this direction), e in [0, L)
+  const uint32_t* bmat;  // 2 KB image of B for this direction
   int* err;
 };
-
-// Row position m (0..Mt-1) of butterfly j of line g.
-template <int L, int G, bool LINE_MINOR>
-__device__ __forceinline__ int bfly_pos(int g, int j) {
-  return LINE_MINOR ? j * G + g : g * LineShape<L>::J + j;
-}
-
-template <int L, int G, bool LINE_MINOR>
-__device__ __forceinline__ void bfly_of_pos(int m, int& g, int& j) {
-  if (LINE_MINOR) {
-    j = m / G;
-    g = m % G;
-  } else {
-    g = m / LineShape<L>::J;
-    j = m % LineShape<L>::J;
-  }
-}
-
-// Byte offset (within a plane) of logical element l of line g.
-template <int L, int G, bool LINE_MINOR>
-__device__ __forceinline__ uint32_t elem_off(int g, int l) {
-  constexpr int Mt = G * L / 16;
-  constexpr uint32_t KSTRIDE = (Mt / 64) * 1024;
-  const int k = l / LineShape<L>::J;
-  const int m = bfly_pos<L, G, LINE_MINOR>(g, l % LineShape<L>::J);
-  return sw128_mn_offset(k, m, 1024u, KSTRIDE);
-}
 
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
-__device__ __forceinline__ float2 h2f(__half2 h) { return __half22float2(h); }
-
-// In-register radix-T DFT (T in {1,2,4,8}), sign = -1 forward, +1 inverse.
+// In-register radix-T DFT (T in {1,2,4,8}), SIGN = -1 forward, +1 inverse.
 template <int T, int SIGN>
 __device__ __forceinline__ void small_dft(float2 (&v)[T]) {
   if constexpr (T == 1) {
@@ -114,7 +81,6 @@ __device__ __forceinline__ void small_dft(float2 (&v)[T]) {
     v[0] = make_float2(a.x + b.x, a.y + b.y);
     v[1] = make_float2(a.x - b.x, a.y - b.y);
   } else if constexpr (T == 4) {
-    // y_c = sum_r v_r * w^{rc}, w = exp(SIGN * i*pi/2)
     float2 s02 = make_float2(v[0].x + v[2].x, v[0].y + v[2].y);
     float2 d02 = make_float2(v[0].x - v[2].x, v[0].y - v[2].y);
     float2 s13 = make_float2(v[1].x + v[3].x, v[1].y + v[3].y);
@@ -127,13 +93,11 @@ __device__ __forceinline__ void small_dft(float2 (&v)[T]) {
     v[3] = make_float2(d02.x - rd13.x, d02.y - rd13.y);
   } else {
     static_assert(T == 8, "tail radix");
-    // radix-8 as 2 x radix-4 (even / odd inputs) + twiddles W8^c
     float2 e[4] = {v[0], v[2], v[4], v[6]};
     float2 o[4] = {v[1], v[3], v[5], v[7]};
     small_dft<4, SIGN>(e);
     small_dft<4, SIGN>(o);
     const float h = 0.70710678118654752f;
-    // W8^c for c = 0..3 (SIGN = -1: exp(-i*pi*c/4))
     const float2 w[4] = {make_float2(1.f, 0.f), make_float2(h, SIGN * h), make_float2(0.f, SIGN * 1.f),
                          make_float2(-h, SIGN * h)};
 #pragma unroll
@@ -145,36 +109,171 @@ __device__ __forceinline__ void small_dft(float2 (&v)[T]) {
   }
 }
 
-template <typename T>
-__device__ __forceinline__ T ldg_vec(const T* p) {
-  return __ldg(p);
+// ---------------------------------------------------------------------------
+// Tile geometry (compile time).
+// ---------------------------------------------------------------------------
+template <int L, int G, bool LINE_MINOR>
+struct Tile {
+  static constexpr int J = LineShape<L>::J;
+  static constexpr int Mt = G * L / 16;
+  static constexpr uint32_t PLANE = Mt * 32;
+  static constexpr uint32_t KSTRIDE = (Mt / 64) * 1024;
+  // column m of butterfly j of line g
+  __device__ __forceinline__ static int pos(int g, int j) { return LINE_MINOR ? j * G + g : g * J + j; }
+  __device__ __forceinline__ static void unpos(int m, int& g, int& j) {
+    if (LINE_MINOR) {
+      j = m / G;
+      g = m % G;
+    } else {
+      g = m / J;
+      j = m % J;
+    }
+  }
+  // byte offset in a plane of logical element l of line g
+  __device__ __forceinline__ static uint32_t off(int g, int l) {
+    return sw128_mn_offset(static_cast<uint32_t>(l / J), static_cast<uint32_t>(pos(g, l % J)), 1024u,
+                           KSTRIDE);
+  }
+};
+
+__device__ __forceinline__ void st_pair(uint8_t* re, uint8_t* im, uint32_t off, float2 v) {
+  *reinterpret_cast<__half*>(re + off) = __float2half_rn(v.x);
+  *reinterpret_cast<__half*>(im + off) = __float2half_rn(v.y);
 }
 
-// Twiddle applied to element l' (logical index written for the next
-// radix-16 stage whose Ns is NSN): W_{16*NSN}^{r' * (j' mod NSN)}.
-template <int L, int NSN>
-__device__ __forceinline__ float2 next_twiddle(const float2* __restrict__ tw, int lp) {
-  constexpr int J = LineShape<L>::J;
-  const int rp = lp / J;
-  const int jp = lp % J;
-  const int e = rp * (jp % NSN) * (L / (16 * NSN));
-  return __ldg(tw + e);
+__device__ __forceinline__ float2 ld_pair(const uint8_t* re, const uint8_t* im, uint32_t off) {
+  return make_float2(__half2float(*reinterpret_cast<const __half*>(re + off)),
+                     __half2float(*reinterpret_cast<const __half*>(im + off)));
 }
 
-__device__ __forceinline__ void st_half_pair(uint8_t* re_plane, uint8_t* im_plane, uint32_t off,
-                                             float2 v) {
-  *reinterpret_cast<__half*>(re_plane + off) = __float2half_rn(v.x);
-  *reinterpret_cast<__half*>(im_plane + off) = __float2half_rn(v.y);
+// four consecutive m (same K row, 8-byte aligned) in one store per plane
+__device__ __forceinline__ void st_quad(uint8_t* re, uint8_t* im, uint32_t off, const float2 (&x)[4]) {
+  __half2 r01 = __floats2half2_rn(x[0].x, x[1].x), r23 = __floats2half2_rn(x[2].x, x[3].x);
+  __half2 i01 = __floats2half2_rn(x[0].y, x[1].y), i23 = __floats2half2_rn(x[2].y, x[3].y);
+  uint2 rr, ii;
+  rr.x = *reinterpret_cast<uint32_t*>(&r01);
+  rr.y = *reinterpret_cast<uint32_t*>(&r23);
+  ii.x = *reinterpret_cast<uint32_t*>(&i01);
+  ii.y = *reinterpret_cast<uint32_t*>(&i23);
+  *reinterpret_cast<uint2*>(re + off) = rr;
+  *reinterpret_cast<uint2*>(im + off) = ii;
 }
 
-// Outer four-step twiddle W_N^{e}, e = (a * b) mod N.
-__device__ __forceinline__ float2 outer_twiddle(const PassArgs& a, long long x, long long y) {
-  const unsigned long long mask = (1ull << a.otw_logn) - 1ull;
-  const unsigned long long e = (static_cast<unsigned long long>(x) * static_cast<unsigned long long>(y)) & mask;
-  const unsigned long long lo_mask = (1ull << a.otw_shift) - 1ull;
-  float2 hi = __ldg(a.otw_hi + (e >> a.otw_shift));
-  float2 lo = __ldg(a.otw_lo + (e & lo_mask));
-  return cmulf(hi, lo);
+__device__ __forceinline__ void ld_quad(const uint8_t* re, const uint8_t* im, uint32_t off, float2 (&x)[4]) {
+  const uint2 rr = *reinterpret_cast<const uint2*>(re + off);
+  const uint2 ii = *reinterpret_cast<const uint2*>(im + off);
+  const float2 r01 = __half22float2(*reinterpret_cast<const __half2*>(&rr.x));
+  const float2 r23 = __half22float2(*reinterpret_cast<const __half2*>(&rr.y));
+  const float2 i01 = __half22float2(*reinterpret_cast<const __half2*>(&ii.x));
+  const float2 i23 = __half22float2(*reinterpret_cast<const __half2*>(&ii.y));
+  x[0] = make_float2(r01.x, i01.x);
+  x[1] = make_float2(r01.y, i01.y);
+  x[2] = make_float2(r23.x, i23.x);
+  x[3] = make_float2(r23.y, i23.y);
+}
+
+// ---------------------------------------------------------------------------
+// One radix-16 stage epilogue (compile-time stage index s).
+//   intermediate stage: D -> x twiddle of the next stage -> FP16 -> next
+//                       stage's positions in shared memory;
+//   last stage        : D -> the IO policy's per-element store, straight to
+//                       global memory (lanes hold adjacent butterflies, or
+//                       adjacent lines in line-minor order, so every warp store
+//                       is one contiguous segment per output index c).
+// ---------------------------------------------------------------------------
+template <int L, int G, bool LINE_MINOR, int s, class IO>
+__device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const float2* __restrict__ tw,
+                                               uint32_t tbase, int warp, int lane, const IO& io,
+                                               long long line0, bool stage_out) {
+  using Sh = LineShape<L>;
+  using Tl = Tile<L, G, LINE_MINOR>;
+  constexpr int J = Sh::J;
+  constexpr int NG = Tl::Mt / 128;
+  constexpr int Ns = Sh::T << (4 * s);
+  constexpr bool LAST = (s == Sh::S - 1);
+#pragma unroll 1
+  for (int grp = warp >> 2; grp < NG; grp += kPassThreads / 128) {
+    uint32_t d[32];
+    tmem_ld_x32(tbase + (static_cast<uint32_t>(32 * (warp & 3)) << 16) + grp * 32u, d);
+    tmem_ld_wait();
+    const int m = grp * 128 + 32 * (warp & 3) + lane;
+    int g, j;
+    Tl::unpos(m, g, j);
+    if constexpr (LAST) {
+      // final outputs X[j + c*J] of line line0 + g
+      const long long line = line0 + g;
+      if (line < io.total_lines) {
+        float2 v[16];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) v[c] = make_float2(__uint_as_float(d[c]), __uint_as_float(d[16 + c]));
+        if (stage_out) {
+          // natural-order half2 copy of the tile for the bulk store
+          uint32_t* row = reinterpret_cast<uint32_t*>(re) + static_cast<uint32_t>(g) * L + j;
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            __half2 h = __floats2half2_rn(v[c].x * io.scale, v[c].y * io.scale);
+            row[c * J] = *reinterpret_cast<uint32_t*>(&h);
+          }
+        } else {
+          io.store_row16(line, j, J, v);
+        }
+      }
+    } else {
+      // output c goes to l' = (j / Ns) * 16Ns + c*Ns + (j % Ns); all 16 land in
+      // the same K row r' = l' / J (16Ns divides J), columns j' = j'0 + c*Ns.
+      const int a = j / Ns, b = j % Ns;
+      const int lp0 = a * 16 * Ns + b;
+      const int rp = lp0 / J;
+      const int jp0 = lp0 % J;
+      // twiddle of the next stage: W_{256 Ns}^{r' (c Ns + b)} = W_L^{e0 + c*de}
+      const int e0 = rp * b * (L / (256 * Ns));
+      const int de = rp * (L / 256);
+      const uint32_t krow = (static_cast<uint32_t>(rp) >> 3) * Tl::KSTRIDE + (rp & 7) * 128u;
+      if constexpr (Ns == 1 && !LINE_MINOR) {
+        // 16 outputs -> 16 consecutive columns: two 16-byte stores per plane
+        uint32_t pr[8], pi[8];
+        // twiddles by recurrence: two table reads per row (FP32 error ~1e-6,
+        // far below the FP16 rounding that follows)
+        float2 w = __ldg(tw + e0);
+        const float2 wstep = __ldg(tw + de);
+#pragma unroll
+        for (int c = 0; c < 16; c += 2) {
+          const float2 w0 = w;
+          const float2 w1 = cmulf(w0, wstep);
+          w = cmulf(w1, wstep);
+          const float2 x0 = cmulf(make_float2(__uint_as_float(d[c]), __uint_as_float(d[16 + c])), w0);
+          const float2 x1 = cmulf(make_float2(__uint_as_float(d[c + 1]), __uint_as_float(d[17 + c])), w1);
+          __half2 hr = __floats2half2_rn(x0.x, x1.x), hi = __floats2half2_rn(x0.y, x1.y);
+          pr[c / 2] = *reinterpret_cast<uint32_t*>(&hr);
+          pi[c / 2] = *reinterpret_cast<uint32_t*>(&hi);
+        }
+        const uint32_t mp = static_cast<uint32_t>(Tl::pos(g, jp0));  // multiple of 16
+        // lanes with bit 2 set store the upper half first, so the 8 lanes of a
+        // quarter-warp cover all 8 16-byte bank groups in each instruction
+        const bool sw = (lane >> 2) & 1;
+        const uint32_t m0 = mp + (sw ? 8u : 0u), m1 = mp + (sw ? 0u : 8u);
+        const uint32_t off0 = krow + (m0 >> 6) * 1024u + ((((m0 & 63u) >> 3) ^ (rp & 7)) << 4);
+        const uint32_t off1 = krow + (m1 >> 6) * 1024u + ((((m1 & 63u) >> 3) ^ (rp & 7)) << 4);
+        const uint4 rlo = make_uint4(pr[0], pr[1], pr[2], pr[3]), rhi = make_uint4(pr[4], pr[5], pr[6], pr[7]);
+        const uint4 ilo = make_uint4(pi[0], pi[1], pi[2], pi[3]), ihi = make_uint4(pi[4], pi[5], pi[6], pi[7]);
+        *reinterpret_cast<uint4*>(re + off0) = sw ? rhi : rlo;
+        *reinterpret_cast<uint4*>(im + off0) = sw ? ihi : ilo;
+        *reinterpret_cast<uint4*>(re + off1) = sw ? rlo : rhi;
+        *reinterpret_cast<uint4*>(im + off1) = sw ? ilo : ihi;
+      } else {
+        float2 w = __ldg(tw + e0);
+        const float2 wstep = __ldg(tw + de);
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+          const float2 x = cmulf(make_float2(__uint_as_float(d[c]), __uint_as_float(d[16 + c])), w);
+          w = cmulf(w, wstep);
+          const uint32_t mp = static_cast<uint32_t>(Tl::pos(g, jp0 + c * Ns));
+          const uint32_t off = krow + (mp >> 6) * 1024u + ((((mp & 63u) >> 3) ^ (rp & 7)) << 4) + (mp & 7u) * 2u;
+          st_pair(re, im, off, x);
+        }
+      }
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -182,48 +281,47 @@ __device__ __forceinline__ float2 outer_twiddle(const PassArgs& a, long long x, 
 //   L          line length
 //   G          lines per tile (G * L / 16 must be 128, 256, 512 or 1024)
 //   LINE_MINOR butterfly order in the tile (true for column passes)
-//   IN_VEC_L   true: vector loads along the line (in_elem_stride == 1);
-//              false: along 4 adjacent lines (in_line_stride == 1)
-//   OUT_VEC_L  same for stores
 //   SIGN       -1 forward, +1 inverse
+//   IO         global-memory policy (see fft_io.cuh)
 // ---------------------------------------------------------------------------
-template <int L, int G, bool LINE_MINOR, bool IN_VEC_L, bool OUT_VEC_L, int SIGN>
-__global__ void __launch_bounds__(kPassThreads, 2) fft_pass_f16(const PassArgs a) {
+template <int L, int G, bool LINE_MINOR, int SIGN, class IO>
+__global__ void __launch_bounds__(kPassThreads, 2) fft_pass_f16(const IO io, const PassCore core) {
   using Sh = LineShape<L>;
+  using Tl = Tile<L, G, LINE_MINOR>;
   constexpr int T = Sh::T;
   constexpr int S = Sh::S;
   constexpr int J = Sh::J;
-  constexpr int Mt = G * L / 16;
+  constexpr int Mt = Tl::Mt;
   constexpr int NG = Mt / 128;
-  constexpr uint32_t PLANE = Mt * 32;  // bytes per plane (16 rows x Mt halves)
-  constexpr uint32_t KSTRIDE = (Mt / 64) * 1024;
+  constexpr uint32_t PLANE = Tl::PLANE;
+  constexpr uint32_t KSTRIDE = Tl::KSTRIDE;
   constexpr uint32_t TMEM_COLS = NG * 32;
   static_assert(Mt % 128 == 0 && Mt <= 1024, "tile size");
   static_assert(TMEM_COLS >= 32 && (TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM columns");
-  static_assert(G % 4 == 0 || IN_VEC_L, "line-vectorised loads need G % 4 == 0");
-  static_assert(G % 4 == 0 || OUT_VEC_L, "line-vectorised stores need G % 4 == 0");
+  static_assert(G % 4 == 0 || IO::IN_VEC_L, "line-vectorised loads need G % 4 == 0");
+  static_assert(G % 4 == 0 || IO::OUT_VEC_L, "line-vectorised stores need G % 4 == 0");
+  static_assert(J >= 4 || !IO::OUT_VEC_L || true, "");
   constexpr uint32_t IDESC = make_idesc_f16_f32(128, 32, true, false);
 
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~static_cast<uintptr_t>(1023));
-  uint8_t* re_plane = smem;
-  uint8_t* im_plane = smem + PLANE;
-  uint8_t* bmat = smem + 2 * PLANE;                               // 2 KB
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(bmat + 2048);      // 8 B
+  uint8_t* re = smem;
+  uint8_t* im = smem + PLANE;
+  uint8_t* bmat = smem + 2 * PLANE;                           // 2 KB
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(bmat + 2048);  // 8 B
+  uint64_t* tma_bar = reinterpret_cast<uint64_t*>(bmat + 2048 + 8);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bmat + 2048 + 16);
-  int* sflag = reinterpret_cast<int*>(bmat + 2048 + 32);
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const int lane = tid & 31;
 
   // ---- one-time setup: B matrix, mbarrier, TMEM ----
-  for (int i = tid; i < 512; i += kPassThreads)
-    reinterpret_cast<uint32_t*>(bmat)[i] = __ldg(a.bmat + i);
+  for (int i = tid; i < 512; i += kPassThreads) reinterpret_cast<uint32_t*>(bmat)[i] = __ldg(core.bmat + i);
   if (tid == 0) {
     mbar_init(mbar, 1);
-    *sflag = 0;
+    mbar_init(tma_bar, 1);
   }
   if (warp == 0) {
     tmem_alloc(tslot, TMEM_COLS);
@@ -234,125 +332,196 @@ __global__ void __launch_bounds__(kPassThreads, 2) fft_pass_f16(const PassArgs a
   __syncthreads();
   tc_fence_after_sync();
   const uint32_t tbase = *tslot;
-  uint32_t phase = 0;
+  uint32_t phase = 0, tma_phase = 0;
+  bool timed_out = false;
+  // Contiguous tiles (element (line, l) at base + line*L + l) move with bulk
+  // TMA copies: one 2*PLANE-byte copy in, one out, through the tile region.
+  const bool tma_in = IO::IN_VEC_L && io.in_contig;
+  const bool stage_out = IO::OUT_VEC_L && io.out_contig && !LINE_MINOR;
 
-  const long long ntiles = (a.total_lines + G - 1) / G;
-  const half2* __restrict__ gin = reinterpret_cast<const half2*>(a.in);
-  half2* __restrict__ gout = reinterpret_cast<half2*>(a.out);
+  const long long ntiles = (io.total_lines + G - 1) / G;
 
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const long long line0 = tile * G;
+    const long long rem = io.total_lines - line0;
+    const int nval = rem < G ? static_cast<int>(rem) : G;
 
     // ================= load (+ radix-T stage) =================
-    if constexpr (IN_VEC_L) {
-      // work item = (line g, quad of butterflies j0..j0+3 of the radix-T stage)
-      constexpr int QPL = (L / T) / 4;  // quads per line
-      for (int it = tid; it < G * QPL; it += kPassThreads) {
+    if (tma_in) {
+      if (tid == 0) {
+        bulk_wait_read_all();  // the previous tile's bulk store has read the region
+        const uint32_t bytes = static_cast<uint32_t>(nval) * L * 4u;
+        mbar_arrive_expect_tx(tma_bar, bytes);
+        bulk_g2s(re, io.tile_src(line0), bytes, tma_bar);
+      }
+      if (!mbar_wait_bounded(tma_bar, tma_phase & 1u)) {
+        timed_out = true;
+        if (lane == 0) atomicOr(core.err, kErrMmaTimeout);
+      }
+      tma_phase++;
+      if (__syncthreads_or(timed_out)) break;
+      // every thread takes its quads of the radix-T stage into registers ...
+      constexpr int QPL = (L / T) / 4;
+      constexpr int ITEMS = G * QPL;
+      constexpr int NU = (ITEMS + kPassThreads - 1) / kPassThreads;
+      uint4 raw[NU][T];
+      const uint32_t* src = reinterpret_cast<const uint32_t*>(re);
+#pragma unroll
+      for (int u = 0; u < NU; ++u) {
+        const int it = tid + u * kPassThreads;
         const int g = it / QPL;
         const int j0 = (it % QPL) * 4;
-        const long long line = line0 + g;
-        float2 v[4][T];
-        if (line < a.total_lines) {
-          const long long seq = line / a.lines_per_seq;
-          const long long li = line % a.lines_per_seq;
-          const half2* base = gin + seq * a.in_seq_stride + li * a.in_line_stride;
 #pragma unroll
-          for (int r = 0; r < T; ++r) {
-            const uint4 raw = *reinterpret_cast<const uint4*>(base + (j0 + r * (L / T)));
-            const half2* hp = reinterpret_cast<const half2*>(&raw);
+        for (int r = 0; r < T; ++r)
+          raw[u][r] = (it < ITEMS && g < nval)
+                          ? *reinterpret_cast<const uint4*>(src + g * L + j0 + r * (L / T))
+                          : make_uint4(0, 0, 0, 0);
+      }
+      __syncthreads();  // ... before the region is overwritten in planar form
 #pragma unroll
-            for (int q = 0; q < 4; ++q) v[q][r] = h2f(hp[q]);
-          }
+      for (int u = 0; u < NU; ++u) {
+        const int it = tid + u * kPassThreads;
+        if (it >= ITEMS) break;
+        const int g = it / QPL;
+        const int j0 = (it % QPL) * 4;
+        if constexpr (T == 1 && !LINE_MINOR && J >= 4) {
+          // de-interleave (re, im) pairs without leaving FP16
+          const uint4 w = raw[u][0];
+          uint2 rr, ii;
+          rr.x = __byte_perm(w.x, w.y, 0x5410);
+          rr.y = __byte_perm(w.z, w.w, 0x5410);
+          ii.x = __byte_perm(w.x, w.y, 0x7632);
+          ii.y = __byte_perm(w.z, w.w, 0x7632);
+          const uint32_t off = Tl::off(g, j0);
+          *reinterpret_cast<uint2*>(re + off) = rr;
+          *reinterpret_cast<uint2*>(im + off) = ii;
         } else {
+          float2 v[T][4];
 #pragma unroll
-          for (int q = 0; q < 4; ++q)
-#pragma unroll
-            for (int r = 0; r < T; ++r) v[q][r] = make_float2(0.f, 0.f);
-        }
-        if constexpr (T == 1) {
-          // four consecutive l -> four consecutive m in the same K row (J >= 4)
-          const uint32_t off = elem_off<L, G, LINE_MINOR>(g, j0);
-          if constexpr (!LINE_MINOR && J >= 4) {
-            __half2 r01 = __floats2half2_rn(v[0][0].x, v[1][0].x);
-            __half2 r23 = __floats2half2_rn(v[2][0].x, v[3][0].x);
-            __half2 i01 = __floats2half2_rn(v[0][0].y, v[1][0].y);
-            __half2 i23 = __floats2half2_rn(v[2][0].y, v[3][0].y);
-            uint2 rr, ii;
-            rr.x = *reinterpret_cast<uint32_t*>(&r01);
-            rr.y = *reinterpret_cast<uint32_t*>(&r23);
-            ii.x = *reinterpret_cast<uint32_t*>(&i01);
-            ii.y = *reinterpret_cast<uint32_t*>(&i23);
-            *reinterpret_cast<uint2*>(re_plane + off) = rr;
-            *reinterpret_cast<uint2*>(im_plane + off) = ii;
-          } else {
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-              st_half_pair(re_plane, im_plane, elem_off<L, G, LINE_MINOR>(g, j0 + q), v[q][0]);
-          }
-        } else {
+          for (int r = 0; r < T; ++r) unpack_h2x4(raw[u][r], v[r]);
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
-            small_dft<T, SIGN>(v[q]);
+            float2 t[T];
+#pragma unroll
+            for (int r = 0; r < T; ++r) t[r] = v[r][q];
+            small_dft<T, SIGN>(t);
+            const int j = j0 + q;
 #pragma unroll
             for (int c = 0; c < T; ++c) {
-              const int lp = (j0 + q) * T + c;
-              float2 w = next_twiddle<L, T>(a.tw, lp);
-              st_half_pair(re_plane, im_plane, elem_off<L, G, LINE_MINOR>(g, lp), cmulf(v[q][c], w));
+              const int lp = j * T + c;
+              float2 x = t[c];
+              if constexpr (T > 1) {
+                const int rp = lp / J, jp = lp % J;
+                x = cmulf(x, __ldg(core.tw + rp * (jp % T) * (L / (16 * T))));
+              }
+              st_pair(re, im, Tl::off(g, lp), x);
+            }
+          }
+        }
+      }
+    } else if constexpr (IO::IN_VEC_L) {
+      // item = (line g, butterflies j0..j0+3 of the radix-T stage); T fetches each
+      constexpr int QPL = (L / T) / 4;
+      constexpr int ITEMS = G * QPL;
+      constexpr int U = T >= 8 ? 1 : 8 / T;
+#pragma unroll 1
+      for (int base = tid; base < ITEMS; base += kPassThreads * U) {
+        typename IO::Raw raw[U][T];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int it = base + u * kPassThreads;
+          const int g = it / QPL;
+          const int j0 = (it % QPL) * 4;
+#pragma unroll
+          for (int r = 0; r < T; ++r)
+            raw[u][r] = io.fetch_l(line0 + g, j0 + r * (L / T), it < ITEMS);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int it = base + u * kPassThreads;
+          if (it >= ITEMS) break;
+          const int g = it / QPL;
+          const int j0 = (it % QPL) * 4;
+          float2 v[T][4];
+#pragma unroll
+          for (int r = 0; r < T; ++r) io.decode_l(raw[u][r], line0 + g, j0 + r * (L / T), v[r]);
+          if constexpr (T == 1) {
+            if constexpr (!LINE_MINOR && J >= 4) {
+              st_quad(re, im, Tl::off(g, j0), v[0]);
+            } else {
+#pragma unroll
+              for (int q = 0; q < 4; ++q) st_pair(re, im, Tl::off(g, j0 + q), v[0][q]);
+            }
+          } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              float2 t[T];
+#pragma unroll
+              for (int r = 0; r < T; ++r) t[r] = v[r][q];
+              small_dft<T, SIGN>(t);
+              // output c of butterfly j -> l' = j*T + c; next stage (Ns = T) twiddle
+              const int j = j0 + q;
+#pragma unroll
+              for (int c = 0; c < T; ++c) {
+                const int lp = j * T + c;
+                const int rp = lp / J, jp = lp % J;
+                const float2 w = __ldg(core.tw + rp * (jp % T) * (L / (16 * T)));
+                st_pair(re, im, Tl::off(g, lp), cmulf(t[c], w));
+              }
             }
           }
         }
       }
     } else {
-      // work item = (quad of adjacent lines g0..g0+3, butterfly j of the radix-T stage)
+      // item = (4 adjacent lines g0..g0+3, butterfly j of the radix-T stage)
       constexpr int GQ = G / 4;
-      for (int it = tid; it < GQ * (L / T); it += kPassThreads) {
-        const int j = it / GQ;
-        const int g0 = (it % GQ) * 4;
-        const long long line = line0 + g0;
-        float2 v[4][T];
-        if (line < a.total_lines) {
-          const long long seq = line / a.lines_per_seq;
-          const long long li = line % a.lines_per_seq;
-          const half2* base = gin + seq * a.in_seq_stride + li * a.in_line_stride;
+      constexpr int ITEMS = GQ * (L / T);
+      constexpr int U = T >= 8 ? 1 : 8 / T;
+#pragma unroll 1
+      for (int base = tid; base < ITEMS; base += kPassThreads * U) {
+        typename IO::Raw raw[U][T];
 #pragma unroll
-          for (int r = 0; r < T; ++r) {
-            const uint4 raw =
-                *reinterpret_cast<const uint4*>(base + static_cast<long long>(j + r * (L / T)) * a.in_elem_stride);
-            const half2* hp = reinterpret_cast<const half2*>(&raw);
+        for (int u = 0; u < U; ++u) {
+          const int it = base + u * kPassThreads;
+          const int j = it / GQ;
+          const int g0 = (it % GQ) * 4;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) v[q][r] = h2f(hp[q]);
-          }
-        } else {
-#pragma unroll
-          for (int q = 0; q < 4; ++q)
-#pragma unroll
-            for (int r = 0; r < T; ++r) v[q][r] = make_float2(0.f, 0.f);
+          for (int r = 0; r < T; ++r) raw[u][r] = io.fetch_g(line0 + g0, j + r * (L / T), it < ITEMS);
         }
 #pragma unroll
-        for (int q = 0; q < 4; ++q) small_dft<T, SIGN>(v[q]);
+        for (int u = 0; u < U; ++u) {
+          const int it = base + u * kPassThreads;
+          if (it >= ITEMS) break;
+          const int j = it / GQ;
+          const int g0 = (it % GQ) * 4;
+          float2 v[T][4];
 #pragma unroll
-        for (int c = 0; c < T; ++c) {
-          const int lp = j * T + c;
-          float2 w = make_float2(1.f, 0.f);
-          if constexpr (T > 1) w = next_twiddle<L, T>(a.tw, lp);
-          if constexpr (LINE_MINOR) {
-            // 4 adjacent lines -> 4 consecutive m in the same K row
-            const uint32_t off = elem_off<L, G, LINE_MINOR>(g0, lp);
-            float2 x0 = cmulf(v[0][c], w), x1 = cmulf(v[1][c], w), x2 = cmulf(v[2][c], w),
-                   x3 = cmulf(v[3][c], w);
-            __half2 r01 = __floats2half2_rn(x0.x, x1.x), r23 = __floats2half2_rn(x2.x, x3.x);
-            __half2 i01 = __floats2half2_rn(x0.y, x1.y), i23 = __floats2half2_rn(x2.y, x3.y);
-            uint2 rr, ii;
-            rr.x = *reinterpret_cast<uint32_t*>(&r01);
-            rr.y = *reinterpret_cast<uint32_t*>(&r23);
-            ii.x = *reinterpret_cast<uint32_t*>(&i01);
-            ii.y = *reinterpret_cast<uint32_t*>(&i23);
-            *reinterpret_cast<uint2*>(re_plane + off) = rr;
-            *reinterpret_cast<uint2*>(im_plane + off) = ii;
-          } else {
+          for (int r = 0; r < T; ++r) io.decode_g(raw[u][r], line0 + g0, j + r * (L / T), v[r]);
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
-              st_half_pair(re_plane, im_plane, elem_off<L, G, LINE_MINOR>(g0 + q, lp), cmulf(v[q][c], w));
+          for (int q = 0; q < 4; ++q) {
+            float2 t[T];
+#pragma unroll
+            for (int r = 0; r < T; ++r) t[r] = v[r][q];
+            small_dft<T, SIGN>(t);
+#pragma unroll
+            for (int r = 0; r < T; ++r) v[r][q] = t[r];
+          }
+#pragma unroll
+          for (int c = 0; c < T; ++c) {
+            const int lp = j * T + c;
+            float2 x[4] = {v[c][0], v[c][1], v[c][2], v[c][3]};
+            if constexpr (T > 1) {
+              const int rp = lp / J, jp = lp % J;
+              const float2 w = __ldg(core.tw + rp * (jp % T) * (L / (16 * T)));
+#pragma unroll
+              for (int q = 0; q < 4; ++q) x[q] = cmulf(x[q], w);
+            }
+            if constexpr (LINE_MINOR) {
+              st_quad(re, im, Tl::off(g0, lp), x);  // 4 adjacent lines -> 4 consecutive m
+            } else {
+#pragma unroll
+              for (int q = 0; q < 4; ++q) st_pair(re, im, Tl::off(g0 + q, lp), x[q]);
+            }
           }
         }
       }
@@ -362,126 +531,49 @@ __global__ void __launch_bounds__(kPassThreads, 2) fft_pass_f16(const PassArgs a
     __syncthreads();
 
     // ================= radix-16 tensor-core stages =================
-    bool timed_out = false;
-#pragma unroll 1
-    for (int s = 0; s < S; ++s) {
+    auto run_stage = [&](auto s_const) {
+      constexpr int s = decltype(s_const)::value;
+      if (timed_out) return;
       if (tid == 0) {
         tc_fence_after_sync();
-        const uint32_t a0 = smem_u32(re_plane), a1 = smem_u32(im_plane), b0 = smem_u32(bmat);
-#pragma unroll 1
+        const uint32_t a0 = smem_u32(re), a1 = smem_u32(im), b0 = smem_u32(bmat);
+        const uint64_t bd0 = make_sdesc(b0, 128u, 512u, kLayoutNone);
+        const uint64_t bd1 = make_sdesc(b0 + 256u, 128u, 512u, kLayoutNone);
+#pragma unroll
         for (int grp = 0; grp < NG; ++grp) {
           const uint64_t ad0 = make_sdesc(a0 + grp * 2048u, 1024u, KSTRIDE, kLayoutSw128);
           const uint64_t ad1 = make_sdesc(a1 + grp * 2048u, 1024u, KSTRIDE, kLayoutSw128);
-          const uint64_t bd0 = make_sdesc(b0, 128u, 512u, kLayoutNone);
-          const uint64_t bd1 = make_sdesc(b0 + 256u, 128u, 512u, kLayoutNone);
           umma_f16(tbase + grp * 32u, ad0, bd0, IDESC, 0u);
           umma_f16(tbase + grp * 32u, ad1, bd1, IDESC, 1u);
         }
         umma_commit(mbar);
       }
-      if (!mbar_wait_bounded(mbar, phase & 1u)) {
-        timed_out = true;
-        if (lane == 0) atomicOr(a.err, kErrMmaTimeout);
-      }
+      bool to = !mbar_wait_bounded(mbar, phase & 1u);
+      if (to && lane == 0) atomicOr(core.err, kErrMmaTimeout);
       phase++;
-      if (__syncthreads_or(timed_out)) {
+      if (__syncthreads_or(to)) {
         timed_out = true;
-        break;
+        return;
       }
       tc_fence_after_sync();
-
-      // Ns of this stage = T * 16^s ; next stage Ns' = 16 * Ns
-      const int Ns = T << (4 * s);
-      const bool last = (s == S - 1);
-      for (int grp = warp >> 2; grp < NG; grp += kPassThreads / 128) {
-        uint32_t d[32];
-        tmem_ld_x32(tbase + (static_cast<uint32_t>(32 * (warp & 3)) << 16) + grp * 32u, d);
-        tmem_ld_wait();
-        const int m = grp * 128 + 32 * (warp & 3) + lane;
-        int g, j;
-        bfly_of_pos<L, G, LINE_MINOR>(m, g, j);
-        if (last) {
-          // final outputs l' = j + c*J: same butterfly column, K row c
-#pragma unroll
-          for (int c = 0; c < 16; ++c) {
-            const uint32_t off = sw128_mn_offset(c, m, 1024u, KSTRIDE);
-            st_half_pair(re_plane, im_plane, off,
-                         make_float2(__uint_as_float(d[c]), __uint_as_float(d[16 + c])));
-          }
-        } else {
-          const int ja = j / Ns, jb = j % Ns;
-          const int NsN = Ns * 16;
-#pragma unroll
-          for (int c = 0; c < 16; ++c) {
-            const int lp = ja * 16 * Ns + c * Ns + jb;
-            const int rp = lp / J, jp = lp % J;
-            const int e = rp * (jp % NsN) * (L / (16 * NsN));
-            const float2 w = __ldg(a.tw + e);
-            const float2 x = cmulf(make_float2(__uint_as_float(d[c]), __uint_as_float(d[16 + c])), w);
-            st_half_pair(re_plane, im_plane, sw128_mn_offset(rp, bfly_pos<L, G, LINE_MINOR>(g, jp), 1024u, KSTRIDE), x);
-          }
-        }
-      }
+      stage_epilogue<L, G, LINE_MINOR, s, IO>(re, im, core.tw, tbase, warp, lane, io, line0, stage_out);
       fence_proxy_async_smem();
       tc_fence_before_sync();
       __syncthreads();
-    }
+    };
+    [&]<int... Is>(std::integer_sequence<int, Is...>) {
+      (run_stage(std::integral_constant<int, Is>{}), ...);
+    }(std::make_integer_sequence<int, S>{});
     if (timed_out) break;
-
-    // ================= store =================
-    const bool do_otw = a.otw_hi != nullptr;
-    if constexpr (OUT_VEC_L) {
-      constexpr int QPL = L / 4;
-      for (int it = tid; it < G * QPL; it += kPassThreads) {
-        const int g = it / QPL;
-        const int l0 = (it % QPL) * 4;
-        const long long line = line0 + g;
-        if (line >= a.total_lines) continue;
-        const long long seq = line / a.lines_per_seq;
-        const long long li = line % a.lines_per_seq;
-        half2 o[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const uint32_t off = elem_off<L, G, LINE_MINOR>(g, l0 + q);
-          float2 x = make_float2(__half2float(*reinterpret_cast<const __half*>(re_plane + off)),
-                                 __half2float(*reinterpret_cast<const __half*>(im_plane + off)));
-          if (do_otw) x = cmulf(x, outer_twiddle(a, li, l0 + q));
-          x.x *= a.scale;
-          x.y *= a.scale;
-          o[q] = __floats2half2_rn(x.x, x.y);
-        }
-        half2* dst = gout + seq * a.out_seq_stride + li * a.out_line_stride + l0;
-        *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<uint4*>(o);
-      }
-    } else {
-      constexpr int GQ = G / 4;
-      for (int it = tid; it < GQ * L; it += kPassThreads) {
-        const int l = it / GQ;
-        const int g0 = (it % GQ) * 4;
-        const long long line = line0 + g0;
-        if (line >= a.total_lines) continue;
-        const long long seq = line / a.lines_per_seq;
-        const long long li = line % a.lines_per_seq;
-        half2 o[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const uint32_t off = elem_off<L, G, LINE_MINOR>(g0 + q, l);
-          float2 x = make_float2(__half2float(*reinterpret_cast<const __half*>(re_plane + off)),
-                                 __half2float(*reinterpret_cast<const __half*>(im_plane + off)));
-          if (do_otw) x = cmulf(x, outer_twiddle(a, li + q, l));
-          x.x *= a.scale;
-          x.y *= a.scale;
-          o[q] = __floats2half2_rn(x.x, x.y);
-        }
-        half2* dst = gout + seq * a.out_seq_stride + li * a.out_line_stride +
-                     static_cast<long long>(l) * a.out_elem_stride;
-        *reinterpret_cast<uint4*>(dst) = *reinterpret_cast<uint4*>(o);
-      }
+    if (stage_out && tid == 0) {
+      // the last stage left the tile in natural order: one bulk store
+      bulk_s2g(io.tile_dst(line0), re, static_cast<uint32_t>(nval) * L * 4u);
+      bulk_commit();
     }
-    __syncthreads();
   }
 
   // ---- teardown ----
+  if (tid == 0) bulk_wait_all();
   tc_fence_before_sync();
   __syncthreads();
   if (warp == 0) tmem_dealloc(tbase, TMEM_COLS);

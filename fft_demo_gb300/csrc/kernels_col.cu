@@ -4,7 +4,7 @@
 
 namespace tcfft {
 
-void register_col_kernels(PassKernel (&tab)[kMaxLogL + 1][kNumTileSel][2]) {
+void register_col_kernels(PassTable& tab) {
   fill_entry<16, 1024, true, false, false>(tab, kTileBig);
   fill_entry<32, 1024, true, false, false>(tab, kTileBig);
   fill_entry<64, 1024, true, false, false>(tab, kTileBig);

@@ -4,7 +4,7 @@
 
 namespace tcfft {
 
-void register_row_kernels(PassKernel (&tab)[kMaxLogL + 1][kNumTileSel][2]) {
+void register_row_kernels(PassTable& tab) {
   fill_entry<16, 128, false, true, true>(tab, kTileSmall);
   fill_entry<32, 128, false, true, true>(tab, kTileSmall);
   fill_entry<64, 128, false, true, true>(tab, kTileSmall);

@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "fft_io.cuh"
+#include "fft_split.cuh"
 #include "fft_tile.cuh"
 
 namespace tcfft {
@@ -14,8 +16,11 @@ enum PassKind : int {
   kNumPassKinds = 3
 };
 
-// Tile-size variants: Mt = butterflies per radix-16 stage in one tile.
-enum TileSel : int { kTileSmall = 0 /* Mt = 128 */, kTileBig = 1 /* Mt = 1024 */, kNumTileSel = 2 };
+// Tile-size variants: Mt = butterflies per radix-16 stage in one tile
+// (FP16: small 128, big 1024; split: small 128, big 512).
+enum TileSel : int { kTileSmall = 0, kTileBig = 1, kNumTileSel = 2 };
+
+enum PrecSel : int { kPrecF16 = 0, kPrecSplit = 1, kNumPrec = 2 };
 
 constexpr int kMinLogL = 4;
 constexpr int kMaxLogL = 14;
@@ -27,13 +32,15 @@ struct PassKernel {
   int Mt = 0;  // butterflies per stage per tile
 };
 
-// sign: 0 = forward, 1 = inverse
-const PassKernel& pass_kernel(int kind, int logL, int tile, int sign);
+using PassTable = PassKernel[kMaxLogL + 1][kNumTileSel][2];
 
 // Filled by the instantiation units.
-void register_row_kernels(PassKernel (&tab)[kMaxLogL + 1][kNumTileSel][2]);
-void register_col_kernels(PassKernel (&tab)[kMaxLogL + 1][kNumTileSel][2]);
-void register_rowt_kernels(PassKernel (&tab)[kMaxLogL + 1][kNumTileSel][2]);
+void register_row_kernels(PassTable& tab);
+void register_col_kernels(PassTable& tab);
+void register_rowt_kernels(PassTable& tab);
+void register_split_row_kernels(PassTable& tab);
+void register_split_col_kernels(PassTable& tab);
+void register_split_rowt_kernels(PassTable& tab);
 
 template <int L, int Mt>
 constexpr int tile_lines() {
@@ -41,13 +48,30 @@ constexpr int tile_lines() {
 }
 
 template <int L, int Mt, bool LINE_MINOR, bool IN_VEC_L, bool OUT_VEC_L>
-void fill_entry(PassKernel (&tab)[kMaxLogL + 1][kNumTileSel][2], int tile) {
+void fill_entry(PassTable& tab, int tile) {
   constexpr int G = tile_lines<L, Mt>();
   constexpr int LOG = ilog2c(L);
   const int smem = pass_smem_bytes<L, G>();
   PassKernel f, i;
-  f.fn = reinterpret_cast<const void*>(&fft_pass_f16<L, G, LINE_MINOR, IN_VEC_L, OUT_VEC_L, -1>);
-  i.fn = reinterpret_cast<const void*>(&fft_pass_f16<L, G, LINE_MINOR, IN_VEC_L, OUT_VEC_L, +1>);
+  using IO = IoHalf<IN_VEC_L, OUT_VEC_L>;
+  f.fn = reinterpret_cast<const void*>(&fft_pass_f16<L, G, LINE_MINOR, -1, IO>);
+  i.fn = reinterpret_cast<const void*>(&fft_pass_f16<L, G, LINE_MINOR, +1, IO>);
+  f.smem = i.smem = smem;
+  f.G = i.G = G;
+  f.Mt = i.Mt = Mt;
+  tab[LOG][tile][0] = f;
+  tab[LOG][tile][1] = i;
+}
+
+template <int L, int Mt, bool LINE_MINOR, bool IN_VEC_L, bool OUT_VEC_L>
+void fill_split_entry(PassTable& tab, int tile) {
+  constexpr int G = tile_lines<L, Mt>();
+  constexpr int LOG = ilog2c(L);
+  const int smem = split_smem_bytes<L, G>();
+  PassKernel f, i;
+  using IO = IoFloat<IN_VEC_L, OUT_VEC_L>;
+  f.fn = reinterpret_cast<const void*>(&fft_pass_split<L, G, LINE_MINOR, -1, IO>);
+  i.fn = reinterpret_cast<const void*>(&fft_pass_split<L, G, LINE_MINOR, +1, IO>);
   f.smem = i.smem = smem;
   f.G = i.G = G;
   f.Mt = i.Mt = Mt;

@@ -24,6 +24,8 @@
  *                   TensorCoreFFTExec tensorcore_fft_conv2d_kernel.cu:1495,1526
  *   tcfft_exec_digitrev  tcfftExec on the digit-reversed input that setup()
  *                   prepares (tcfft_half.cu:1376-1394, gen_rev :1351)
+ *   tcfft_exec_digitrev_2d  tcfftExec_2d on setup_2d()'s input
+ *                   (tcfft_half_2d.cu:1128, :1253)
  */
 #ifndef TCFFT_GB300_H
 #define TCFFT_GB300_H
@@ -74,6 +76,13 @@ tcfftStatus tcfft_exec(tcfftPlan plan, const void *in, void *out, int direction,
  * in place allowed. 1D FP16 plans only. */
 tcfftStatus tcfft_exec_digitrev(tcfftPlan plan, const void *in, void *out, const int *radices,
                                 int n_radices, void *stream);
+
+/* 2D forward transform of input whose rows are stored in the digit-reversed
+ * order of radices_x and whose elements within a row follow radices_y, as the
+ * reference's setup_2d() prepares (tcfft_half_2d.cu:1253-1273). 2D FP16 plans. */
+tcfftStatus tcfft_exec_digitrev_2d(tcfftPlan plan, const void *in, void *out, const int *radices_x,
+                                   int n_radices_x, const int *radices_y, int n_radices_y,
+                                   void *stream);
 
 /* Synchronise `stream` and report any error a kernel of this plan flagged
  * (e.g. TCFFT_TIMEOUT from a bounded wait). Clears the flag. */
