@@ -20,6 +20,8 @@ OK, INVALID_SIZE, UNSUPPORTED, ALLOC_FAILED, LAUNCH_FAILED, TIMEOUT, CAPACITY, I
 FP16, SPLIT_FP32 = 0, 1
 # tcfftDirection
 FORWARD, INVERSE = -1, 1
+# tcfftConvMode
+CONV_VALID_CORR, CONV_SAME, CONV_FULL = 0, 1, 2
 
 _lib = None
 
@@ -56,6 +58,12 @@ def _declare(L):
         "tcfft_get_last_error": (i, []),
         "tcfft_status_string": (ctypes.c_char_p, [i]),
         "tcfft_last_launch_count": (i, []),
+        "tcfft_conv2d_plan": (i, [ctypes.POINTER(vp), i, i, i, i, i, i, i, i, ll]),
+        "tcfft_conv2d_set_filters": (i, [vp, vp, vp]),
+        "tcfft_conv2d_exec": (i, [vp, vp, vp, ll, vp]),
+        "tcfft_conv2d_shape": (i, [vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)]),
+        "tcfft_conv2d_check": (i, [vp, vp]),
+        "tcfft_conv2d_destroy": (i, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -166,3 +174,63 @@ def plan_1d(n, batch=1, precision=FP16):
 
 def plan_2d(nx, ny, batch=1, precision=FP16):
     return Plan(batch=batch, precision=precision, shape2d=(nx, ny))
+
+
+class Conv2d:
+    """2D FFT convolution plan (fft_conv2d_half / convolve_direct_fft equivalent).
+
+    images [batch][S][sy][sx] real on the GPU (float16 for FP16 plans, float32
+    for split plans); filters [F][S][fy][fx] float32 on the GPU, transformed
+    once by set_filters and kept resident; exec returns [batch][F][oy][ox].
+    """
+
+    def __init__(self, S, F, sy, sx, fy, fx, mode=CONV_VALID_CORR, precision=FP16, max_batch=1):
+        self._h = ctypes.c_void_p()
+        self.S, self.F, self.sy, self.sx, self.fy, self.fx = S, F, sy, sx, fy, fx
+        self.mode, self.precision, self.max_batch = mode, precision, max_batch
+        _check(lib().tcfft_conv2d_plan(ctypes.byref(self._h), S, F, sy, sx, fy, fx, mode, precision,
+                                       max_batch), "conv2d_plan")
+        r, c, p = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(lib().tcfft_conv2d_shape(self._h, ctypes.byref(r), ctypes.byref(c), ctypes.byref(p)))
+        self.out_rows, self.out_cols, self.padded = r.value, c.value, p.value
+
+    @property
+    def dtype(self):
+        import torch
+        return torch.float16 if self.precision == FP16 else torch.float32
+
+    def set_filters(self, filters, stream=None):
+        import torch
+        if filters.dtype != torch.float32 or not filters.is_cuda or not filters.is_contiguous() or \
+                filters.numel() != self.F * self.S * self.fy * self.fx:
+            raise TcfftError(INVALID_VALUE, "filters: contiguous float32 CUDA [F][S][fy][fx]")
+        self._filters = filters
+        _check(lib().tcfft_conv2d_set_filters(self._h, _ptr(filters), _stream_ptr(stream)),
+               "set_filters")
+
+    def exec(self, images, out=None, stream=None):
+        import torch
+        batch = images.numel() // (self.S * self.sy * self.sx)
+        if images.dtype != self.dtype or not images.is_cuda or not images.is_contiguous() or \
+                batch * self.S * self.sy * self.sx != images.numel():
+            raise TcfftError(INVALID_VALUE, "images: contiguous %s CUDA [batch][S][sy][sx]" % self.dtype)
+        if out is None:
+            out = torch.empty((batch, self.F, self.out_rows, self.out_cols), dtype=self.dtype,
+                              device=images.device)
+        _check(lib().tcfft_conv2d_exec(self._h, _ptr(images), _ptr(out), batch, _stream_ptr(stream)),
+               "conv2d_exec")
+        return out
+
+    def check(self, stream=None):
+        _check(lib().tcfft_conv2d_check(self._h, _stream_ptr(stream)), "conv2d_check")
+
+    def destroy(self):
+        if self._h:
+            lib().tcfft_conv2d_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass

@@ -1,0 +1,139 @@
+"""Autotuner: per-size tile variants for the pass kernels, measured and cached.
+
+A transform is a chain of passes (row / column / transposing row). Each pass
+kind has tile variants (tcfft_pass_info: lines per tile, CTAs per SM). For a
+workload the tuner times every variant of every pass of the transform with
+CUDA events, keeps the fastest and writes the choices to a JSON cache keyed by
+device name, precision, pass kind and log2 of the pass length. Loading the
+cache re-applies the choices through tcfft_tune_set.
+
+Cache path: $TCFFT_TUNE_CACHE, default ~/.cache/tcfft_gb300/tune.json.
+"""
+import ctypes
+import json
+import math
+import os
+
+from . import FP16, FORWARD, lib, plan_1d, plan_2d, _check
+
+PASS_ROW, PASS_COL, PASS_ROWT = 0, 1, 2
+TILE_SMALL, TILE_BIG, TILE_MID = 0, 1, 2
+TILE_NAMES = {TILE_SMALL: "small", TILE_BIG: "big", TILE_MID: "mid"}
+
+
+def cache_path():
+    return os.environ.get("TCFFT_TUNE_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "tcfft_gb300", "tune.json"))
+
+
+def _device_name():
+    import torch
+    return torch.cuda.get_device_name(0)
+
+
+def passes_of(n, precision, dims=1, shape2d=None):
+    """(pass kind, log2 length) of each pass the library runs for a transform."""
+    if dims == 2:
+        nx, ny = shape2d
+        return [(PASS_ROW, int(math.log2(ny))), (PASS_COL, int(math.log2(nx)))]
+    logn = int(math.log2(n))
+    single_max = 14 if precision == FP16 else 13
+    pass_max = 12 if precision == FP16 else 11
+    if logn <= single_max:
+        return [(PASS_ROW, logn)]
+    a = min(logn // 2, 10)
+    if logn - a > pass_max:
+        a = logn - pass_max
+    return [(PASS_COL, a), (PASS_ROWT, logn - a)]
+
+
+def variants(precision, kind, logl):
+    out = []
+    for t in (TILE_SMALL, TILE_BIG, TILE_MID):
+        g, c, s = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        st = lib().tcfft_pass_info(precision, kind, logl, t, ctypes.byref(g), ctypes.byref(c),
+                                   ctypes.byref(s))
+        if st == 0:
+            out.append(t)
+    return out
+
+
+def set_tile(precision, kind, logl, tile):
+    _check(lib().tcfft_tune_set(precision, kind, logl, tile), "tune_set")
+
+
+def _time_exec(plan, x, y, reps):
+    import torch
+    for _ in range(2):
+        plan.exec(x, y, direction=FORWARD)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        plan.exec(x, y, direction=FORWARD)
+    e1.record()
+    torch.cuda.synchronize()
+    plan.check()
+    return e0.elapsed_time(e1) / reps
+
+
+def tune(n, batch, precision=FP16, shape2d=None, reps=10, verbose=False):
+    """Tune every pass of one transform; returns {(kind, logl): tile}."""
+    import torch
+    lib().tcfft_tune_set.argtypes = [ctypes.c_int] * 4
+    lib().tcfft_pass_info.argtypes = [ctypes.c_int] * 4 + [ctypes.c_void_p] * 3
+    dims = 2 if shape2d else 1
+    plan = plan_2d(shape2d[0], shape2d[1], batch, precision) if shape2d else plan_1d(n, batch, precision)
+    total = plan.n * batch
+    dt = torch.float16 if precision == FP16 else torch.float32
+    x = (torch.rand((total, 2), device="cuda") * 2 - 1).to(dt)
+    y = torch.empty_like(x)
+    chosen = {}
+    for kind, logl in passes_of(plan.n, precision, dims, shape2d):
+        best, best_ms = None, float("inf")
+        for t in variants(precision, kind, logl):
+            set_tile(precision, kind, logl, t)
+            ms = _time_exec(plan, x, y, reps)
+            if verbose:
+                print("  pass kind=%d log2L=%d tile=%s: %.4f ms" % (kind, logl, TILE_NAMES[t], ms))
+            if ms < best_ms:
+                best, best_ms = t, ms
+        set_tile(precision, kind, logl, best)
+        chosen[(kind, logl)] = best
+    plan.destroy()
+    return chosen
+
+
+def save(choices, precision, path=None):
+    path = path or cache_path()
+    data = {}
+    if os.path.exists(path):
+        try:
+            data = json.load(open(path))
+        except Exception:
+            data = {}
+    dev = data.setdefault(_device_name(), {})
+    for (kind, logl), tile in choices.items():
+        dev["%d/%d/%d" % (precision, kind, logl)] = tile
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    with open(path, "w") as f:
+        json.dump(data, f, indent=1, sort_keys=True)
+    return path
+
+
+def load(path=None):
+    """Apply cached choices for this device; returns how many were applied."""
+    path = path or cache_path()
+    if not os.path.exists(path):
+        return 0
+    try:
+        data = json.load(open(path)).get(_device_name(), {})
+    except Exception:
+        return 0
+    lib().tcfft_tune_set.argtypes = [ctypes.c_int] * 4
+    n = 0
+    for key, tile in data.items():
+        prec, kind, logl = (int(v) for v in key.split("/"))
+        if lib().tcfft_tune_set(prec, kind, logl, int(tile)) == 0:
+            n += 1
+    return n

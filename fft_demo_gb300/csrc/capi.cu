@@ -35,6 +35,15 @@ int g_occ[kNumPrec][kNumPassKinds][kMaxLogL + 1][kNumTileSel][2];
 std::once_flag g_once;
 cudaError_t g_init_err = cudaSuccess;
 int g_num_sms = 0;
+// Tile variant per (precision, pass kind, log2 length); -1 = built-in choice.
+// Written by tcfft_tune_set (the autotuner), read at every launch.
+int g_tune[kNumPrec][kNumPassKinds][kMaxLogL + 1];
+std::once_flag g_tune_once;
+void tune_reset() {
+  for (auto& a : g_tune)
+    for (auto& b : a)
+      for (int& c : b) c = -1;
+}
 
 void init_registry() {
   register_row_kernels(g_tab[kPrecF16][kPassRow]);
@@ -170,12 +179,15 @@ tcfftStatus launch_pass(int prec, int kind, int logL, int tile, int sign_idx, co
   return TCFFT_OK;
 }
 
-// Tile size for a contiguous-line pass: small tiles when big ones would
-// leave SMs idle.
-int pick_row_tile(int prec, int logL, long long lines) {
-  const PassKernel& small = g_tab[prec][kPassRow][logL][kTileSmall][0];
-  const PassKernel& big = g_tab[prec][kPassRow][logL][kTileBig][0];
-  if (!small.fn) return kTileBig;
+// Tile variant for a pass: the tuned choice if one is set and built,
+// otherwise big tiles, or small ones when big ones would leave SMs idle.
+int choose_tile(int prec, int kind, int logL, long long lines) {
+  std::call_once(g_tune_once, tune_reset);
+  const int t = g_tune[prec][kind][logL];
+  if (t >= 0 && t < kNumTileSel && g_tab[prec][kind][logL][t][0].fn) return t;
+  const PassKernel& small = g_tab[prec][kind][logL][kTileSmall][0];
+  const PassKernel& big = g_tab[prec][kind][logL][kTileBig][0];
+  if (!small.fn || !big.fn) return kTileBig;
   const long long big_tiles = (lines + big.G - 1) / big.G;
   return big_tiles >= 2ll * g_num_sms ? kTileBig : kTileSmall;
 }
@@ -212,7 +224,7 @@ tcfftStatus exec_passes(tcfftPlanImpl* p, int prec, const void* in, void* out, i
     io.in_elem = io.out_elem = 1;
     io.in_contig = io.out_contig = true;
     io.contig_len = p->n;
-    s = launch_pass(prec, kPassRow, logL, pick_row_tile(prec, logL, p->batch), sg, io, make_core(p, sg, logL), st);
+    s = launch_pass(prec, kPassRow, logL, choose_tile(prec, kPassRow, logL, p->batch), sg, io, make_core(p, sg, logL), st);
   } else if (p->dims == 1) {
     const long long n1 = 1ll << p->log_n1, n2 = 1ll << p->log_n2;
     // pass 1: length-n1 FFTs down the columns of [n1][n2], times W_N^{n2*k1}
@@ -224,7 +236,8 @@ tcfftStatus exec_passes(tcfftPlanImpl* p, int prec, const void* in, void* out, i
     a.otw.lo = p->otw_lo[sg];
     a.otw.shift = p->otw_shift;
     a.otw.logn = p->otw_logn;
-    s = launch_pass(prec, kPassCol, p->log_n1, kTileBig, sg, a, make_core(p, sg, p->log_n1), st);
+    s = launch_pass(prec, kPassCol, p->log_n1, choose_tile(prec, kPassCol, p->log_n1, a.total_lines), sg, a,
+                    make_core(p, sg, p->log_n1), st);
     if (s == TCFFT_OK) {
       // pass 2: length-n2 FFTs along the rows, row k1 -> X[k1 + n1*k2]
       auto b = make_io<IOT<true, false>, E>(p->ws, out, p->batch * n1, p->log_n1, scale);
@@ -235,7 +248,8 @@ tcfftStatus exec_passes(tcfftPlanImpl* p, int prec, const void* in, void* out, i
       b.out_elem = n1;
       b.in_contig = true;  // rows k1 of consecutive sequences follow each other
       b.contig_len = n2;
-      s = launch_pass(prec, kPassRowT, p->log_n2, kTileBig, sg, b, make_core(p, sg, p->log_n2), st);
+      s = launch_pass(prec, kPassRowT, p->log_n2, choose_tile(prec, kPassRowT, p->log_n2, b.total_lines), sg, b,
+                      make_core(p, sg, p->log_n2), st);
     }
   } else {
     const int lx = ilog2ll(p->nx), ly = ilog2ll(p->ny);
@@ -245,14 +259,14 @@ tcfftStatus exec_passes(tcfftPlanImpl* p, int prec, const void* in, void* out, i
     a.in_elem = a.out_elem = 1;
     a.in_contig = a.out_contig = true;
     a.contig_len = p->ny;
-    s = launch_pass(prec, kPassRow, ly, pick_row_tile(prec, ly, a.total_lines), sg, a, make_core(p, sg, ly), st);
+    s = launch_pass(prec, kPassRow, ly, choose_tile(prec, kPassRow, ly, a.total_lines), sg, a, make_core(p, sg, ly), st);
     if (s == TCFFT_OK) {
       // columns: length nx, stride ny, in place
       auto b = make_io<IOT<false, false>, E>(out, out, p->batch * p->ny, ly, scale);
       b.in_seq = b.out_seq = p->n;
       b.in_line = b.out_line = 1;
       b.in_elem = b.out_elem = p->ny;
-      s = launch_pass(prec, kPassCol, lx, kTileBig, sg, b, make_core(p, sg, lx), st);
+      s = launch_pass(prec, kPassCol, lx, choose_tile(prec, kPassCol, lx, b.total_lines), sg, b, make_core(p, sg, lx), st);
     }
   }
   return s;
@@ -543,5 +557,41 @@ const char* tcfft_status_string(tcfftStatus s) {
 }
 
 int tcfft_last_launch_count(void) { return g_last_launches; }
+
+tcfftStatus tcfft_tune_set(int precision, int pass_kind, int log2_len, int tile) {
+  if (precision < 0 || precision >= kNumPrec || pass_kind < 0 || pass_kind >= kNumPassKinds || log2_len < 0 ||
+      log2_len > kMaxLogL || tile < -1 || tile >= kNumTileSel)
+    return ret(TCFFT_INVALID_VALUE);
+  std::call_once(g_tune_once, tune_reset);
+  tcfftStatus s = ensure_init();
+  if (s != TCFFT_OK) return ret(s);
+  if (tile >= 0 && !g_tab[precision][pass_kind][log2_len][tile][0].fn) return ret(TCFFT_UNSUPPORTED);
+  g_tune[precision][pass_kind][log2_len] = tile;
+  return ret(TCFFT_OK);
+}
+
+tcfftStatus tcfft_tune_get(int precision, int pass_kind, int log2_len, int* tile) {
+  if (!tile || precision < 0 || precision >= kNumPrec || pass_kind < 0 || pass_kind >= kNumPassKinds ||
+      log2_len < 0 || log2_len > kMaxLogL)
+    return ret(TCFFT_INVALID_VALUE);
+  std::call_once(g_tune_once, tune_reset);
+  *tile = g_tune[precision][pass_kind][log2_len];
+  return ret(TCFFT_OK);
+}
+
+tcfftStatus tcfft_pass_info(int precision, int pass_kind, int log2_len, int tile, int* lines_per_tile,
+                            int* ctas_per_sm, int* num_sms) {
+  if (precision < 0 || precision >= kNumPrec || pass_kind < 0 || pass_kind >= kNumPassKinds || log2_len < 0 ||
+      log2_len > kMaxLogL || tile < 0 || tile >= kNumTileSel)
+    return ret(TCFFT_INVALID_VALUE);
+  tcfftStatus s = ensure_init();
+  if (s != TCFFT_OK) return ret(s);
+  const PassKernel& pk = g_tab[precision][pass_kind][log2_len][tile][0];
+  if (!pk.fn) return ret(TCFFT_UNSUPPORTED);
+  if (lines_per_tile) *lines_per_tile = pk.G;
+  if (ctas_per_sm) *ctas_per_sm = g_occ[precision][pass_kind][log2_len][tile][0];
+  if (num_sms) *num_sms = g_num_sms;
+  return ret(TCFFT_OK);
+}
 
 }  // extern "C"

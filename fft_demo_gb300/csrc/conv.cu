@@ -1,0 +1,390 @@
+// 2D FFT convolution (C ABI): plan, resident filter spectra, execution.
+//
+// Pipeline per batch of images (P x P padded transform, P = 2^k):
+//   1 row pass    real image rows (zero-padded on load) -> half-spectrum rows,
+//                 only the sy rows that hold data            (scale 1/P)
+//   2 column pass columns, rows >= sy read as zero -> spectrum (scale 1/P)
+//   3 pointwise   Y[f] = sum_s X[s] * K[f][s] in FP32 (K resident)
+//   4 column pass inverse, only the rows of the output window are stored
+//   5 row pass    inverse, real part of the output window's columns
+// The two forward scales make the spectra 1/P^2 of the unnormalised DFT, so
+// the unnormalised inverse yields the convolution itself and FP16 spectra stay
+// in range for image values up to ~1e3.
+//
+// Reference semantics (tensorcore_fft_conv2d.cpp:12-58, 250-289;
+// tensorcore_fft_conv2d_kernel.cu:1034-1150, 1222-1285, 1373-1404):
+// conv2d_forward flips each filter 180 degrees, zero-pads image and filter,
+// multiplies the spectra, sums over input channels in FP32, inverse-FFTs and
+// reads the window at offset (fx-1, fx-1) scaled by 1/P^2: the valid
+// cross-correlation, TCFFT_CONV_VALID_CORR here. The reference quantises the
+// FP32 product to FP16 with a per-filter power-of-ten scale
+// (fft_cpx_point_wise_quant_p1..p3) before its FP16 inverse FFT; this library
+// scales the forward transforms by 1/P instead and keeps the product in the
+// plan's precision.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <new>
+
+#include "../../include/tcfft_gb300.h"
+#include "conv_kernels.cuh"
+#include "tables.cuh"
+
+using namespace tcfft;
+
+namespace {
+
+thread_local tcfftStatus g_conv_last = TCFFT_OK;
+tcfftStatus cret(tcfftStatus s) {
+  g_conv_last = s;
+  return s;
+}
+
+ConvTable g_ctab[2];  // [precision]
+int g_cocc[2][kNumConvPass][kConvMaxLogP + 1];
+std::once_flag g_conv_once;
+cudaError_t g_conv_err = cudaSuccess;
+int g_conv_sms = 0;
+
+void conv_init() {
+  register_conv_f16(g_ctab[0]);
+  register_conv_split(g_ctab[1]);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_conv_sms, cudaDevAttrMultiProcessorCount, dev);
+  for (int pr = 0; pr < 2 && e == cudaSuccess; ++pr)
+    for (int k = 0; k < kNumConvPass && e == cudaSuccess; ++k)
+      for (int l = kConvMinLogP; l <= kConvMaxLogP && e == cudaSuccess; ++l) {
+        ConvKernel& ck = g_ctab[pr][k][l];
+        if (!ck.fn) continue;
+        e = cudaFuncSetAttribute(ck.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, ck.smem);
+        if (e == cudaSuccess)
+          e = cudaFuncSetAttribute(ck.fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                   cudaSharedmemCarveoutMaxShared);
+        cudaFuncAttributes fa;
+        if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, ck.fn);
+        if (e != cudaSuccess) break;
+        const int regs_per_warp = ((fa.numRegs * 32 + 255) / 256) * 256;
+        int occ = 65536 / (regs_per_warp * (kPassThreads / 32));
+        const int by_smem = (228 * 1024) / (ck.smem + 1024);
+        if (by_smem < occ) occ = by_smem;
+        const int tmem = 512 / (ck.Mt / (pr == 0 ? 4 : 2));
+        if (tmem < occ) occ = tmem;
+        g_cocc[pr][k][l] = occ < 1 ? 1 : occ;
+      }
+  g_conv_err = e;
+}
+
+int ilog2i(long long v) {
+  int l = 0;
+  while ((1ll << l) < v) ++l;
+  return l;
+}
+
+// Y[b][f][i] = sum_s X[b][s][i] * K[f][s][i]
+template <class E>
+__global__ void conv_pointwise_kernel(const E* __restrict__ X, const E* __restrict__ K, E* __restrict__ Y,
+                                      long long plane, int S, int F, long long total) {
+  for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
+       t += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const long long i = t % plane;
+    const long long bf = t / plane;
+    const int f = static_cast<int>(bf % F);
+    const long long b = bf / F;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int s = 0; s < S; ++s) {
+      const float2 x = from_elem(X[(b * S + s) * plane + i]);
+      const float2 k = from_elem(K[(static_cast<long long>(f) * S + s) * plane + i]);
+      acc.x += x.x * k.x - x.y * k.y;
+      acc.y += x.x * k.y + x.y * k.x;
+    }
+    Y[t] = to_elem<E>(acc);
+  }
+}
+
+}  // namespace
+
+struct tcfftConvImpl {
+  int S = 0, F = 0, sy = 0, sx = 0, fy = 0, fx = 0, mode = 0, precision = 0;
+  int P = 0, logP = 0;
+  int oy = 0, ox = 0, r0 = 0, c0 = 0;
+  long long max_batch = 0;
+  size_t esz = 4;  // bytes per complex element (4 FP16, 8 split)
+  void* K = nullptr;
+  void* X = nullptr;
+  void* Xf = nullptr;
+  void* Y = nullptr;
+  void* Z = nullptr;
+  float2* tw[2] = {nullptr, nullptr};
+  uint16_t* bmat[2] = {nullptr, nullptr};
+  int* err = nullptr;
+  bool filters_set = false;
+};
+
+namespace {
+
+void conv_free(tcfftConvImpl* c) {
+  if (!c) return;
+  cudaFree(c->K);
+  cudaFree(c->X);
+  cudaFree(c->Xf);
+  cudaFree(c->Y);
+  cudaFree(c->Z);
+  for (int s = 0; s < 2; ++s) {
+    cudaFree(c->tw[s]);
+    cudaFree(c->bmat[s]);
+  }
+  cudaFree(c->err);
+  delete c;
+}
+
+template <class IO>
+tcfftStatus conv_launch(tcfftConvImpl* c, int pass, int sign_idx, const IO& io, cudaStream_t st) {
+  const int pr = c->precision == TCFFT_FP16 ? 0 : 1;
+  const ConvKernel& k = g_ctab[pr][pass][c->logP];
+  if (!k.fn) return TCFFT_UNSUPPORTED;
+  PassCore core;
+  core.tw = c->tw[sign_idx];
+  core.bmat = reinterpret_cast<const uint32_t*>(c->bmat[sign_idx]);
+  core.err = c->err;
+  const long long ntiles = (io.total_lines + k.G - 1) / k.G;
+  long long grid = static_cast<long long>(g_conv_sms) * g_cocc[pr][pass][c->logP];
+  if (grid > ntiles) grid = ntiles;
+  if (grid < 1) grid = 1;
+  void* args[] = {const_cast<IO*>(&io), &core};
+  if (cudaLaunchKernel(k.fn, dim3(static_cast<unsigned>(grid)), dim3(kPassThreads), args, static_cast<size_t>(k.smem),
+                       st) != cudaSuccess)
+    return TCFFT_LAUNCH_FAILED;
+  return TCFFT_OK;
+}
+
+template <class T>
+T zero_io() {
+  T t;
+  std::memset(&t, 0, sizeof(t));
+  return t;
+}
+
+// Row pass forward on real input rows: `count` images of rows x cols, flip
+// for correlation filters.
+template <class R, class E>
+tcfftStatus conv_row_fwd(tcfftConvImpl* c, int pass, const R* in, E* out, long long count, int rows, int cols,
+                         int flip, float scale, cudaStream_t st) {
+  auto io = zero_io<IoRealRowIn<R, E>>();
+  io.in = in;
+  io.out = out;
+  io.total_lines = count * rows;
+  io.sy = rows;
+  io.sx = cols;
+  io.P = c->P;
+  io.in_image_stride = static_cast<long long>(rows) * cols;
+  io.flip = flip;
+  io.scale = scale;
+  return conv_launch(c, pass, 0, io, st);
+}
+
+template <class E>
+tcfftStatus conv_col(tcfftConvImpl* c, int pass, int sign_idx, const E* in, E* out, long long count, int valid_rows,
+                     int r0, int nr, float scale, cudaStream_t st) {
+  auto io = zero_io<IoColMaskCrop<E>>();
+  io.in = in;
+  io.out = out;
+  io.total_lines = count * c->P;
+  io.P = c->P;
+  io.lps_log2 = c->logP;
+  io.valid_rows = valid_rows;
+  io.r0 = r0;
+  io.nr = nr;
+  io.scale = scale;
+  return conv_launch(c, pass, sign_idx, io, st);
+}
+
+template <class E, class RO>
+tcfftStatus conv_row_inv(tcfftConvImpl* c, const E* in, RO* out, long long count, float scale, cudaStream_t st) {
+  auto io = zero_io<IoRowCropReal<E, RO>>();
+  io.in = in;
+  io.out = out;
+  io.total_lines = count * c->oy;
+  io.P = c->P;
+  io.c0 = c->c0;
+  io.nc = c->ox;
+  io.scale = scale;
+  return conv_launch(c, kConvRowInv, 1, io, st);
+}
+
+template <class E, class RI>
+tcfftStatus conv_run(tcfftConvImpl* c, const RI* images, RI* out, long long batch, cudaStream_t st) {
+  const float inv_p = 1.0f / static_cast<float>(c->P);
+  E* X = static_cast<E*>(c->X);
+  E* Xf = static_cast<E*>(c->Xf);
+  E* Y = static_cast<E*>(c->Y);
+  E* Z = static_cast<E*>(c->Z);
+  tcfftStatus s = conv_row_fwd<RI, E>(c, kConvRowFwdImg, images, X, batch * c->S, c->sy, c->sx, 0, inv_p, st);
+  if (s == TCFFT_OK) s = conv_col<E>(c, kConvColFwd, 0, X, Xf, batch * c->S, c->sy, 0, c->P, inv_p, st);
+  if (s == TCFFT_OK) {
+    const long long plane = static_cast<long long>(c->P) * c->P;
+    const long long total = batch * c->F * plane;
+    conv_pointwise_kernel<E><<<static_cast<unsigned>(g_conv_sms * 8), 256, 0, st>>>(
+        Xf, static_cast<const E*>(c->K), Y, plane, c->S, c->F, total);
+    if (cudaGetLastError() != cudaSuccess) s = TCFFT_LAUNCH_FAILED;
+  }
+  if (s == TCFFT_OK) s = conv_col<E>(c, kConvColInv, 1, Y, Z, batch * c->F, c->P, c->r0, c->oy, 1.0f, st);
+  if (s == TCFFT_OK) s = conv_row_inv<E, RI>(c, Z, out, batch * c->F, 1.0f, st);
+  return s;
+}
+
+}  // namespace
+
+extern "C" {
+
+tcfftStatus tcfft_conv2d_plan(tcfftConv* conv, int S, int F, int sy, int sx, int fy, int fx, int mode,
+                              int precision, long long max_batch) {
+  if (!conv) return cret(TCFFT_INVALID_VALUE);
+  *conv = nullptr;
+  if (S < 1 || F < 1 || sy < 1 || sx < 1 || fy < 1 || fx < 1 || max_batch < 1) return cret(TCFFT_INVALID_SIZE);
+  if (precision != TCFFT_FP16 && precision != TCFFT_SPLIT_FP32) return cret(TCFFT_INVALID_VALUE);
+  if (mode != TCFFT_CONV_VALID_CORR && mode != TCFFT_CONV_SAME && mode != TCFFT_CONV_FULL)
+    return cret(TCFFT_INVALID_VALUE);
+  if (mode == TCFFT_CONV_VALID_CORR && (fy > sy || fx > sx)) return cret(TCFFT_INVALID_SIZE);
+  if (mode == TCFFT_CONV_SAME && ((fy % 2) == 0 || (fx % 2) == 0)) return cret(TCFFT_INVALID_SIZE);
+  std::call_once(g_conv_once, conv_init);
+  if (g_conv_err != cudaSuccess) return cret(TCFFT_NO_DEVICE);
+  tcfftConvImpl* c = new (std::nothrow) tcfftConvImpl();
+  if (!c) return cret(TCFFT_ALLOC_FAILED);
+  c->S = S;
+  c->F = F;
+  c->sy = sy;
+  c->sx = sx;
+  c->fy = fy;
+  c->fx = fx;
+  c->mode = mode;
+  c->precision = precision;
+  c->max_batch = max_batch;
+  c->esz = precision == TCFFT_FP16 ? 4 : 8;
+  // Smallest power of two free of wrap-around inside the output window.
+  long long need = 0;
+  if (mode == TCFFT_CONV_VALID_CORR) {
+    need = sy > sx ? sy : sx;
+    c->oy = sy - fy + 1;
+    c->ox = sx - fx + 1;
+    c->r0 = fy - 1;
+    c->c0 = fx - 1;
+  } else if (mode == TCFFT_CONV_SAME) {
+    const long long ny = sy + (fy - 1) / 2, nx = sx + (fx - 1) / 2;
+    need = ny > nx ? ny : nx;
+    c->oy = sy;
+    c->ox = sx;
+    c->r0 = (fy - 1) / 2;
+    c->c0 = (fx - 1) / 2;
+  } else {
+    const long long ny = sy + fy - 1, nx = sx + fx - 1;
+    need = ny > nx ? ny : nx;
+    c->oy = sy + fy - 1;
+    c->ox = sx + fx - 1;
+    c->r0 = 0;
+    c->c0 = 0;
+  }
+  if (need < (1 << kConvMinLogP)) need = 1 << kConvMinLogP;
+  c->logP = ilog2i(need);
+  c->P = 1 << c->logP;
+  const int max_log = precision == TCFFT_FP16 ? kConvMaxLogP : kConvMaxLogP - 1;
+  if (c->logP > max_log) {
+    conv_free(c);
+    return cret(TCFFT_INVALID_SIZE);
+  }
+  const size_t plane = static_cast<size_t>(c->P) * c->P;
+  tcfftStatus s = TCFFT_OK;
+  auto alloc = [&](void** p, size_t bytes) {
+    if (s == TCFFT_OK && cudaMalloc(p, bytes) != cudaSuccess) s = TCFFT_ALLOC_FAILED;
+  };
+  const size_t filt_rows = static_cast<size_t>(F) * S * fy * c->P;
+  const size_t img_rows = static_cast<size_t>(max_batch) * S * sy * c->P;
+  alloc(&c->K, static_cast<size_t>(F) * S * plane * c->esz);
+  alloc(&c->X, (img_rows > filt_rows ? img_rows : filt_rows) * c->esz);
+  alloc(&c->Xf, static_cast<size_t>(max_batch) * S * plane * c->esz);
+  alloc(&c->Y, static_cast<size_t>(max_batch) * F * plane * c->esz);
+  alloc(&c->Z, static_cast<size_t>(max_batch) * F * c->oy * c->P * c->esz);
+  for (int d = 0; d < 2; ++d) {
+    alloc(reinterpret_cast<void**>(&c->tw[d]), sizeof(float2) * c->P);
+    alloc(reinterpret_cast<void**>(&c->bmat[d]), 4096);
+    if (s == TCFFT_OK && (gen_twiddles(c->tw[d], c->P, c->logP, 0, d == 0 ? -1 : 1, 0) != cudaSuccess ||
+                          gen_dft16_bmat(c->bmat[d], d == 0 ? -1 : 1, 0, 0) != cudaSuccess ||
+                          gen_dft16_bmat(c->bmat[d] + 1024, d == 0 ? -1 : 1, 1, 0) != cudaSuccess))
+      s = TCFFT_LAUNCH_FAILED;
+  }
+  alloc(reinterpret_cast<void**>(&c->err), sizeof(int));
+  if (s == TCFFT_OK && cudaMemset(c->err, 0, sizeof(int)) != cudaSuccess) s = TCFFT_LAUNCH_FAILED;
+  if (s == TCFFT_OK && cudaDeviceSynchronize() != cudaSuccess) s = TCFFT_LAUNCH_FAILED;
+  if (s != TCFFT_OK) {
+    conv_free(c);
+    return cret(s);
+  }
+  *conv = c;
+  return cret(TCFFT_OK);
+}
+
+tcfftStatus tcfft_conv2d_set_filters(tcfftConv c, const float* filters, void* stream) {
+  if (!c || !filters) return cret(TCFFT_INVALID_VALUE);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int flip = c->mode == TCFFT_CONV_VALID_CORR ? 1 : 0;
+  const long long count = static_cast<long long>(c->F) * c->S;
+  tcfftStatus s;
+  if (c->precision == TCFFT_FP16) {
+    s = conv_row_fwd<float, half2>(c, kConvRowFwdFilt, filters, static_cast<half2*>(c->X), count, c->fy, c->fx, flip,
+                                   1.0f, st);
+    if (s == TCFFT_OK)
+      s = conv_col<half2>(c, kConvColFwd, 0, static_cast<half2*>(c->X), static_cast<half2*>(c->K), count, c->fy, 0,
+                          c->P, 1.0f, st);
+  } else {
+    s = conv_row_fwd<float, float2>(c, kConvRowFwdFilt, filters, static_cast<float2*>(c->X), count, c->fy, c->fx,
+                                    flip, 1.0f, st);
+    if (s == TCFFT_OK)
+      s = conv_col<float2>(c, kConvColFwd, 0, static_cast<float2*>(c->X), static_cast<float2*>(c->K), count, c->fy,
+                           0, c->P, 1.0f, st);
+  }
+  if (s == TCFFT_OK) c->filters_set = true;
+  return cret(s);
+}
+
+tcfftStatus tcfft_conv2d_exec(tcfftConv c, const void* images, void* out, long long batch, void* stream) {
+  if (!c || !images || !out) return cret(TCFFT_INVALID_VALUE);
+  if (batch < 1 || batch > c->max_batch) return cret(TCFFT_CAPACITY);
+  if (!c->filters_set) return cret(TCFFT_INVALID_VALUE);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  tcfftStatus s;
+  if (c->precision == TCFFT_FP16)
+    s = conv_run<half2, __half>(c, static_cast<const __half*>(images), static_cast<__half*>(out), batch, st);
+  else
+    s = conv_run<float2, float>(c, static_cast<const float*>(images), static_cast<float*>(out), batch, st);
+  return cret(s);
+}
+
+tcfftStatus tcfft_conv2d_shape(tcfftConv c, int* out_rows, int* out_cols, int* padded) {
+  if (!c) return cret(TCFFT_INVALID_VALUE);
+  if (out_rows) *out_rows = c->oy;
+  if (out_cols) *out_cols = c->ox;
+  if (padded) *padded = c->P;
+  return cret(TCFFT_OK);
+}
+
+tcfftStatus tcfft_conv2d_check(tcfftConv c, void* stream) {
+  if (!c) return cret(TCFFT_INVALID_VALUE);
+  if (cudaStreamSynchronize(static_cast<cudaStream_t>(stream)) != cudaSuccess) return cret(TCFFT_LAUNCH_FAILED);
+  int h = 0;
+  if (cudaMemcpy(&h, c->err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return cret(TCFFT_LAUNCH_FAILED);
+  if (h) {
+    cudaMemset(c->err, 0, sizeof(int));
+    return cret(TCFFT_TIMEOUT);
+  }
+  return cret(TCFFT_OK);
+}
+
+tcfftStatus tcfft_conv2d_destroy(tcfftConv c) {
+  if (!c) return cret(TCFFT_INVALID_VALUE);
+  conv_free(c);
+  return cret(TCFFT_OK);
+}
+
+}  // extern "C"

@@ -277,7 +277,70 @@ __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const f
 }
 
 // ---------------------------------------------------------------------------
-// The pass kernel (FP16 storage; FP32 accumulation and twiddles).
+// Per-CTA state shared by the tiles a CTA processes. Shared-memory layout:
+//   [0, 2048)      B matrix image (the 16-point DFT, this direction)
+//   [2048, 2112)   mbarriers (MMA, TMA), TMEM address slot
+//   [3072, ...)    tile planes (real plane, imaginary plane), 1024-aligned
+// ---------------------------------------------------------------------------
+constexpr uint32_t kPlaneOffset = 3072;
+
+struct PassState {
+  uint8_t* smem;
+  uint8_t* bmat;
+  uint64_t* mbar;
+  uint64_t* tma_bar;
+  uint32_t* tslot;
+  uint32_t tbase;
+  uint32_t phase;
+  uint32_t tma_phase;
+};
+
+__device__ __forceinline__ uint8_t* aligned_dynamic_smem() {
+  extern __shared__ uint8_t smem_raw[];
+  return reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                    ~static_cast<uintptr_t>(1023));
+}
+
+// B matrix, barriers, TMEM allocation (whole CTA).
+template <uint32_t TMEM_COLS>
+__device__ __forceinline__ void pass_setup(PassState& st, const uint32_t* __restrict__ bmat_g) {
+  st.smem = aligned_dynamic_smem();
+  st.bmat = st.smem;
+  st.mbar = reinterpret_cast<uint64_t*>(st.smem + 2048);
+  st.tma_bar = reinterpret_cast<uint64_t*>(st.smem + 2056);
+  st.tslot = reinterpret_cast<uint32_t*>(st.smem + 2064);
+  const int tid = threadIdx.x;
+  for (int i = tid; i < 512; i += kPassThreads) reinterpret_cast<uint32_t*>(st.bmat)[i] = __ldg(bmat_g + i);
+  if (tid == 0) {
+    mbar_init(st.mbar, 1);
+    mbar_init(st.tma_bar, 1);
+  }
+  if ((tid >> 5) == 0) {
+    tmem_alloc(st.tslot, TMEM_COLS);
+    tmem_relinquish();
+  }
+  fence_proxy_async_smem();
+  tc_fence_before_sync();
+  __syncthreads();
+  tc_fence_after_sync();
+  st.tbase = *st.tslot;
+  st.phase = 0;
+  st.tma_phase = 0;
+}
+
+// Outstanding bulk stores complete, TMEM released (whole CTA).
+template <uint32_t TMEM_COLS>
+__device__ __forceinline__ void pass_teardown(PassState& st) {
+  if (threadIdx.x == 0) bulk_wait_all();
+  tc_fence_before_sync();
+  __syncthreads();
+  if ((threadIdx.x >> 5) == 0) tmem_dealloc(st.tbase, TMEM_COLS);
+}
+
+// ---------------------------------------------------------------------------
+// One tile: G lines of length L starting at line0 (FP16 storage, FP32
+// accumulation and twiddles). Returns false if a bounded wait gave up (the
+// error word is set; the caller stops and tears down).
 //   L          line length
 //   G          lines per tile (G * L / 16 must be 128, 256, 512 or 1024)
 //   LINE_MINOR butterfly order in the tile (true for column passes)
@@ -285,7 +348,7 @@ __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const f
 //   IO         global-memory policy (see fft_io.cuh)
 // ---------------------------------------------------------------------------
 template <int L, int G, bool LINE_MINOR, int SIGN, class IO>
-__global__ void __launch_bounds__(kPassThreads, 2) fft_pass_f16(const IO io, const PassCore core) {
+__device__ __forceinline__ bool pass_tile(PassState& st, const IO& io, const PassCore& core, long long line0) {
   using Sh = LineShape<L>;
   using Tl = Tile<L, G, LINE_MINOR>;
   constexpr int T = Sh::T;
@@ -295,54 +358,20 @@ __global__ void __launch_bounds__(kPassThreads, 2) fft_pass_f16(const IO io, con
   constexpr int NG = Mt / 128;
   constexpr uint32_t PLANE = Tl::PLANE;
   constexpr uint32_t KSTRIDE = Tl::KSTRIDE;
-  constexpr uint32_t TMEM_COLS = NG * 32;
   static_assert(Mt % 128 == 0 && Mt <= 1024, "tile size");
-  static_assert(TMEM_COLS >= 32 && (TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM columns");
   static_assert(G % 4 == 0 || IO::IN_VEC_L, "line-vectorised loads need G % 4 == 0");
   static_assert(G % 4 == 0 || IO::OUT_VEC_L, "line-vectorised stores need G % 4 == 0");
-  static_assert(J >= 4 || !IO::OUT_VEC_L || true, "");
   constexpr uint32_t IDESC = make_idesc_f16_f32(128, 32, true, false);
-
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
-                                             ~static_cast<uintptr_t>(1023));
-  uint8_t* re = smem;
-  uint8_t* im = smem + PLANE;
-  uint8_t* bmat = smem + 2 * PLANE;                           // 2 KB
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(bmat + 2048);  // 8 B
-  uint64_t* tma_bar = reinterpret_cast<uint64_t*>(bmat + 2048 + 8);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bmat + 2048 + 16);
-
+  uint8_t* re = st.smem + kPlaneOffset;
+  uint8_t* im = re + PLANE;
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const int lane = tid & 31;
-
-  // ---- one-time setup: B matrix, mbarrier, TMEM ----
-  for (int i = tid; i < 512; i += kPassThreads) reinterpret_cast<uint32_t*>(bmat)[i] = __ldg(core.bmat + i);
-  if (tid == 0) {
-    mbar_init(mbar, 1);
-    mbar_init(tma_bar, 1);
-  }
-  if (warp == 0) {
-    tmem_alloc(tslot, TMEM_COLS);
-    tmem_relinquish();
-  }
-  fence_proxy_async_smem();
-  tc_fence_before_sync();
-  __syncthreads();
-  tc_fence_after_sync();
-  const uint32_t tbase = *tslot;
-  uint32_t phase = 0, tma_phase = 0;
   bool timed_out = false;
   // Contiguous tiles (element (line, l) at base + line*L + l) move with bulk
   // TMA copies: one 2*PLANE-byte copy in, one out, through the tile region.
   const bool tma_in = IO::IN_VEC_L && io.in_contig;
   const bool stage_out = IO::OUT_VEC_L && io.out_contig && !LINE_MINOR;
-
-  const long long ntiles = (io.total_lines + G - 1) / G;
-
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const long long line0 = tile * G;
     const long long rem = io.total_lines - line0;
     const int nval = rem < G ? static_cast<int>(rem) : G;
 
@@ -351,15 +380,15 @@ __global__ void __launch_bounds__(kPassThreads, 2) fft_pass_f16(const IO io, con
       if (tid == 0) {
         bulk_wait_read_all();  // the previous tile's bulk store has read the region
         const uint32_t bytes = static_cast<uint32_t>(nval) * L * 4u;
-        mbar_arrive_expect_tx(tma_bar, bytes);
-        bulk_g2s(re, io.tile_src(line0), bytes, tma_bar);
+        mbar_arrive_expect_tx(st.tma_bar, bytes);
+        bulk_g2s(re, io.tile_src(line0), bytes, st.tma_bar);
       }
-      if (!mbar_wait_bounded(tma_bar, tma_phase & 1u)) {
+      if (!mbar_wait_bounded(st.tma_bar, st.tma_phase & 1u)) {
         timed_out = true;
         if (lane == 0) atomicOr(core.err, kErrMmaTimeout);
       }
-      tma_phase++;
-      if (__syncthreads_or(timed_out)) break;
+      st.tma_phase++;
+      if (__syncthreads_or(timed_out)) return false;
       // every thread takes its quads of the radix-T stage into registers ...
       constexpr int QPL = (L / T) / 4;
       constexpr int ITEMS = G * QPL;
@@ -381,7 +410,7 @@ __global__ void __launch_bounds__(kPassThreads, 2) fft_pass_f16(const IO io, con
 #pragma unroll
       for (int u = 0; u < NU; ++u) {
         const int it = tid + u * kPassThreads;
-        if (it >= ITEMS) break;
+        if (ITEMS % kPassThreads != 0 && it >= ITEMS) continue;
         const int g = it / QPL;
         const int j0 = (it % QPL) * 4;
         if constexpr (T == 1 && !LINE_MINOR && J >= 4) {
@@ -536,27 +565,27 @@ __global__ void __launch_bounds__(kPassThreads, 2) fft_pass_f16(const IO io, con
       if (timed_out) return;
       if (tid == 0) {
         tc_fence_after_sync();
-        const uint32_t a0 = smem_u32(re), a1 = smem_u32(im), b0 = smem_u32(bmat);
+        const uint32_t a0 = smem_u32(re), a1 = smem_u32(im), b0 = smem_u32(st.bmat);
         const uint64_t bd0 = make_sdesc(b0, 128u, 512u, kLayoutNone);
         const uint64_t bd1 = make_sdesc(b0 + 256u, 128u, 512u, kLayoutNone);
 #pragma unroll
         for (int grp = 0; grp < NG; ++grp) {
           const uint64_t ad0 = make_sdesc(a0 + grp * 2048u, 1024u, KSTRIDE, kLayoutSw128);
           const uint64_t ad1 = make_sdesc(a1 + grp * 2048u, 1024u, KSTRIDE, kLayoutSw128);
-          umma_f16(tbase + grp * 32u, ad0, bd0, IDESC, 0u);
-          umma_f16(tbase + grp * 32u, ad1, bd1, IDESC, 1u);
+          umma_f16(st.tbase + grp * 32u, ad0, bd0, IDESC, 0u);
+          umma_f16(st.tbase + grp * 32u, ad1, bd1, IDESC, 1u);
         }
-        umma_commit(mbar);
+        umma_commit(st.mbar);
       }
-      bool to = !mbar_wait_bounded(mbar, phase & 1u);
+      bool to = !mbar_wait_bounded(st.mbar, st.phase & 1u);
       if (to && lane == 0) atomicOr(core.err, kErrMmaTimeout);
-      phase++;
+      st.phase++;
       if (__syncthreads_or(to)) {
         timed_out = true;
         return;
       }
       tc_fence_after_sync();
-      stage_epilogue<L, G, LINE_MINOR, s, IO>(re, im, core.tw, tbase, warp, lane, io, line0, stage_out);
+      stage_epilogue<L, G, LINE_MINOR, s, IO>(re, im, core.tw, st.tbase, warp, lane, io, line0, stage_out);
       fence_proxy_async_smem();
       tc_fence_before_sync();
       __syncthreads();
@@ -564,25 +593,39 @@ __global__ void __launch_bounds__(kPassThreads, 2) fft_pass_f16(const IO io, con
     [&]<int... Is>(std::integer_sequence<int, Is...>) {
       (run_stage(std::integral_constant<int, Is>{}), ...);
     }(std::make_integer_sequence<int, S>{});
-    if (timed_out) break;
+    if (timed_out) return false;
     if (stage_out && tid == 0) {
       // the last stage left the tile in natural order: one bulk store
       bulk_s2g(io.tile_dst(line0), re, static_cast<uint32_t>(nval) * L * 4u);
       bulk_commit();
     }
-  }
+    return true;
+}
 
-  // ---- teardown ----
-  if (tid == 0) bulk_wait_all();
-  tc_fence_before_sync();
-  __syncthreads();
-  if (warp == 0) tmem_dealloc(tbase, TMEM_COLS);
+template <int L, int G>
+__host__ __device__ constexpr uint32_t pass_tmem_cols() {
+  return static_cast<uint32_t>(G * L / 16 / 128 * 32);
+}
+
+// ---------------------------------------------------------------------------
+// The pass kernel: persistent CTAs over the tiles of one pass.
+// ---------------------------------------------------------------------------
+template <int L, int G, bool LINE_MINOR, int SIGN, class IO, int MINB = 2>
+__global__ void __launch_bounds__(kPassThreads, MINB) fft_pass_f16(const IO io, const PassCore core) {
+  constexpr uint32_t TMEM_COLS = pass_tmem_cols<L, G>();
+  static_assert(TMEM_COLS >= 32 && (TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM columns");
+  PassState st;
+  pass_setup<TMEM_COLS>(st, core.bmat);
+  const long long ntiles = (io.total_lines + G - 1) / G;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+    if (!pass_tile<L, G, LINE_MINOR, SIGN, IO>(st, io, core, tile * G)) break;
+  pass_teardown<TMEM_COLS>(st);
 }
 
 // Dynamic shared memory bytes for a pass kernel instance (+1 KB alignment slack).
 template <int L, int G>
 constexpr int pass_smem_bytes() {
-  return 2 * (G * L / 16) * 32 + 2048 + 64 + 1024;
+  return static_cast<int>(kPlaneOffset) + 2 * (G * L / 16) * 32 + 1024;
 }
 
 }  // namespace tcfft

@@ -17,8 +17,9 @@ enum PassKind : int {
 };
 
 // Tile-size variants: Mt = butterflies per radix-16 stage in one tile
-// (FP16: small 128, big 1024; split: small 128, big 512).
-enum TileSel : int { kTileSmall = 0, kTileBig = 1, kNumTileSel = 2 };
+// (FP16: small 128, big 1024, mid 512 compiled for 3 CTAs/SM;
+//  split: small 128, big 512).
+enum TileSel : int { kTileSmall = 0, kTileBig = 1, kTileMid = 2, kNumTileSel = 3 };
 
 enum PrecSel : int { kPrecF16 = 0, kPrecSplit = 1, kNumPrec = 2 };
 
@@ -47,15 +48,15 @@ constexpr int tile_lines() {
   return Mt * 16 / L;
 }
 
-template <int L, int Mt, bool LINE_MINOR, bool IN_VEC_L, bool OUT_VEC_L>
+template <int L, int Mt, bool LINE_MINOR, bool IN_VEC_L, bool OUT_VEC_L, int MINB = 2>
 void fill_entry(PassTable& tab, int tile) {
   constexpr int G = tile_lines<L, Mt>();
   constexpr int LOG = ilog2c(L);
   const int smem = pass_smem_bytes<L, G>();
   PassKernel f, i;
   using IO = IoHalf<IN_VEC_L, OUT_VEC_L>;
-  f.fn = reinterpret_cast<const void*>(&fft_pass_f16<L, G, LINE_MINOR, -1, IO>);
-  i.fn = reinterpret_cast<const void*>(&fft_pass_f16<L, G, LINE_MINOR, +1, IO>);
+  f.fn = reinterpret_cast<const void*>(&fft_pass_f16<L, G, LINE_MINOR, -1, IO, MINB>);
+  i.fn = reinterpret_cast<const void*>(&fft_pass_f16<L, G, LINE_MINOR, +1, IO, MINB>);
   f.smem = i.smem = smem;
   f.G = i.G = G;
   f.Mt = i.Mt = Mt;

@@ -90,12 +90,68 @@ tcfftStatus tcfft_check(tcfftPlan plan, void *stream);
 
 tcfftStatus tcfft_destroy(tcfftPlan plan);
 
+/* ------------------------------------------------------------------------
+ * 2D FFT convolution
+ *   images  [batch][S][sy][sx] real (half for TCFFT_FP16, float for split)
+ *   filters [F][S][fy][fx] float, transformed once and kept on the device
+ *   out     [batch][F][oy][ox] real (same type as images)
+ * Modes:
+ *   TCFFT_CONV_VALID_CORR  out[f] = sum_s valid cross-correlation of image s
+ *                          with filter (f, s); oy = sy-fy+1, ox = sx-fx+1.
+ *                          This is fft_conv2d_half::conv2d_forward
+ *                          (tensorcore_fft_conv2d.cpp:283) and
+ *                          naive_fft_conv2d_ss_sf_valid (main.cpp:97).
+ *   TCFFT_CONV_SAME        true convolution, centred (fy, fx odd); oy = sy,
+ *                          ox = sx; S must be 1 or the channels are summed.
+ *   TCFFT_CONV_FULL        full linear convolution; oy = sy+fy-1,
+ *                          ox = sx+fx-1 (convolve_direct_fft family,
+ *                          fftconvolve2d.cu:184, without its 1/fftSize).
+ * The padded transform size P is the smallest power of two without
+ * wrap-around inside the output window (P <= 4096 FP16, <= 2048 split).
+ * ------------------------------------------------------------------------ */
+typedef enum tcfftConvMode {
+  TCFFT_CONV_VALID_CORR = 0,
+  TCFFT_CONV_SAME = 1,
+  TCFFT_CONV_FULL = 2
+} tcfftConvMode;
+
+typedef struct tcfftConvImpl *tcfftConv;
+
+/* Plan for batches of up to max_batch images (device buffers are sized for it). */
+tcfftStatus tcfft_conv2d_plan(tcfftConv *conv, int S, int F, int sy, int sx, int fy, int fx, int mode,
+                              int precision, long long max_batch);
+/* Transform and keep the filters (device float [F][S][fy][fx]). Replaces the
+ * filter FFT of the fft_conv2d_half constructor (tensorcore_fft_conv2d.cpp:46-57). */
+tcfftStatus tcfft_conv2d_set_filters(tcfftConv conv, const float *filters, void *stream);
+/* out = conv(images) for `batch` <= max_batch images (device buffers). */
+tcfftStatus tcfft_conv2d_exec(tcfftConv conv, const void *images, void *out, long long batch, void *stream);
+/* Output window and padded transform size of the plan. */
+tcfftStatus tcfft_conv2d_shape(tcfftConv conv, int *out_rows, int *out_cols, int *padded);
+/* Synchronise `stream`, report a flagged device error. */
+tcfftStatus tcfft_conv2d_check(tcfftConv conv, void *stream);
+tcfftStatus tcfft_conv2d_destroy(tcfftConv conv);
+
 /* Last status returned on this thread, and a readable name for a status. */
 tcfftStatus tcfft_get_last_error(void);
 const char *tcfft_status_string(tcfftStatus status);
 
 /* Number of kernel launches the last tcfft_exec* call on this thread made. */
 int tcfft_last_launch_count(void);
+
+/* ------------------------------------------------------------------------
+ * Tuning (used by the autotuner, fft_demo_gb300/autotune.py)
+ * A transform is a chain of passes; each pass kind has several tile
+ * variants (lines per CTA tile, CTAs per SM). The tuned variant per
+ * (precision, pass kind, log2 of the pass length) is process-wide state.
+ * ------------------------------------------------------------------------ */
+typedef enum tcfftPassKind { TCFFT_PASS_ROW = 0, TCFFT_PASS_COL = 1, TCFFT_PASS_ROWT = 2 } tcfftPassKind;
+typedef enum tcfftTile { TCFFT_TILE_SMALL = 0, TCFFT_TILE_BIG = 1, TCFFT_TILE_MID = 2 } tcfftTile;
+/* tile = -1 restores the built-in choice. */
+tcfftStatus tcfft_tune_set(int precision, int pass_kind, int log2_len, int tile);
+tcfftStatus tcfft_tune_get(int precision, int pass_kind, int log2_len, int *tile);
+/* Geometry of a pass variant: lines per tile, co-resident CTAs per SM, SMs. */
+tcfftStatus tcfft_pass_info(int precision, int pass_kind, int log2_len, int tile, int *lines_per_tile,
+                            int *ctas_per_sm, int *num_sms);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,113 @@
+"""GPU parity tests of the 2D FFT convolution, through the C ABI.
+
+Oracles (oracle/liborc.so): valid cross-correlation summed over channels
+(restating naive_fft_conv2d_ss_sf_valid, main.cpp:97), 'same' and full
+linear convolution, all FP64 direct sums.
+Tolerances (relative L2 vs FP64): FP16 plans 3e-3 (REL_L2_CONV_FP16),
+split plans 1e-5 (REL_L2_CONV_SPLIT).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+REL_L2_CONV_FP16 = 3e-3
+REL_L2_CONV_SPLIT = 1e-5
+
+
+def reference_data(s, f, C, F, seed=42):
+    """Values like the reference's generate_data (main.cpp:32): 0.1 * (k % 10)."""
+    rng = np.random.default_rng(seed)
+    sig = 0.1 * rng.integers(0, 10, (C, s, s))
+    filt = 0.1 * rng.integers(0, 10, (F, C, f, f))
+    return sig, filt
+
+
+def run_conv(tc, images, filters, mode, precision, S, F):
+    import torch
+    B = images.shape[0]
+    sy, sx = images.shape[-2:]
+    fy, fx = filters.shape[-2:]
+    conv = tc.Conv2d(S, F, sy, sx, fy, fx, mode=mode, precision=precision, max_batch=B)
+    dt = torch.float16 if precision == tc.FP16 else torch.float32
+    img = torch.from_numpy(np.ascontiguousarray(images)).to(dt).cuda()
+    w = torch.from_numpy(np.ascontiguousarray(filters)).float().cuda()
+    conv.set_filters(w)
+    out = conv.exec(img)
+    conv.check()
+    return out.double().cpu().numpy(), conv
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_valid_correlation_reference_config(tc, orc, precision):
+    """nx=ny=256, 13x13 filters, 16 filters, C=1 (main.cpp:322-328)."""
+    sig, filt = reference_data(256, 13, 1, 16)
+    out, conv = run_conv(tc, sig[None], filt, tc.CONV_VALID_CORR, precision, 1, 16)
+    ref = orc.corr2d_valid(sig, filt)
+    if precision == tc.FP16:
+        sig_h = sig.astype(np.float16).astype(np.float64)
+        ref = orc.corr2d_valid(sig_h, filt)
+    err = orc.rel_l2(out[0], ref)
+    tol = REL_L2_CONV_FP16 if precision == tc.FP16 else REL_L2_CONV_SPLIT
+    assert err < tol, err
+    assert conv.padded == 256 and out.shape == (1, 16, 244, 244)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_valid_correlation_multichannel(tc, orc, precision):
+    rng = np.random.default_rng(3)
+    S, F, s, f = 3, 2, 100, 7
+    sig = rng.uniform(0, 1, (2, S, s, s))
+    filt = rng.uniform(-1, 1, (F, S, f, f))
+    out, _ = run_conv(tc, sig, filt, tc.CONV_VALID_CORR, precision, S, F)
+    if precision == tc.FP16:
+        sig = sig.astype(np.float16).astype(np.float64)
+    for b in range(2):
+        err = orc.rel_l2(out[b], orc.corr2d_valid(sig[b], filt))
+        assert err < (REL_L2_CONV_FP16 if precision == tc.FP16 else REL_L2_CONV_SPLIT), err
+
+
+@pytest.mark.parametrize("precision,side,f", [(0, 256, 31), (1, 200, 15), (0, 64, 3), (1, 128, 7)])
+def test_same_convolution(tc, orc, precision, side, f):
+    """'same' mode, filter N(0,1) normalised to unit L1 (config 3's recipe)."""
+    rng = np.random.default_rng(side)
+    img = rng.uniform(0, 1, (2, 1, side, side))
+    w = rng.standard_normal((1, 1, f, f))
+    w /= np.abs(w).sum()
+    out, conv = run_conv(tc, img, w, tc.CONV_SAME, precision, 1, 1)
+    if precision == tc.FP16:
+        img = img.astype(np.float16).astype(np.float64)
+    for b in range(2):
+        ref = orc.conv2d_same(img[b, 0], w[0, 0])
+        err = orc.rel_l2(out[b, 0], ref)
+        assert err < (REL_L2_CONV_FP16 if precision == tc.FP16 else REL_L2_CONV_SPLIT), err
+
+
+def test_full_convolution_split(tc, orc):
+    rng = np.random.default_rng(5)
+    img = rng.uniform(-1, 1, (1, 1, 96, 80))
+    ks = rng.uniform(-1, 1, (4, 1, 9, 5))
+    out, conv = run_conv(tc, img, ks, tc.CONV_FULL, tc.SPLIT_FP32, 1, 4)
+    ref = orc.conv2d_full(img[0, 0], ks[:, 0])
+    assert out.shape == (1, 4, 104, 84)
+    assert orc.rel_l2(out[0], ref) < REL_L2_CONV_SPLIT
+
+
+def test_delta_filter_is_shift(tc):
+    """Known answer: a delta filter at (a, b) shifts the image (full mode)."""
+    import torch
+    rng = np.random.default_rng(2)
+    img = rng.uniform(0, 1, (1, 1, 64, 64)).astype(np.float32)
+    w = np.zeros((1, 1, 5, 5), np.float32)
+    w[0, 0, 2, 3] = 1.0
+    out, _ = run_conv(tc, img, w, tc.CONV_FULL, tc.SPLIT_FP32, 1, 1)
+    np.testing.assert_allclose(out[0, 0, 2:66, 3:67], img[0, 0], atol=1e-5)
+
+
+def test_conv_errors(tc):
+    with pytest.raises(tc.TcfftError):
+        tc.Conv2d(1, 1, 64, 64, 4, 4, mode=tc.CONV_SAME)  # even filter in 'same' mode
+    with pytest.raises(tc.TcfftError):
+        tc.Conv2d(1, 1, 8, 8, 9, 9, mode=tc.CONV_VALID_CORR)  # filter larger than image
+    with pytest.raises(tc.TcfftError):
+        tc.Conv2d(1, 1, 3000, 3000, 31, 31, mode=tc.CONV_SAME, precision=tc.SPLIT_FP32)
