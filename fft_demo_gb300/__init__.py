@@ -51,6 +51,10 @@ def _declare(L):
         "tcfft_plan_1d": (i, [ctypes.POINTER(vp), ll, ll, i]),
         "tcfft_plan_2d": (i, [ctypes.POINTER(vp), i, i, ll, i]),
         "tcfft_workspace_bytes": (i, [vp, ctypes.POINTER(ctypes.c_size_t)]),
+        "tcfft_plan_set_fused": (i, [vp, i]),
+        "tcfft_tune_set": (i, [i, i, i, i]),
+        "tcfft_tune_get": (i, [i, i, i, ctypes.POINTER(i)]),
+        "tcfft_pass_info": (i, [i, i, i, i, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)]),
         "tcfft_exec": (i, [vp, vp, vp, i, f, vp]),
         "tcfft_exec_digitrev": (i, [vp, vp, vp, ctypes.POINTER(i), i, vp]),
         "tcfft_check": (i, [vp, vp]),
@@ -155,6 +159,10 @@ class Plan:
     def check(self, stream=None):
         """Synchronise and raise if a kernel of this plan flagged an error."""
         _check(lib().tcfft_check(self._h, _stream_ptr(stream)), "check")
+
+    def set_fused(self, enable):
+        """Large 1D FP16 sizes: one fused launch (default) or two pass launches."""
+        _check(lib().tcfft_plan_set_fused(self._h, 1 if enable else 0), "set_fused")
 
     def destroy(self):
         if self._h:

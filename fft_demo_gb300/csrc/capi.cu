@@ -31,6 +31,8 @@ tcfftStatus ret(tcfftStatus s) {
 }
 
 PassTable g_tab[kNumPrec][kNumPassKinds];
+FusedTable g_fused;
+int g_fused_occ[kFusedMaxLog + 1][2];
 int g_occ[kNumPrec][kNumPassKinds][kMaxLogL + 1][kNumTileSel][2];
 std::once_flag g_once;
 cudaError_t g_init_err = cudaSuccess;
@@ -52,6 +54,7 @@ void init_registry() {
   register_split_row_kernels(g_tab[kPrecSplit][kPassRow]);
   register_split_col_kernels(g_tab[kPrecSplit][kPassCol]);
   register_split_rowt_kernels(g_tab[kPrecSplit][kPassRowT]);
+  register_fused_kernels(g_fused);
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
@@ -86,6 +89,24 @@ void init_registry() {
           const int tmem_limit = 512 / (pk.Mt / (pr == kPrecF16 ? 4 : 2));
           g_occ[pr][k][l][t][s] = occ < tmem_limit ? occ : tmem_limit;
         }
+  for (int l = kFusedMinLog; l <= kFusedMaxLog && e == cudaSuccess; ++l)
+    for (int sg = 0; sg < 2 && e == cudaSuccess; ++sg) {
+      FusedKernel& fk = g_fused[l][sg];
+      if (!fk.fn) continue;
+      e = cudaFuncSetAttribute(fk.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, fk.smem);
+      if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(fk.fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+      cudaFuncAttributes fa;
+      if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, fk.fn);
+      if (e != cudaSuccess) break;
+      const int regs_per_warp = ((fa.numRegs * 32 + 255) / 256) * 256;
+      int occ = 65536 / (regs_per_warp * (kPassThreads / 32));
+      const int by_smem = (228 * 1024) / (fk.smem + static_cast<int>(fa.sharedSizeBytes) + 1024);
+      if (by_smem < occ) occ = by_smem;
+      const int cols1 = (16384 / 16 / 128) * 32;  // Mt = 1024 tiles: 256 TMEM columns
+      if (512 / cols1 < occ) occ = 512 / cols1;
+      g_fused_occ[l][sg] = occ < 1 ? 1 : occ;
+    }
   g_init_err = e;
 }
 
@@ -119,6 +140,11 @@ struct tcfftPlanImpl {
   void* ws = nullptr;
   size_t ws_bytes = 0;
   void* perm_ws = nullptr;  // un-permute buffer for in-place digit-reversed input
+  // fused four-step (FP16, 2^15 <= n <= 2^24): one launch, workspace ring
+  bool fused = false;
+  int chunk_seqs = 0, nchunks = 0, ring = 0;
+  void* ring_ws = nullptr;
+  int* counters = nullptr;  // [0] item counter, then done1[nchunks], done2[nchunks]
   int* err = nullptr;
 };
 
@@ -157,6 +183,8 @@ void free_plan(tcfftPlanImpl* p) {
   }
   cudaFree(p->ws);
   cudaFree(p->perm_ws);
+  cudaFree(p->ring_ws);
+  cudaFree(p->counters);
   cudaFree(p->err);
   delete p;
 }
@@ -187,7 +215,10 @@ int choose_tile(int prec, int kind, int logL, long long lines) {
   if (t >= 0 && t < kNumTileSel && g_tab[prec][kind][logL][t][0].fn) return t;
   const PassKernel& small = g_tab[prec][kind][logL][kTileSmall][0];
   const PassKernel& big = g_tab[prec][kind][logL][kTileBig][0];
-  if (!small.fn || !big.fn) return kTileBig;
+  const PassKernel& mid = g_tab[prec][kind][logL][kTileMid][0];
+  // prefetching mid tiles (3 CTAs/SM) when they fill the GPU, measured fastest
+  if (mid.fn && (lines + mid.G - 1) / mid.G >= 3ll * g_num_sms) return kTileMid;
+  if (!small.fn || !big.fn) return big.fn ? kTileBig : (mid.fn ? kTileMid : kTileSmall);
   const long long big_tiles = (lines + big.G - 1) / big.G;
   return big_tiles >= 2ll * g_num_sms ? kTileBig : kTileSmall;
 }
@@ -270,6 +301,60 @@ tcfftStatus exec_passes(tcfftPlanImpl* p, int prec, const void* in, void* out, i
     }
   }
   return s;
+}
+
+// Both four-step passes in one persistent launch (see fft_fused.cuh).
+tcfftStatus exec_fused(tcfftPlanImpl* p, const void* in, void* out, int sg, float scale, cudaStream_t st) {
+  const int logn = p->log_n1 + p->log_n2;
+  const FusedKernel& fk = g_fused[logn][sg];
+  const long long n1 = 1ll << p->log_n1, n2 = 1ll << p->log_n2;
+  IoHalf<false, false> a;
+  std::memset(&a, 0, sizeof(a));
+  a.in = static_cast<const half2*>(in);
+  a.out = static_cast<half2*>(p->ring_ws);
+  a.lps_log2 = p->log_n2;
+  a.in_seq = a.out_seq = p->n;
+  a.in_line = a.out_line = 1;
+  a.in_elem = a.out_elem = n2;
+  a.otw.hi = p->otw_hi[sg];
+  a.otw.lo = p->otw_lo[sg];
+  a.otw.shift = p->otw_shift;
+  a.otw.logn = p->otw_logn;
+  a.scale = 1.0f;
+  IoHalf<true, false, true> b;
+  std::memset(&b, 0, sizeof(b));
+  b.in = static_cast<const half2*>(p->ring_ws);
+  b.out = static_cast<half2*>(out);
+  b.lps_log2 = p->log_n1;
+  b.in_seq = b.out_seq = p->n;
+  b.in_line = n2;
+  b.in_elem = 1;
+  b.out_line = 1;
+  b.out_elem = n1;
+  b.scale = scale;
+  PassCore c1 = make_core(p, sg, p->log_n1), c2 = make_core(p, sg, p->log_n2);
+  FusedSched sc;
+  sc.counter = reinterpret_cast<unsigned int*>(p->counters);
+  sc.done1 = p->counters + 1;
+  sc.done2 = p->counters + 1 + p->nchunks;
+  sc.nchunks = p->nchunks;
+  sc.tiles1 = static_cast<int>((static_cast<long long>(p->chunk_seqs) * n2 + fk.G1 - 1) / fk.G1);
+  sc.tiles2 = static_cast<int>((static_cast<long long>(p->chunk_seqs) * n1 + fk.G2 - 1) / fk.G2);
+  sc.ring = p->ring;
+  sc.chunk_seqs = p->chunk_seqs;
+  sc.batch = p->batch;
+  sc.n = p->n;
+  if (cudaMemsetAsync(p->counters, 0, sizeof(int) * (1 + 2 * static_cast<size_t>(p->nchunks)), st) != cudaSuccess)
+    return TCFFT_LAUNCH_FAILED;
+  long long items = static_cast<long long>(sc.nchunks) * (sc.tiles1 + sc.tiles2);
+  long long grid = static_cast<long long>(g_num_sms) * g_fused_occ[logn][sg];
+  if (grid > items) grid = items;
+  void* args[] = {&a, &b, &c1, &c2, &sc};
+  if (cudaLaunchKernel(fk.fn, dim3(static_cast<unsigned>(grid)), dim3(kPassThreads), args,
+                       static_cast<size_t>(fk.smem), st) != cudaSuccess)
+    return TCFFT_LAUNCH_FAILED;
+  ++g_last_launches;
+  return TCFFT_OK;
 }
 
 __global__ void digitrev_gather_kernel(const half2* __restrict__ in, half2* __restrict__ out,
@@ -368,7 +453,23 @@ tcfftStatus tcfft_plan_1d(tcfftPlan* plan, long long n, long long batch, int pre
             gen_twiddles(p->otw_hi[d], nhi, logn, p->otw_shift, sg, 0) != cudaSuccess)
           s = TCFFT_LAUNCH_FAILED;
       }
-      if (s == TCFFT_OK) {
+      const bool can_fuse = precision == TCFFT_FP16 && logn >= kFusedMinLog && logn <= kFusedMaxLog &&
+                            g_fused[logn][0].fn && g_fused[logn][0].log_n1 == p->log_n1;
+      if (s == TCFFT_OK && can_fuse) {
+        // chunks of ~16 MiB; a ring of two workspace slots
+        const long long per_seq = n * 4;
+        long long cs = (16ll << 20) / per_seq;
+        if (cs < 1) cs = 1;
+        if (cs > batch) cs = batch;
+        p->chunk_seqs = static_cast<int>(cs);
+        p->nchunks = static_cast<int>((batch + cs - 1) / cs);
+        p->ring = p->nchunks >= 2 ? 2 : 1;
+        p->ws_bytes = static_cast<size_t>(p->ring) * static_cast<size_t>(cs) * static_cast<size_t>(per_seq);
+        if (cudaMalloc(&p->ring_ws, p->ws_bytes) != cudaSuccess ||
+            cudaMalloc(&p->counters, sizeof(int) * (1 + 2 * static_cast<size_t>(p->nchunks))) != cudaSuccess)
+          s = TCFFT_ALLOC_FAILED;
+        p->fused = true;
+      } else if (s == TCFFT_OK) {
         p->ws_bytes = static_cast<size_t>(n) * static_cast<size_t>(batch) * (precision == TCFFT_FP16 ? 4u : 8u);
         if (cudaMalloc(&p->ws, p->ws_bytes) != cudaSuccess) s = TCFFT_ALLOC_FAILED;
       }
@@ -412,6 +513,22 @@ tcfftStatus tcfft_plan_2d(tcfftPlan* plan, int nx, int ny, long long batch, int 
   return ret(TCFFT_OK);
 }
 
+tcfftStatus tcfft_plan_set_fused(tcfftPlan p, int enable) {
+  if (!p) return ret(TCFFT_INVALID_VALUE);
+  if (enable) {
+    if (!p->ring_ws) return ret(TCFFT_UNSUPPORTED);
+    p->fused = true;
+    return ret(TCFFT_OK);
+  }
+  if (!p->fused) return ret(TCFFT_OK);
+  if (!p->ws) {
+    const size_t bytes = static_cast<size_t>(p->n) * static_cast<size_t>(p->batch) * 4u;
+    if (cudaMalloc(&p->ws, bytes) != cudaSuccess) return ret(TCFFT_ALLOC_FAILED);
+  }
+  p->fused = false;
+  return ret(TCFFT_OK);
+}
+
 tcfftStatus tcfft_workspace_bytes(tcfftPlan plan, size_t* bytes) {
   if (!plan || !bytes) return ret(TCFFT_INVALID_VALUE);
   *bytes = plan->ws_bytes;
@@ -427,7 +544,9 @@ tcfftStatus tcfft_exec(tcfftPlan p, const void* in, void* out, int direction, fl
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int sg = direction == TCFFT_FORWARD ? 0 : 1;
   tcfftStatus s;
-  if (p->precision == TCFFT_FP16)
+  if (p->fused)
+    s = exec_fused(p, in, out, sg, scale, st);
+  else if (p->precision == TCFFT_FP16)
     s = exec_passes<IoHalf, half2>(p, kPrecF16, in, out, sg, scale, st);
   else
     s = exec_passes<IoFloat, float2>(p, kPrecSplit, in, out, sg, scale, st);
@@ -476,7 +595,7 @@ tcfftStatus tcfft_exec_digitrev(tcfftPlan p, const void* in, void* out, const in
 }
 
 tcfftStatus tcfft_exec_digitrev_2d(tcfftPlan p, const void* in, void* out, const int* radices_x, int n_radices_x,
-                                   const int* radices_y, int n_radices_y, void* stream) {
+                                   const int* radices_y, int n_radices_y, int direction, void* stream) {
   g_last_launches = 0;
   if (!p || !in || !out || n_radices_x < 0 || n_radices_x > 9 || n_radices_y < 0 || n_radices_y > 9 ||
       (n_radices_x > 0 && !radices_x) || (n_radices_y > 0 && !radices_y))
@@ -514,7 +633,7 @@ tcfftStatus tcfft_exec_digitrev_2d(tcfftPlan p, const void* in, void* out, const
     src = dst;
   }
   const int before = src != in ? 1 : 0;
-  tcfftStatus s = tcfft_exec(p, src, out, TCFFT_FORWARD, 1.0f, stream);
+  tcfftStatus s = tcfft_exec(p, src, out, direction, 1.0f, stream);
   g_last_launches += before;
   return ret(s);
 }

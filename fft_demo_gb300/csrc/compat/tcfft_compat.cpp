@@ -197,7 +197,7 @@ void tcfftExec_2d(tcfftHandle_2d plan, half* data) {
     return;
   }
   g_compat_status = tcfft_exec_digitrev_2d(native, data, data, plan.radices_x, plan.n_radices_x, plan.radices_y,
-                                           plan.n_radices_y, nullptr);
+                                           plan.n_radices_y, TCFFT_FORWARD, nullptr);
 }
 
 void tcfftDestroy_2d(tcfftHandle_2d* plan) {

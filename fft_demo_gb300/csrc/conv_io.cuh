@@ -150,6 +150,13 @@ struct IoColMaskCrop {
     return r;
   }
   __device__ __forceinline__ Raw fetch_l(long long, int, bool) const { return Raw{}; }
+  __device__ __forceinline__ const void* src_g(long long line0, int l, bool& ok) const {
+    ok = line0 < total_lines && l < valid_rows;
+    if (!ok) return in;
+    const long long img = line0 >> lps_log2;
+    const long long col = line0 & ((1ll << lps_log2) - 1);
+    return in + img * static_cast<long long>(valid_rows) * P + static_cast<long long>(l) * P + col;
+  }
   __device__ __forceinline__ void decode_g(const Raw& r, long long, int, float2 (&v)[4]) const {
 #pragma unroll
     for (int q = 0; q < 4; ++q) v[q] = from_elem(r.e[q]);

@@ -27,6 +27,17 @@ __device__ __forceinline__ uint4 ldg_nc_v4(const void* p) {
   return r;
 }
 
+// L2-coherent load (skips L1): for data written earlier in the same kernel by
+// other CTAs (the fused four-step workspace).
+__device__ __forceinline__ uint4 ldg_cg_v4(const void* p) {
+  uint4 r;
+  asm volatile("ld.global.cg.v4.u32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+               : "l"(p)
+               : "memory");
+  return r;
+}
+
 __device__ __forceinline__ void stg_v4(void* p, uint4 v) {
   asm volatile("st.global.v4.u32 [%0], {%1,%2,%3,%4};" ::"l"(p), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
                : "memory");
@@ -58,7 +69,9 @@ struct OuterTwiddle {
 };
 
 // Interleaved complex half in and out, arbitrary strides (in elements).
-template <bool IN_L, bool OUT_L>
+// COHERENT: input is read with L2-coherent loads (it is written by other CTAs
+// of the same launch).
+template <bool IN_L, bool OUT_L, bool COHERENT = false>
 struct IoHalf {
   static constexpr bool IN_VEC_L = IN_L;
   static constexpr bool OUT_VEC_L = OUT_L;
@@ -88,11 +101,25 @@ struct IoHalf {
   }
   __device__ __forceinline__ Raw fetch_l(long long line, int l0, bool ok) const {
     if (!ok || line >= total_lines) return make_uint4(0, 0, 0, 0);
+    if constexpr (COHERENT) return ldg_cg_v4(in + in_base(line) + l0);
     return ldg_nc_v4(in + in_base(line) + l0);
   }
   __device__ __forceinline__ Raw fetch_g(long long line0, int l, bool ok) const {
     if (!ok || line0 >= total_lines) return make_uint4(0, 0, 0, 0);
+    if constexpr (COHERENT) return ldg_cg_v4(in + in_base(line0) + static_cast<long long>(l) * in_elem);
     return ldg_nc_v4(in + in_base(line0) + static_cast<long long>(l) * in_elem);
+  }
+  // Source of the 16-byte chunk at element l of 4 adjacent lines / at
+  // elements l0..l0+3 of one line, for asynchronous copies; ok = false when
+  // the lines lie past the end (the copy then zero-fills).
+  __device__ __forceinline__ const void* src_g(long long line0, int l, bool& ok) const {
+    ok = line0 < total_lines;
+    return ok ? static_cast<const void*>(in + in_base(line0) + static_cast<long long>(l) * in_elem)
+              : static_cast<const void*>(in);
+  }
+  __device__ __forceinline__ const void* src_l(long long line, int l0, bool& ok) const {
+    ok = line < total_lines;
+    return ok ? static_cast<const void*>(in + in_base(line) + l0) : static_cast<const void*>(in);
   }
   __device__ __forceinline__ void decode_l(const Raw& r, long long, int, float2 (&v)[4]) const {
     unpack_h2x4(r, v);
@@ -114,9 +141,15 @@ struct IoHalf {
         w = cmulf(w, step);
       }
     }
+    const long long step = static_cast<long long>(J) * out_elem;
+    half2* q = p + static_cast<long long>(j) * out_elem;
+    if (scale == 1.0f) {
 #pragma unroll
-    for (int c = 0; c < 16; ++c)
-      p[static_cast<long long>(j + c * J) * out_elem] = __floats2half2_rn(v[c].x * scale, v[c].y * scale);
+      for (int c = 0; c < 16; ++c) q[c * step] = __floats2half2_rn(v[c].x, v[c].y);
+    } else {
+#pragma unroll
+      for (int c = 0; c < 16; ++c) q[c * step] = __floats2half2_rn(v[c].x * scale, v[c].y * scale);
+    }
   }
 };
 

@@ -263,13 +263,29 @@ __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const f
       } else {
         float2 w = __ldg(tw + e0);
         const float2 wstep = __ldg(tw + de);
+        // column step between consecutive outputs: Ns (line-major) or Ns*G
+        // (line-minor); when it is a multiple of 64 (one swizzle atom) the
+        // swizzled offset moves by a compile-time amount per output
+        constexpr uint32_t CSTEP = LINE_MINOR ? static_cast<uint32_t>(Ns * G) : static_cast<uint32_t>(Ns);
+        if constexpr (CSTEP % 64 == 0) {
+          const uint32_t mp0 = static_cast<uint32_t>(Tl::pos(g, jp0));
+          const uint32_t off0 =
+              krow + (mp0 >> 6) * 1024u + ((((mp0 & 63u) >> 3) ^ (rp & 7)) << 4) + (mp0 & 7u) * 2u;
 #pragma unroll
-        for (int c = 0; c < 16; ++c) {
-          const float2 x = cmulf(make_float2(__uint_as_float(d[c]), __uint_as_float(d[16 + c])), w);
-          w = cmulf(w, wstep);
-          const uint32_t mp = static_cast<uint32_t>(Tl::pos(g, jp0 + c * Ns));
-          const uint32_t off = krow + (mp >> 6) * 1024u + ((((mp & 63u) >> 3) ^ (rp & 7)) << 4) + (mp & 7u) * 2u;
-          st_pair(re, im, off, x);
+          for (int c = 0; c < 16; ++c) {
+            const float2 x = cmulf(make_float2(__uint_as_float(d[c]), __uint_as_float(d[16 + c])), w);
+            w = cmulf(w, wstep);
+            st_pair(re, im, off0 + static_cast<uint32_t>(c) * (CSTEP / 64u) * 1024u, x);
+          }
+        } else {
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            const float2 x = cmulf(make_float2(__uint_as_float(d[c]), __uint_as_float(d[16 + c])), w);
+            w = cmulf(w, wstep);
+            const uint32_t mp = static_cast<uint32_t>(Tl::pos(g, jp0 + c * Ns));
+            const uint32_t off = krow + (mp >> 6) * 1024u + ((((mp & 63u) >> 3) ^ (rp & 7)) << 4) + (mp & 7u) * 2u;
+            st_pair(re, im, off, x);
+          }
         }
       }
     }
@@ -335,6 +351,58 @@ __device__ __forceinline__ void pass_teardown(PassState& st) {
   tc_fence_before_sync();
   __syncthreads();
   if ((threadIdx.x >> 5) == 0) tmem_dealloc(st.tbase, TMEM_COLS);
+}
+
+// The S radix-16 tensor-core stages of one tile held in the planes (MMA
+// batch, commit, bounded wait, epilogue). False if a wait gave up.
+template <int L, int G, bool LINE_MINOR, int SIGN, class IO>
+__device__ __forceinline__ bool run_stages(PassState& st, const IO& io, const PassCore& core, long long line0,
+                                           uint8_t* re, uint8_t* im, bool stage_out) {
+  using Sh = LineShape<L>;
+  using Tl = Tile<L, G, LINE_MINOR>;
+  constexpr int S = Sh::S;
+  constexpr int NG = Tl::Mt / 128;
+  constexpr uint32_t KSTRIDE = Tl::KSTRIDE;
+  constexpr uint32_t IDESC = make_idesc_f16_f32(128, 32, true, false);
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5;
+  const int lane = tid & 31;
+  bool timed_out = false;
+    // ================= radix-16 tensor-core stages =================
+    auto run_stage = [&](auto s_const) {
+      constexpr int s = decltype(s_const)::value;
+      if (timed_out) return;
+      if (tid == 0) {
+        tc_fence_after_sync();
+        const uint32_t a0 = smem_u32(re), a1 = smem_u32(im), b0 = smem_u32(st.bmat);
+        const uint64_t bd0 = make_sdesc(b0, 128u, 512u, kLayoutNone);
+        const uint64_t bd1 = make_sdesc(b0 + 256u, 128u, 512u, kLayoutNone);
+#pragma unroll
+        for (int grp = 0; grp < NG; ++grp) {
+          const uint64_t ad0 = make_sdesc(a0 + grp * 2048u, 1024u, KSTRIDE, kLayoutSw128);
+          const uint64_t ad1 = make_sdesc(a1 + grp * 2048u, 1024u, KSTRIDE, kLayoutSw128);
+          umma_f16(st.tbase + grp * 32u, ad0, bd0, IDESC, 0u);
+          umma_f16(st.tbase + grp * 32u, ad1, bd1, IDESC, 1u);
+        }
+        umma_commit(st.mbar);
+      }
+      bool to = !mbar_wait_bounded(st.mbar, st.phase & 1u);
+      if (to && lane == 0) atomicOr(core.err, kErrMmaTimeout);
+      st.phase++;
+      if (__syncthreads_or(to)) {
+        timed_out = true;
+        return;
+      }
+      tc_fence_after_sync();
+      stage_epilogue<L, G, LINE_MINOR, s, IO>(re, im, core.tw, st.tbase, warp, lane, io, line0, stage_out);
+      fence_proxy_async_smem();
+      tc_fence_before_sync();
+      __syncthreads();
+    };
+    [&]<int... Is>(std::integer_sequence<int, Is...>) {
+      (run_stage(std::integral_constant<int, Is>{}), ...);
+    }(std::make_integer_sequence<int, S>{});
+    return !timed_out;
 }
 
 // ---------------------------------------------------------------------------
@@ -559,41 +627,7 @@ __device__ __forceinline__ bool pass_tile(PassState& st, const IO& io, const Pas
     tc_fence_before_sync();
     __syncthreads();
 
-    // ================= radix-16 tensor-core stages =================
-    auto run_stage = [&](auto s_const) {
-      constexpr int s = decltype(s_const)::value;
-      if (timed_out) return;
-      if (tid == 0) {
-        tc_fence_after_sync();
-        const uint32_t a0 = smem_u32(re), a1 = smem_u32(im), b0 = smem_u32(st.bmat);
-        const uint64_t bd0 = make_sdesc(b0, 128u, 512u, kLayoutNone);
-        const uint64_t bd1 = make_sdesc(b0 + 256u, 128u, 512u, kLayoutNone);
-#pragma unroll
-        for (int grp = 0; grp < NG; ++grp) {
-          const uint64_t ad0 = make_sdesc(a0 + grp * 2048u, 1024u, KSTRIDE, kLayoutSw128);
-          const uint64_t ad1 = make_sdesc(a1 + grp * 2048u, 1024u, KSTRIDE, kLayoutSw128);
-          umma_f16(st.tbase + grp * 32u, ad0, bd0, IDESC, 0u);
-          umma_f16(st.tbase + grp * 32u, ad1, bd1, IDESC, 1u);
-        }
-        umma_commit(st.mbar);
-      }
-      bool to = !mbar_wait_bounded(st.mbar, st.phase & 1u);
-      if (to && lane == 0) atomicOr(core.err, kErrMmaTimeout);
-      st.phase++;
-      if (__syncthreads_or(to)) {
-        timed_out = true;
-        return;
-      }
-      tc_fence_after_sync();
-      stage_epilogue<L, G, LINE_MINOR, s, IO>(re, im, core.tw, st.tbase, warp, lane, io, line0, stage_out);
-      fence_proxy_async_smem();
-      tc_fence_before_sync();
-      __syncthreads();
-    };
-    [&]<int... Is>(std::integer_sequence<int, Is...>) {
-      (run_stage(std::integral_constant<int, Is>{}), ...);
-    }(std::make_integer_sequence<int, S>{});
-    if (timed_out) return false;
+    if (!run_stages<L, G, LINE_MINOR, SIGN, IO>(st, io, core, line0, re, im, stage_out)) return false;
     if (stage_out && tid == 0) {
       // the last stage left the tile in natural order: one bulk store
       bulk_s2g(io.tile_dst(line0), re, static_cast<uint32_t>(nval) * L * 4u);
@@ -620,6 +654,236 @@ __global__ void __launch_bounds__(kPassThreads, MINB) fft_pass_f16(const IO io, 
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
     if (!pass_tile<L, G, LINE_MINOR, SIGN, IO>(st, io, core, tile * G)) break;
   pass_teardown<TMEM_COLS>(st);
+}
+
+// ---------------------------------------------------------------------------
+// Prefetching pass kernel. Each CTA owns a raw input buffer beside the
+// planes; tile t+1's input streams into it (one TMA bulk copy for contiguous
+// tiles, 16-byte cp.async chunks otherwise) while tile t runs its
+// tensor-core stages, so the load latency leaves the critical path.
+//   shared memory: [B matrix, barriers][planes: 2*PLANE][raw: 2*PLANE]
+//   raw layout: natural [line][l] half2 (vector-along-line inputs) or
+//               line-minor [l][line] half2 (column inputs)
+// ---------------------------------------------------------------------------
+template <int L, int G, bool LINE_MINOR, class IO>
+__device__ __forceinline__ void prefetch_tile(PassState& st, const IO& io, long long line0, uint8_t* raw) {
+  if (IO::IN_VEC_L && io.in_contig) {
+    if (threadIdx.x == 0) {
+      const long long rem = io.total_lines - line0;
+      const int nval = rem < G ? static_cast<int>(rem) : G;
+      const uint32_t bytes = static_cast<uint32_t>(nval) * L * 4u;
+      mbar_arrive_expect_tx(st.tma_bar, bytes);
+      bulk_g2s(raw, io.tile_src(line0), bytes, st.tma_bar);
+    }
+  } else if constexpr (!IO::IN_VEC_L) {
+    constexpr int GQ = G / 4;
+    constexpr int CH = L * GQ;
+#pragma unroll 4
+    for (int c = threadIdx.x; c < CH; c += kPassThreads) {
+      const int l = c / GQ, q = c % GQ;
+      bool ok;
+      const void* src = io.src_g(line0 + 4 * q, l, ok);
+      cp_async16(raw + (static_cast<uint32_t>(l) * G + 4u * q) * 4u, src, ok ? 16u : 0u);
+    }
+    cp_async_commit();
+  } else {
+    constexpr int QPL = L / 4;
+    constexpr int CH = G * QPL;
+#pragma unroll 4
+    for (int c = threadIdx.x; c < CH; c += kPassThreads) {
+      const int g = c / QPL, q = c % QPL;
+      bool ok;
+      const void* src = io.src_l(line0 + g, 4 * q, ok);
+      cp_async16(raw + (static_cast<uint32_t>(g) * L + 4u * q) * 4u, src, ok ? 16u : 0u);
+    }
+    cp_async_commit();
+  }
+}
+
+// Wait for the prefetched tile (whole CTA). False if the bounded wait gave up.
+template <class IO>
+__device__ __forceinline__ bool wait_prefetch(PassState& st, const IO& io, const PassCore& core) {
+  if (IO::IN_VEC_L && io.in_contig) {
+    const bool ok = mbar_wait_bounded(st.tma_bar, st.tma_phase & 1u);
+    st.tma_phase++;
+    if (!ok && (threadIdx.x & 31) == 0) atomicOr(core.err, kErrMmaTimeout);
+    return !__syncthreads_or(!ok);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  return true;
+}
+
+// raw (staged input) -> planes, with the radix-T first stage and the first
+// radix-16 stage's twiddle. Lines >= nval read as zero.
+template <int L, int G, bool LINE_MINOR, int SIGN, class IO>
+__device__ __forceinline__ void permute_raw(const uint8_t* raw, uint8_t* re, uint8_t* im, const PassCore& core,
+                                            int nval) {
+  using Sh = LineShape<L>;
+  using Tl = Tile<L, G, LINE_MINOR>;
+  constexpr int T = Sh::T;
+  constexpr int J = Sh::J;
+  const int tid = threadIdx.x;
+  const uint4 zero = make_uint4(0, 0, 0, 0);
+  if constexpr (IO::IN_VEC_L) {
+    constexpr int QPL = (L / T) / 4;
+    constexpr int ITEMS = G * QPL;
+#pragma unroll 2
+    for (int it = tid; it < ITEMS; it += kPassThreads) {
+      const int g = it / QPL;
+      const int j0 = (it % QPL) * 4;
+      uint4 w[T];
+#pragma unroll
+      for (int r = 0; r < T; ++r)
+        w[r] = g < nval ? *reinterpret_cast<const uint4*>(raw + (static_cast<uint32_t>(g) * L + j0 + r * (L / T)) * 4u)
+                        : zero;
+      if constexpr (T == 1 && !LINE_MINOR && J >= 4) {
+        uint2 rr, ii;
+        rr.x = __byte_perm(w[0].x, w[0].y, 0x5410);
+        rr.y = __byte_perm(w[0].z, w[0].w, 0x5410);
+        ii.x = __byte_perm(w[0].x, w[0].y, 0x7632);
+        ii.y = __byte_perm(w[0].z, w[0].w, 0x7632);
+        const uint32_t off = Tl::off(g, j0);
+        *reinterpret_cast<uint2*>(re + off) = rr;
+        *reinterpret_cast<uint2*>(im + off) = ii;
+      } else {
+        float2 v[T][4];
+#pragma unroll
+        for (int r = 0; r < T; ++r) unpack_h2x4(w[r], v[r]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          float2 t[T];
+#pragma unroll
+          for (int r = 0; r < T; ++r) t[r] = v[r][q];
+          small_dft<T, SIGN>(t);
+          const int j = j0 + q;
+#pragma unroll
+          for (int c = 0; c < T; ++c) {
+            const int lp = j * T + c;
+            float2 x = t[c];
+            if constexpr (T > 1) {
+              const int rp = lp / J, jp = lp % J;
+              x = cmulf(x, __ldg(core.tw + rp * (jp % T) * (L / (16 * T))));
+            }
+            st_pair(re, im, Tl::off(g, lp), x);
+          }
+        }
+      }
+    }
+  } else {
+    constexpr int GQ = G / 4;
+    constexpr int ITEMS = GQ * (L / T);
+#pragma unroll 2
+    for (int it = tid; it < ITEMS; it += kPassThreads) {
+      const int j = it / GQ;
+      const int g0 = (it % GQ) * 4;
+      uint4 w[T];
+#pragma unroll
+      for (int r = 0; r < T; ++r)
+        w[r] = *reinterpret_cast<const uint4*>(raw + (static_cast<uint32_t>(j + r * (L / T)) * G + g0) * 4u);
+      if constexpr (T == 1 && LINE_MINOR) {
+        uint2 rr, ii;
+        rr.x = __byte_perm(w[0].x, w[0].y, 0x5410);
+        rr.y = __byte_perm(w[0].z, w[0].w, 0x5410);
+        ii.x = __byte_perm(w[0].x, w[0].y, 0x7632);
+        ii.y = __byte_perm(w[0].z, w[0].w, 0x7632);
+        const uint32_t off = Tl::off(g0, j);
+        *reinterpret_cast<uint2*>(re + off) = rr;
+        *reinterpret_cast<uint2*>(im + off) = ii;
+      } else {
+        float2 v[T][4];
+#pragma unroll
+        for (int r = 0; r < T; ++r) unpack_h2x4(w[r], v[r]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          float2 t[T];
+#pragma unroll
+          for (int r = 0; r < T; ++r) t[r] = v[r][q];
+          small_dft<T, SIGN>(t);
+#pragma unroll
+          for (int r = 0; r < T; ++r) v[r][q] = t[r];
+        }
+#pragma unroll
+        for (int c = 0; c < T; ++c) {
+          const int lp = j * T + c;
+          float2 x[4] = {v[c][0], v[c][1], v[c][2], v[c][3]};
+          if constexpr (T > 1) {
+            const int rp = lp / J, jp = lp % J;
+            const float2 tw = __ldg(core.tw + rp * (jp % T) * (L / (16 * T)));
+#pragma unroll
+            for (int q = 0; q < 4; ++q) x[q] = cmulf(x[q], tw);
+          }
+          if constexpr (LINE_MINOR) {
+            st_quad(re, im, Tl::off(g0, lp), x);
+          } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) st_pair(re, im, Tl::off(g0 + q, lp), x[q]);
+          }
+        }
+      }
+    }
+  }
+}
+
+template <int L, int G, bool LINE_MINOR, int SIGN, class IO, int MINB = 3>
+__global__ void __launch_bounds__(kPassThreads, MINB) fft_pass_f16_pf(const IO io, const PassCore core) {
+  using Tl = Tile<L, G, LINE_MINOR>;
+  constexpr uint32_t TMEM_COLS = pass_tmem_cols<L, G>();
+  static_assert(TMEM_COLS >= 32 && (TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM columns");
+  static_assert(G % 4 == 0 || IO::IN_VEC_L, "line-vectorised loads need G % 4 == 0");
+  PassState st;
+  pass_setup<TMEM_COLS>(st, core.bmat);
+  uint8_t* re = st.smem + kPlaneOffset;
+  uint8_t* im = re + Tl::PLANE;
+  uint8_t* raw = re + 2 * Tl::PLANE;
+  const bool stage_out = IO::OUT_VEC_L && io.out_contig && !LINE_MINOR;
+  const bool tma_in = IO::IN_VEC_L && io.in_contig;
+  const long long ntiles = (io.total_lines + G - 1) / G;
+  long long tile = blockIdx.x;
+  bool pending = false;
+  if (tile < ntiles) {
+    prefetch_tile<L, G, LINE_MINOR, IO>(st, io, tile * G, raw);
+    pending = true;
+  }
+  for (; tile < ntiles; tile += gridDim.x) {
+    const long long line0 = tile * G;
+    const long long rem = io.total_lines - line0;
+    const int nval = rem < G ? static_cast<int>(rem) : G;
+    if (!wait_prefetch(st, io, core)) {
+      pending = false;
+      break;
+    }
+    pending = false;
+    if (stage_out && threadIdx.x == 0) bulk_wait_read_all();  // previous store has read the planes
+    __syncthreads();
+    permute_raw<L, G, LINE_MINOR, SIGN, IO>(raw, re, im, core, nval);
+    fence_proxy_async_smem();
+    tc_fence_before_sync();
+    __syncthreads();
+    if (tile + gridDim.x < ntiles) {
+      prefetch_tile<L, G, LINE_MINOR, IO>(st, io, (tile + gridDim.x) * G, raw);
+      pending = true;
+    }
+    if (!run_stages<L, G, LINE_MINOR, SIGN, IO>(st, io, core, line0, re, im, stage_out)) break;
+    if (stage_out && threadIdx.x == 0) {
+      bulk_s2g(io.tile_dst(line0), re, static_cast<uint32_t>(nval) * L * 4u);
+      bulk_commit();
+    }
+  }
+  // an early exit may leave a prefetch in flight: let it land before the CTA ends
+  if (pending) {
+    if (tma_in) {
+      mbar_wait_bounded(st.tma_bar, st.tma_phase & 1u);
+    } else {
+      cp_async_wait_all();
+    }
+  }
+  pass_teardown<TMEM_COLS>(st);
+}
+
+template <int L, int G>
+constexpr int pass_pf_smem_bytes() {
+  return static_cast<int>(kPlaneOffset) + 4 * (G * L / 16) * 32 + 1024;
 }
 
 // Dynamic shared memory bytes for a pass kernel instance (+1 KB alignment slack).

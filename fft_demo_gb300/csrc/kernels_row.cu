@@ -24,14 +24,14 @@ void register_row_kernels(PassTable& tab) {
   fill_entry<4096, 1024, false, true, true>(tab, kTileBig);
   fill_entry<8192, 1024, false, true, true>(tab, kTileBig);
   fill_entry<16384, 1024, false, true, true>(tab, kTileBig);
-  fill_entry<64, 512, false, true, true, 3>(tab, kTileMid);
-  fill_entry<128, 512, false, true, true, 3>(tab, kTileMid);
-  fill_entry<256, 512, false, true, true, 3>(tab, kTileMid);
-  fill_entry<512, 512, false, true, true, 3>(tab, kTileMid);
-  fill_entry<1024, 512, false, true, true, 3>(tab, kTileMid);
-  fill_entry<2048, 512, false, true, true, 3>(tab, kTileMid);
-  fill_entry<4096, 512, false, true, true, 3>(tab, kTileMid);
-  fill_entry<8192, 512, false, true, true, 3>(tab, kTileMid);
+  fill_pf_entry<64, 512, false, true, true, 3>(tab, kTileMid);
+  fill_pf_entry<128, 512, false, true, true, 3>(tab, kTileMid);
+  fill_pf_entry<256, 512, false, true, true, 3>(tab, kTileMid);
+  fill_pf_entry<512, 512, false, true, true, 3>(tab, kTileMid);
+  fill_pf_entry<1024, 512, false, true, true, 3>(tab, kTileMid);
+  fill_pf_entry<2048, 512, false, true, true, 3>(tab, kTileMid);
+  fill_pf_entry<4096, 512, false, true, true, 3>(tab, kTileMid);
+  fill_pf_entry<8192, 512, false, true, true, 3>(tab, kTileMid);
 }
 
 }  // namespace tcfft

@@ -15,12 +15,12 @@ void register_rowt_kernels(PassTable& tab) {
   fill_entry<1024, 1024, true, true, false>(tab, kTileBig);
   fill_entry<2048, 1024, true, true, false>(tab, kTileBig);
   fill_entry<4096, 1024, true, true, false>(tab, kTileBig);
-  fill_entry<64, 512, true, true, false, 3>(tab, kTileMid);
-  fill_entry<128, 512, true, true, false, 3>(tab, kTileMid);
-  fill_entry<256, 512, true, true, false, 3>(tab, kTileMid);
-  fill_entry<512, 512, true, true, false, 3>(tab, kTileMid);
-  fill_entry<1024, 512, true, true, false, 3>(tab, kTileMid);
-  fill_entry<2048, 512, true, true, false, 3>(tab, kTileMid);
+  fill_pf_entry<64, 512, true, true, false, 3>(tab, kTileMid);
+  fill_pf_entry<128, 512, true, true, false, 3>(tab, kTileMid);
+  fill_pf_entry<256, 512, true, true, false, 3>(tab, kTileMid);
+  fill_pf_entry<512, 512, true, true, false, 3>(tab, kTileMid);
+  fill_pf_entry<1024, 512, true, true, false, 3>(tab, kTileMid);
+  fill_pf_entry<2048, 512, true, true, false, 3>(tab, kTileMid);
 }
 
 }  // namespace tcfft

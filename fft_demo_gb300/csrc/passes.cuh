@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "fft_fused.cuh"
 #include "fft_io.cuh"
 #include "fft_split.cuh"
 #include "fft_tile.cuh"
@@ -64,6 +65,23 @@ void fill_entry(PassTable& tab, int tile) {
   tab[LOG][tile][1] = i;
 }
 
+// Prefetching variant (raw input buffer beside the planes; fft_pass_f16_pf).
+template <int L, int Mt, bool LINE_MINOR, bool IN_VEC_L, bool OUT_VEC_L, int MINB = 3>
+void fill_pf_entry(PassTable& tab, int tile) {
+  constexpr int G = tile_lines<L, Mt>();
+  constexpr int LOG = ilog2c(L);
+  const int smem = pass_pf_smem_bytes<L, G>();
+  PassKernel f, i;
+  using IO = IoHalf<IN_VEC_L, OUT_VEC_L>;
+  f.fn = reinterpret_cast<const void*>(&fft_pass_f16_pf<L, G, LINE_MINOR, -1, IO, MINB>);
+  i.fn = reinterpret_cast<const void*>(&fft_pass_f16_pf<L, G, LINE_MINOR, +1, IO, MINB>);
+  f.smem = i.smem = smem;
+  f.G = i.G = G;
+  f.Mt = i.Mt = Mt;
+  tab[LOG][tile][0] = f;
+  tab[LOG][tile][1] = i;
+}
+
 template <int L, int Mt, bool LINE_MINOR, bool IN_VEC_L, bool OUT_VEC_L>
 void fill_split_entry(PassTable& tab, int tile) {
   constexpr int G = tile_lines<L, Mt>();
@@ -78,6 +96,33 @@ void fill_split_entry(PassTable& tab, int tile) {
   f.Mt = i.Mt = Mt;
   tab[LOG][tile][0] = f;
   tab[LOG][tile][1] = i;
+}
+
+// Fused four-step kernels, indexed by log2 N (15..24) and direction.
+constexpr int kFusedMinLog = 15, kFusedMaxLog = 24;
+struct FusedKernel {
+  const void* fn = nullptr;
+  int smem = 0;
+  int log_n1 = 0, log_n2 = 0;
+  int G1 = 0, G2 = 0;
+};
+using FusedTable = FusedKernel[kFusedMaxLog + 1][2];
+void register_fused_kernels(FusedTable& tab);
+
+template <int L1, int L2>
+void fill_fused(FusedTable& tab) {
+  constexpr int G1 = 16384 / L1, G2 = 16384 / L2;
+  constexpr int LOG = ilog2c(static_cast<long long>(L1) * L2);
+  FusedKernel f, i;
+  f.fn = reinterpret_cast<const void*>(&fft_fourstep_fused<L1, G1, L2, G2, -1>);
+  i.fn = reinterpret_cast<const void*>(&fft_fourstep_fused<L1, G1, L2, G2, +1>);
+  f.smem = i.smem = fused_smem_bytes<L1, G1, L2, G2>();
+  f.log_n1 = i.log_n1 = ilog2c(L1);
+  f.log_n2 = i.log_n2 = ilog2c(L2);
+  f.G1 = i.G1 = G1;
+  f.G2 = i.G2 = G2;
+  tab[LOG][0] = f;
+  tab[LOG][1] = i;
 }
 
 }  // namespace tcfft

@@ -1,0 +1,187 @@
+// Drop-in replacement for yuelingfan/fft_demo tensorcore_fft_conv2d.h: the
+// FFT-convolution class fft_conv2d_half with the same enums, plan struct,
+// public members and method signatures (tensorcore_fft_conv2d.h:1-196),
+// served by the sm_103a library behind include/tcfft_gb300.h.
+//
+// Semantics kept (reference file:line):
+//   fft_conv2d_half(signal, filter, S, F, sy, sx, fy, fx, GPU)  (.cpp:12)
+//       host FP64 signal [S][sy][sx] and filters [F][S][fy][fx]; filters are
+//       transformed once and kept on the device
+//   conv2d_forward(output)           (.cpp:283) output [F][sy-fy+1][sx-fx+1]
+//       (host FP64) = sum over channels of the valid cross-correlation
+//   conv2d_forward(signal, filter, output, S, F, sy, sx, fy, fx, GPU) (.cpp:291)
+//   conv2d_backward(delta_in)        (.cpp:364) fills delta_for_filter
+//       [F][S][fy][fx] and delta_for_signal [S][sy][sx] (host FP64, malloc'ed)
+//   fft_2d_c2c / ifft_2d_c2c         (.cpp:79,147) host FP64 complex
+//       [batch][y][x] -> 2D (inverse) FFT, unnormalised
+//   TensorCoreFFTCreate / TensorCoreFFTExec (kernel.cu:1557,1495,1526):
+//       bidirectional 2D plan over half2 data whose axes are digit-reversed
+//       as gen_rev's rev tables order them
+// Differences: any image size whose padded transform fits (P <= 4096, the
+// reference stops at 512); FP32 channel sum without the per-tile power-of-ten
+// quantisation; the backward pass computes the true gradients (the
+// reference's readout offsets are written for square, equal-size cases);
+// `GPU` (__VOLTA__/__AMPERE__) is accepted and ignored. Internal pipeline
+// steps of the reference (fft_pointwise, quant kernels, ...) are kept as
+// declarations so code naming them compiles; see their comments below.
+#pragma once
+#include <array>
+#include <cstdio>
+#include <cstdlib>
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <string>
+
+enum __GPU_ARCH__
+{
+    __VOLTA__,
+    __AMPERE__
+};
+
+enum __OBJ__
+{
+    __SIGNAL__,
+    __FILTER__
+};
+
+/// fft = 1 -> forward, fft = -1 -> inverse (unnormalised)
+struct fftPlan
+{
+    __GPU_ARCH__ GPU = __AMPERE__;
+    __OBJ__ OBJ = __SIGNAL__;
+    int fft;
+    int Nx, Ny, N_batch;
+    int radices_x[3] = {16, 16, 2};
+    int radices_y[3] = {16, 16, 2};
+    int n_radices_x, n_radices_y;
+    int mergings[2] = {0, 0};
+    void (*layer_0[3])(half2 *, half *, half *, int fft);
+    void (*layer_1[3])(int, half2 *, half *, half *, int fft);
+    half *F_real, *F_imag;
+    half *F_real_tmp, *F_imag_tmp;  // F_real_tmp carries the native plan handle
+};
+
+class fft_conv2d_half
+{
+public:
+    std::string workpath;
+    __GPU_ARCH__ GPU;
+
+    int sx;
+    int sy;
+    int fx;
+    int fy;
+    int S;
+    int F;
+    int padded_x;
+    int padded_y;
+    int output_x;
+    int output_y;
+
+    double *signal;
+    double *filter;
+    double *cu_signal;
+    double *cu_filter;
+
+    half *cu_signal_padded;
+    half *cu_filter_padded;
+
+    int *rev_x_cu;
+    int *rev_y_cu;
+    int rev_256[1024];  // digit-reversal tables (filled by gen_rev)
+    int rev_512[1024];
+
+    void print_cu(half *src, int x, int y, int item_per_group, int batch);
+    void print_cu(float *src, int x, int y, int item_per_group, int batch);
+    void print_cu(double *src, int x, int y, int item_per_group, int batch);
+    void printplan(fftPlan plan);
+
+    // digit-reverse + FP64 -> FP16 of a [batch][y][x] complex device array
+    void rev(double *src, half *dst, int x, int y, int batch, int offset, cudaStream_t stream);
+    void TensorCoreFFTCreate(fftPlan *plan, int nx, int ny, int n_batch, int fft, __GPU_ARCH__ GPU);
+    void TensorCoreFFTExec(fftPlan plan, half *data, cudaStream_t stream);
+    void TensorCoreFFTExec(fftPlan plan, half *data);
+    void TensorCoreFFTDestroy(fftPlan *plan);  // added: the reference leaks plans
+    void gen_rev(int Nx, int Ny);
+    void read_out_scale_half2double(half *src, double *dst, double *dst_in_host, int src_x, int src_y, int dst_x,
+                                    int dst_y, int batch, double scale);
+    void read_out_scale_double2double(double *src, double *dst, double *dst_in_host, int src_x, int src_y,
+                                      int dst_x, int dst_y, int batch, double scale = 1.0);
+
+    void half2double(half *src, double *dst, int x, int y, int item_per_group, int batch, cudaStream_t stream);
+    void double2half(double *src, half *dst, int x, int y, int item_per_group, int batch);
+
+    void fft_2d_c2c(double *input, double *output, int x, int y, int batch, __GPU_ARCH__ GPU, int num_streams = 8,
+                    bool benchmark = false);
+    void ifft_2d_c2c(double *input, double *output, int x, int y, int batch, __GPU_ARCH__ GPU, int num_streams = 8,
+                     bool benchmark = false);
+
+    fft_conv2d_half();
+    fft_conv2d_half(int in_channel, int out_channel, int kernel_size, __GPU_ARCH__ GPU);
+    fft_conv2d_half(double *signal, double *filter, int S, int F, int sy, int sx, int fy, int fx, __GPU_ARCH__ GPU);
+    ~fft_conv2d_half();
+
+    void tmp_test();
+    std::string toString();
+
+    /*FOR CONV2D FORWARD-PROPAGATION*/
+    double *output;
+
+    fftPlan plan_signal;
+    fftPlan plan_filter;
+    fftPlan plan_pointwise;
+
+    float *cu_pointwise_float;
+    half *cu_pointwise_half;
+    float *max_per_line;
+    float *max_per_tile;
+
+    double *cu_conv2d_forward_result_padded;
+
+    // The reference's internal forward steps. The whole pipeline runs in
+    // conv2d_forward here; these entry points run it too (fft_conv2d_inv_rev_pad
+    // and fft_pointwise/fft_conv_final_stage/readout_fwd are no-ops that keep
+    // the names available; TENSORCORE_FFT_CONV_2D computes into `output`).
+    void fft_conv2d_inv_rev_pad();
+    void conv2d_forward(double *output);
+    void TENSORCORE_FFT_CONV_2D();
+    void readout_fwd(bool free = true);
+    void fft_pointwise(float scale = 1.0, bool use_more_G_memory = true);
+    void fft_conv_final_stage();
+
+    void conv2d_forward(double *input, double *weight, double *output, int S, int F, int sy, int sx, int fy, int fx,
+                        __GPU_ARCH__ GPU);
+
+    /*FOR CONV2D BACKWARD-PROPAGATION*/
+    fftPlan plan_delta_in_for_bp_filter;
+    fftPlan plan_signal_for_bp_filter;
+    fftPlan plan_pointwise_for_bp_filter;
+
+    fftPlan plan_delta_in_for_bp_signal;
+    fftPlan plan_filter_for_bp_signal;
+    fftPlan plan_pointwise_for_bp_signal;
+
+    double *cu_delta_in;
+    half *cu_delta_in_padded;
+    half *cu_pointwise_for_delta_filter;
+    half *cu_pointwise_for_delta_signal;
+
+    double *delta_weight_double;
+
+    double *delta_for_filter;
+    double *delta_for_signal;
+
+    // Internal backward steps of the reference: kept as names (no-ops);
+    // conv2d_backward computes both gradients.
+    void fft_conv2d_rev_pad(double *siganl, double *filter, half *signal_padded, half *filter_padded, int padded_x,
+                            int sx, int fx, int S, int F);
+    void inv_pad_deltain_signal(int padded_x);
+    void pad_fx_1_circles_of_0(double *cu_delta_in_0_padded, int k, int x, int y);
+    void pointwise_for_delta_weight(int padded_x);
+    void pointwise_for_delta_input(int padded_x, half *delta_for_input_pointwise);
+    void conv2d_backward(double *delta_in);
+
+    // Added: the native convolution plan behind this object (tcfftConv).
+    void *native_conv = nullptr;
+    int last_status = 0;
+};

@@ -62,6 +62,12 @@ tcfftStatus tcfft_plan_1d(tcfftPlan *plan, long long n, long long batch, int pre
  * nx, ny = 2^k in [16, 4096]. */
 tcfftStatus tcfft_plan_2d(tcfftPlan *plan, int nx, int ny, long long batch, int precision);
 
+/* 1D FP16 plans with 2^15 <= n <= 2^24 run both four-step passes in one
+ * persistent launch that keeps the intermediate in a small L2-resident
+ * workspace ring (default). enable = 0 switches the plan to two separate
+ * pass launches through a full-size workspace (allocated on first use). */
+tcfftStatus tcfft_plan_set_fused(tcfftPlan plan, int enable);
+
 /* Bytes of device workspace the plan holds (allocated at plan time). */
 tcfftStatus tcfft_workspace_bytes(tcfftPlan plan, size_t *bytes);
 
@@ -77,12 +83,14 @@ tcfftStatus tcfft_exec(tcfftPlan plan, const void *in, void *out, int direction,
 tcfftStatus tcfft_exec_digitrev(tcfftPlan plan, const void *in, void *out, const int *radices,
                                 int n_radices, void *stream);
 
-/* 2D forward transform of input whose rows are stored in the digit-reversed
- * order of radices_x and whose elements within a row follow radices_y, as the
- * reference's setup_2d() prepares (tcfft_half_2d.cu:1253-1273). 2D FP16 plans. */
+/* 2D transform (direction TCFFT_FORWARD / TCFFT_INVERSE, unnormalised) of
+ * input whose rows are stored in the digit-reversed order of radices_x and
+ * whose elements within a row follow radices_y, as the reference's
+ * setup_2d() (tcfft_half_2d.cu:1253-1273) and fft_conv2d_half's rev tables
+ * (tensorcore_fft_conv2d.h:72,96) prepare. 2D FP16 plans. */
 tcfftStatus tcfft_exec_digitrev_2d(tcfftPlan plan, const void *in, void *out, const int *radices_x,
                                    int n_radices_x, const int *radices_y, int n_radices_y,
-                                   void *stream);
+                                   int direction, void *stream);
 
 /* Synchronise `stream` and report any error a kernel of this plan flagged
  * (e.g. TCFFT_TIMEOUT from a bounded wait). Clears the flag. */

@@ -1,0 +1,115 @@
+// Drop-in check: drives the library only through the reference's own headers
+// and call sequences (main.cpp:164-200, 267-316; main_2d.cpp:76, 186-200),
+// compiled against include/compat/*.h and linked with libtcfft_gb300.so.
+// Writes raw FP64 / FP32 results for tests/test_compat_gpu.py to check against
+// the FP64 oracle.
+//   usage: compat_driver OUT_DIR
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fftconvolve2d.cuh"
+#include "tcfft_half.h"
+#include "tcfft_half_2d.h"
+#include "tensorcore_fft_conv2d.h"
+
+static unsigned long long g_state = 42;
+static double next_val() {  // seeded values in {0, 0.1, ..., 0.9}, like generate_data (main.cpp:32)
+  g_state = g_state * 6364136223846793005ull + 1442695040888963407ull;
+  return 0.1 * static_cast<double>((g_state >> 33) % 10);
+}
+
+static void dump(const std::string& path, const void* data, size_t bytes) {
+  FILE* f = fopen(path.c_str(), "wb");
+  if (!f) {
+    perror(path.c_str());
+    exit(2);
+  }
+  fwrite(data, 1, bytes, f);
+  fclose(f);
+}
+
+int main(int argc, char** argv) {
+  const std::string out = argc > 1 ? argv[1] : ".";
+  // ---- 1D: setup / doit / finalize (main.cpp:164-180) ----
+  {
+    const int n = 256, batch = 64;
+    std::vector<double> data(2 * n * batch), result(2 * n * batch);
+    for (auto& v : data) v = next_val();
+    setup(data.data(), n, batch);
+    doit(1);
+    finalize(result.data(), batch);
+    dump(out + "/in_1d.bin", data.data(), data.size() * 8);
+    dump(out + "/out_1d.bin", result.data(), result.size() * 8);
+    printf("1d status %d\n", tcfftGetLastError());
+  }
+  // ---- 1D through tcfftCreate / tcfftExec on an unconfigured size (4096) ----
+  {
+    const int n = 4096, batch = 8;
+    std::vector<double> data(2 * n * batch), result(2 * n * batch);
+    for (auto& v : data) v = next_val();
+    setup(data.data(), n, batch);
+    doit(2);  // two forward transforms in a row
+    finalize(result.data(), batch);
+    dump(out + "/in_1d_4096.bin", data.data(), data.size() * 8);
+    dump(out + "/out_1d_4096.bin", result.data(), result.size() * 8);
+  }
+  // ---- 2D: setup_2d / doit_2d / finalize_2d (main.cpp:182-198) ----
+  {
+    const int nx = 256, ny = 512, batch = 2;
+    std::vector<double> data(2 * nx * ny * batch), result(2 * nx * ny * batch);
+    for (auto& v : data) v = next_val();
+    setup_2d(data.data(), nx, ny, batch);
+    doit_2d(1);
+    finalize_2d(result.data(), batch);
+    dump(out + "/in_2d.bin", data.data(), data.size() * 8);
+    dump(out + "/out_2d.bin", result.data(), result.size() * 8);
+  }
+  // ---- conv forward (main.cpp:267-305), backward, fft_2d_c2c ----
+  {
+    const int s = 256, f = 13, C = 1, F = 16, o = s - f + 1;
+    std::vector<double> signal(s * s * C), filter(f * f * F * C), output(o * o * F);
+    for (auto& v : signal) v = next_val();
+    for (auto& v : filter) v = next_val();
+    fft_conv2d_half conv(signal.data(), filter.data(), C, F, s, s, f, f, __AMPERE__);
+    conv.conv2d_forward(output.data());
+    dump(out + "/conv_signal.bin", signal.data(), signal.size() * 8);
+    dump(out + "/conv_filter.bin", filter.data(), filter.size() * 8);
+    dump(out + "/conv_out.bin", output.data(), output.size() * 8);
+    printf("conv status %d padded %d\n", conv.last_status, conv.padded_x);
+    std::vector<double> delta(o * o * F);
+    for (auto& v : delta) v = next_val() - 0.45;
+    conv.conv2d_backward(delta.data());
+    dump(out + "/conv_delta.bin", delta.data(), delta.size() * 8);
+    dump(out + "/conv_dw.bin", conv.delta_for_filter, sizeof(double) * f * f * F * C);
+    dump(out + "/conv_dx.bin", conv.delta_for_signal, sizeof(double) * s * s * C);
+    free(conv.delta_for_filter);
+    free(conv.delta_for_signal);
+    std::vector<double> cin(2 * 256 * 256 * 2), cout_(2 * 256 * 256 * 2);
+    for (auto& v : cin) v = next_val();
+    conv.fft_2d_c2c(cin.data(), cout_.data(), 256, 256, 2, __AMPERE__);
+    dump(out + "/c2c_in.bin", cin.data(), cin.size() * 8);
+    dump(out + "/c2c_out.bin", cout_.data(), cout_.size() * 8);
+  }
+  // ---- cuFFT-family full convolution (main.cpp:307-314) ----
+  {
+    const int kernelCount = 16, f = 13, o = 244;
+    std::vector<float> sig(o * o), ker(f * f * kernelCount), res((o + f - 1) * (o + f - 1) * kernelCount);
+    for (auto& v : sig) v = static_cast<float>(next_val());
+    for (auto& v : ker) v = static_cast<float>(next_val());
+    convolve_direct_fft(sig.data(), ker.data(), kernelCount, o, o, f, f, res.data());
+    dump(out + "/full_sig.bin", sig.data(), sig.size() * 4);
+    dump(out + "/full_ker.bin", ker.data(), ker.size() * 4);
+    dump(out + "/full_out.bin", res.data(), res.size() * 4);
+    std::vector<float> res2(res.size());
+    convolve_turbo_fft_v2(sig.data(), ker.data(), kernelCount, o, o, f, f, res2.data());
+    dump(out + "/full_out_v2.bin", res2.data(), res2.size() * 4);
+    std::vector<cufftComplex> spec((kernelCount / 2) * 256 * 256);
+    direct_fft(ker.data(), kernelCount, o, o, f, f, spec.data());
+    dump(out + "/direct_fft.bin", spec.data(), spec.size() * sizeof(cufftComplex));
+  }
+  printf("compat driver done\n");
+  return 0;
+}

@@ -1,0 +1,73 @@
+"""Generate fixtures of the reference's own GPU output (run on a GPU host).
+
+Runs the reference's tcFFT kernels -- cubins compiled from its source by
+oracle/ref_build.sh (oracle/_ref/ref_tcfft{1d,2d}.cubin) -- through
+oracle/ref_launch.py on seeded uniform[-1,1] FP16 inputs, for both kernel
+wirings (the V100 kernels tcfftCreate assigns and the _A100 kernels), and
+writes one .npz per case: natural-order input, the permuted input the
+reference consumes, and the reference's output.
+
+Usage: python tests/golden/make_ref_gpu_fixtures.py OUT_DIR
+The committed copies live in tests/golden/ref_tcfft_*.npz.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, "oracle"))
+
+import ref_launch  # noqa: E402
+
+CASES_1D = [(256, 256), (512, 256), (1024, 256), (131072, 2)]
+CASES_2D = [(256, 256, 2), (512, 512, 2)]
+
+
+def main():
+    out_dir = sys.argv[1] if len(sys.argv) > 1 else HERE
+    os.makedirs(out_dir, exist_ok=True)
+    g = np.load(os.path.join(HERE, "reference_perm.npz"))
+    for n, batch in CASES_1D:
+        plan = g["plan_%d" % n]
+        nr = int(plan[0])
+        radices = [int(r) for r in plan[1:1 + nr]]
+        n_mergings = int(plan[10])
+        mergings = [int(m) for m in plan[11:14]]
+        if ("gen_rev_%d" % n) in g.files:
+            rev = g["gen_rev_%d" % n]
+        else:
+            import pyoracle
+            rev = pyoracle.gen_rev(n, radices)
+        rng = np.random.default_rng(1000 + n)
+        x = rng.uniform(-1, 1, (batch, n, 2)).astype(np.float16)
+        xp = np.ascontiguousarray(x[:, rev, :])
+        res = {"input": x, "input_permuted": xp, "radices": np.array(radices, np.int32),
+               "mergings": np.array(mergings[:n_mergings], np.int32)}
+        for variant in ("A100", "V100"):
+            res["out_" + variant] = ref_launch.run_1d(xp, n, batch, mergings, n_mergings, variant)
+        np.savez_compressed(os.path.join(out_dir, "ref_tcfft_1d_%d.npz" % n), **res)
+        print("1d", n, "done")
+    for nx, ny, batch in CASES_2D:
+        p2 = g["plan2d_%d" % nx]
+        nrx = int(p2[0])
+        rx = [int(r) for r in p2[1:1 + nrx]]
+        nry = int(p2[4])
+        ry = [int(r) for r in p2[5:5 + nry]]
+        mergings = [int(p2[8]), int(p2[9])]
+        rev_x = g["gen_rev_2d_%d" % nx]
+        rev_y = g["gen_rev_2d_%d" % ny]
+        rng = np.random.default_rng(2000 + nx)
+        x = rng.uniform(-1, 1, (batch, nx, ny, 2)).astype(np.float16)
+        xp = np.ascontiguousarray(x[:, rev_x][:, :, rev_y])
+        res = {"input": x, "input_permuted": xp, "radices_x": np.array(rx, np.int32),
+               "radices_y": np.array(ry, np.int32), "mergings": np.array(mergings, np.int32)}
+        for variant in ("A100", "V100"):
+            res["out_" + variant] = ref_launch.run_2d(xp, nx, ny, batch, mergings, variant)
+        np.savez_compressed(os.path.join(out_dir, "ref_tcfft_2d_%d.npz" % nx), **res)
+        print("2d", nx, "done")
+
+
+if __name__ == "__main__":
+    main()

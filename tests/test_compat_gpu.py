@@ -1,0 +1,103 @@
+"""Drop-in test: the reference's own call sequences, compiled against the
+compat headers (include/compat/*.h) and linked with libtcfft_gb300.so
+(tests/compat_driver.cpp), checked against the FP64 oracle.
+
+Tolerances (relative L2): FP16 paths 3e-3 (REL_FP16), split-precision
+(FP32) paths 1e-5 (REL_SPLIT); two FP16 transforms in a row 5e-3.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REL_FP16 = 3e-3
+REL_SPLIT = 1e-5
+
+
+@pytest.fixture(scope="module")
+def driver_out(tc, tmp_path_factory):
+    out = tmp_path_factory.mktemp("compat")
+    exe = str(out / "compat_driver")
+    libdir = os.path.join(REPO, "fft_demo_gb300")
+    cmd = ["nvcc", "-std=c++17", "-O2", "-I" + os.path.join(REPO, "include", "compat"),
+           os.path.join(REPO, "tests", "compat_driver.cpp"), "-o", exe, "-L" + libdir, "-ltcfft_gb300",
+           "-Xlinker", "-rpath=" + libdir, "-lcufft"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe, str(out)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "compat driver done" in r.stdout
+    return out
+
+
+def load(d, name, dtype=np.float64):
+    return np.fromfile(os.path.join(d, name), dtype=dtype)
+
+
+def cplx(a):
+    return a[0::2] + 1j * a[1::2]
+
+
+def h(a):
+    return a.astype(np.float16).astype(np.float64)
+
+
+def test_setup_doit_finalize_1d(driver_out, orc):
+    x = cplx(h(load(driver_out, "in_1d.bin"))).reshape(64, 256)
+    y = cplx(load(driver_out, "out_1d.bin")).reshape(64, 256)
+    assert orc.rel_l2(y, orc.fft1d(x)) < REL_FP16
+
+
+def test_unconfigured_size_two_transforms(driver_out, orc):
+    x = cplx(h(load(driver_out, "in_1d_4096.bin"))).reshape(8, 4096)
+    y = cplx(load(driver_out, "out_1d_4096.bin")).reshape(8, 4096)
+    assert orc.rel_l2(y, orc.fft1d(orc.fft1d(x))) < 5e-3
+
+
+def test_setup_doit_finalize_2d(driver_out, orc):
+    x = cplx(h(load(driver_out, "in_2d.bin"))).reshape(2, 256, 512)
+    y = cplx(load(driver_out, "out_2d.bin")).reshape(2, 256, 512)
+    assert orc.rel_l2(y, orc.fft2d(x)) < REL_FP16
+
+
+def test_conv_class_forward(driver_out, orc):
+    sig = h(load(driver_out, "conv_signal.bin")).reshape(1, 256, 256)
+    filt = load(driver_out, "conv_filter.bin").reshape(16, 1, 13, 13)
+    out = load(driver_out, "conv_out.bin").reshape(16, 244, 244)
+    assert orc.rel_l2(out, orc.corr2d_valid(sig, filt)) < REL_FP16
+
+
+def test_conv_class_backward(driver_out, orc):
+    sig = load(driver_out, "conv_signal.bin").reshape(1, 256, 256)
+    filt = load(driver_out, "conv_filter.bin").reshape(16, 1, 13, 13)
+    delta = load(driver_out, "conv_delta.bin").reshape(16, 244, 244)
+    dw = load(driver_out, "conv_dw.bin").reshape(16, 1, 13, 13)
+    dx = load(driver_out, "conv_dx.bin").reshape(1, 256, 256)
+    ref_dw = orc.corr2d_valid(sig, delta[:, None])  # [F][fy][fx]
+    assert orc.rel_l2(dw[:, 0], ref_dw) < 1e-4
+    ref_dx = sum(orc.conv2d_full(delta[f], filt[f]) for f in range(16))  # [1][256][256]
+    assert orc.rel_l2(dx, ref_dx) < 1e-4
+
+
+def test_conv_class_fft_2d_c2c(driver_out, orc):
+    x = cplx(h(load(driver_out, "c2c_in.bin"))).reshape(2, 256, 256)
+    y = cplx(load(driver_out, "c2c_out.bin")).reshape(2, 256, 256)
+    assert orc.rel_l2(y, orc.fft2d(x)) < REL_FP16
+
+
+def test_fftconvolve2d_family(driver_out, orc):
+    sig = load(driver_out, "full_sig.bin", np.float32).astype(np.float64).reshape(244, 244)
+    ker = load(driver_out, "full_ker.bin", np.float32).astype(np.float64).reshape(16, 13, 13)
+    out = load(driver_out, "full_out.bin", np.float32).reshape(16, 256, 256)
+    out2 = load(driver_out, "full_out_v2.bin", np.float32).reshape(16, 256, 256)
+    ref = orc.conv2d_full(sig, ker)
+    assert orc.rel_l2(out, ref) < REL_SPLIT
+    assert np.array_equal(out, out2)
+    spec = load(driver_out, "direct_fft.bin", np.float32)
+    spec = (spec[0::2] + 1j * spec[1::2]).reshape(8, 256, 256)
+    packed = np.zeros((8, 256, 256), complex)
+    packed[:, :13, :13] = ker[0::2] + 1j * ker[1::2]
+    assert orc.rel_l2(spec, orc.fft2d(packed, sign=+1)) < REL_SPLIT

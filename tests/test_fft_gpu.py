@@ -147,3 +147,32 @@ def test_error_paths(tc):
     assert st == tc.INVALID_VALUE
     assert L.tcfft_exec(plan._h, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(x.data_ptr()),
                         5, 1.0, None) == tc.INVALID_VALUE
+
+
+@pytest.mark.parametrize("n,batch", [(1 << 15, 600), (1 << 20, 9), (1 << 22, 3)])
+def test_fused_four_step_matches_two_pass(tc, orc, n, batch):
+    """One-launch chunked four-step == two pass launches (several chunks,
+    ragged last chunk), in place and out of place, and == the FP64 oracle."""
+    import torch
+    g = torch.Generator(device="cuda")
+    g.manual_seed(n)
+    x = (torch.rand((batch, n, 2), device="cuda", generator=g) * 2 - 1).half()
+    plan = tc.plan_1d(n, batch)
+    y_fused = torch.empty_like(x)
+    plan.exec(x, y_fused)
+    plan.check()
+    plan.set_fused(False)
+    y_two = torch.empty_like(x)
+    plan.exec(x, y_two)
+    plan.check()
+    assert torch.equal(y_fused, y_two)
+    plan.set_fused(True)
+    z = x.clone()
+    plan.exec(z)  # in place
+    plan.check()
+    assert torch.equal(z, y_fused)
+    xs = x[:2].double().cpu().numpy()
+    xs = xs[..., 0] + 1j * xs[..., 1]
+    ys = y_fused[:2].double().cpu().numpy()
+    ys = ys[..., 0] + 1j * ys[..., 1]
+    assert orc.rel_l2(ys, orc.fft1d(xs)) < REL_L2_FP16
