@@ -57,6 +57,7 @@ def _declare(L):
         "tcfft_pass_info": (i, [i, i, i, i, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)]),
         "tcfft_exec": (i, [vp, vp, vp, i, f, vp]),
         "tcfft_exec_digitrev": (i, [vp, vp, vp, ctypes.POINTER(i), i, vp]),
+        "tcfft_exec_digitrev_2d": (i, [vp, vp, vp, ctypes.POINTER(i), i, ctypes.POINTER(i), i, i, vp]),
         "tcfft_check": (i, [vp, vp]),
         "tcfft_destroy": (i, [vp]),
         "tcfft_get_last_error": (i, []),
@@ -154,6 +155,19 @@ class Plan:
         arr = (ctypes.c_int * max(1, len(radices)))(*radices)
         _check(lib().tcfft_exec_digitrev(self._h, _ptr(x), _ptr(out), arr, len(radices),
                                          _stream_ptr(stream)), "exec_digitrev")
+        return out
+
+    def exec_digitrev_2d(self, x, radices_x, radices_y, out=None, direction=FORWARD, stream=None):
+        """2D FFT of input whose axes are in the reference's digit-reversed order."""
+        self._validate(x)
+        if out is None:
+            out = x
+        self._validate(out)
+        ax = (ctypes.c_int * max(1, len(radices_x)))(*radices_x)
+        ay = (ctypes.c_int * max(1, len(radices_y)))(*radices_y)
+        _check(lib().tcfft_exec_digitrev_2d(self._h, _ptr(x), _ptr(out), ax, len(radices_x), ay,
+                                            len(radices_y), int(direction), _stream_ptr(stream)),
+               "exec_digitrev_2d")
         return out
 
     def check(self, stream=None):

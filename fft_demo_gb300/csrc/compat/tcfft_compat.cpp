@@ -40,7 +40,8 @@ const Shape1d kShapes1d[] = {
 // permutation the reference's gen_rev builds (tcfft_half.cu:1351), computed
 // in closed form (peel the index's digits from the last radix to the first;
 // the k-th digit peeled becomes the k-th most significant digit of the
-// position).
+// position; what is left unpeeled keeps its place, so an empty list gives the
+// identity, as gen_rev does for sizes tcfftCreate leaves unconfigured).
 std::vector<int> digit_reversal(int n, const int* radices, int n_radices) {
   std::vector<int> rev(static_cast<size_t>(n));
   for (int idx = 0; idx < n; ++idx) {
@@ -52,6 +53,7 @@ std::vector<int> digit_reversal(int n, const int* radices, int n_radices) {
       span /= r;
       pos += d * span;
     }
+    pos += rest;
     rev[static_cast<size_t>(pos)] = idx;
   }
   return rev;

@@ -118,11 +118,64 @@ __device__ __forceinline__ void split_stage_epilogue(const SplitPlanes& P, const
 }
 
 // ---------------------------------------------------------------------------
-// Split-precision pass kernel. Same geometry rules as fft_pass_f16, with
-// G * L / 16 in {128, 256, 512} (4 planes + 64 TMEM columns per 128 rows).
+// Split-precision tile machinery. Shared-memory layout:
+//   [0, 4096)      B matrix images (hi, lo)
+//   [4096, 4160)   mbarrier, TMEM slot, tile maximum
+//   [5120, ...)    four planes (re hi, im hi, re lo, im lo), 1024-aligned
 // ---------------------------------------------------------------------------
+constexpr uint32_t kSplitPlaneOffset = 5120;
+
+struct SplitState {
+  uint8_t* smem;
+  uint8_t* bhi;
+  uint8_t* blo;
+  uint64_t* mbar;
+  uint32_t* tslot;
+  int* smax;
+  uint32_t tbase;
+  uint32_t phase;
+};
+
+template <uint32_t TMEM_COLS>
+__device__ __forceinline__ void split_setup(SplitState& st, const uint32_t* __restrict__ bmat_g) {
+  st.smem = aligned_dynamic_smem();
+  st.bhi = st.smem;
+  st.blo = st.smem + 2048;
+  st.mbar = reinterpret_cast<uint64_t*>(st.smem + 4096);
+  st.tslot = reinterpret_cast<uint32_t*>(st.smem + 4112);
+  st.smax = reinterpret_cast<int*>(st.smem + 4128);
+  const int tid = threadIdx.x;
+  for (int i = tid; i < 1024; i += kPassThreads) reinterpret_cast<uint32_t*>(st.bhi)[i] = __ldg(bmat_g + i);
+  if (tid == 0) mbar_init(st.mbar, 1);
+  if ((tid >> 5) == 0) {
+    tmem_alloc(st.tslot, TMEM_COLS);
+    tmem_relinquish();
+  }
+  fence_proxy_async_smem();
+  tc_fence_before_sync();
+  __syncthreads();
+  tc_fence_after_sync();
+  st.tbase = *st.tslot;
+  st.phase = 0;
+}
+
+template <uint32_t TMEM_COLS>
+__device__ __forceinline__ void split_teardown(SplitState& st) {
+  tc_fence_before_sync();
+  __syncthreads();
+  if ((threadIdx.x >> 5) == 0) tmem_dealloc(st.tbase, TMEM_COLS);
+}
+
+template <int L, int G>
+__host__ __device__ constexpr uint32_t split_tmem_cols() {
+  return static_cast<uint32_t>(G * L / 16 / 128 * 64);
+}
+
+// One split-precision tile: G lines of length L starting at line0. Same
+// geometry rules as pass_tile, with G * L / 16 in {128, 256, 512} (4 planes
+// + 64 TMEM columns per 128 rows). False if a bounded wait gave up.
 template <int L, int G, bool LINE_MINOR, int SIGN, class IO>
-__global__ void __launch_bounds__(kPassThreads, 2) fft_pass_split(const IO io, const PassCore core) {
+__device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const PassCore& core, long long line0) {
   using Sh = LineShape<L>;
   using Tl = Tile<L, G, LINE_MINOR>;
   constexpr int T = Sh::T;
@@ -132,46 +185,17 @@ __global__ void __launch_bounds__(kPassThreads, 2) fft_pass_split(const IO io, c
   constexpr int NG = Mt / 128;
   constexpr uint32_t PLANE = Tl::PLANE;
   constexpr uint32_t KSTRIDE = Tl::KSTRIDE;
-  constexpr uint32_t TMEM_COLS = NG * 64;
   static_assert(Mt % 128 == 0 && Mt <= 512, "tile size");
-  static_assert(TMEM_COLS >= 32 && (TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM columns");
   static_assert(G % 4 == 0 || IO::IN_VEC_L, "line-vectorised loads need G % 4 == 0");
   constexpr uint32_t IDESC = make_idesc_f16_f32(128, 32, true, false);
-
-  extern __shared__ uint8_t smem_raw[];
-  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
-                                             ~static_cast<uintptr_t>(1023));
-  SplitPlanes P{smem, smem + PLANE, smem + 2 * PLANE, smem + 3 * PLANE};
-  uint8_t* bhi = smem + 4 * PLANE;  // 2 KB
-  uint8_t* blo = bhi + 2048;        // 2 KB
-  uint64_t* mbar = reinterpret_cast<uint64_t*>(blo + 2048);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(blo + 2048 + 16);
-  int* smax = reinterpret_cast<int*>(blo + 2048 + 32);
-
+  constexpr int U = T >= 8 ? 1 : 8 / T;
+  uint8_t* pl = st.smem + kSplitPlaneOffset;
+  SplitPlanes P{pl, pl + PLANE, pl + 2 * PLANE, pl + 3 * PLANE};
   const int tid = threadIdx.x;
   const int warp = tid >> 5;
   const int lane = tid & 31;
-
-  for (int i = tid; i < 1024; i += kPassThreads) reinterpret_cast<uint32_t*>(bhi)[i] = __ldg(core.bmat + i);
-  if (tid == 0) mbar_init(mbar, 1);
-  if (warp == 0) {
-    tmem_alloc(tslot, TMEM_COLS);
-    tmem_relinquish();
-  }
-  fence_proxy_async_smem();
-  tc_fence_before_sync();
-  __syncthreads();
-  tc_fence_after_sync();
-  const uint32_t tbase = *tslot;
-  uint32_t phase = 0;
   bool timed_out = false;
-
-  const long long ntiles = (io.total_lines + G - 1) / G;
-  constexpr int U = T >= 8 ? 1 : 8 / T;
-
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const long long line0 = tile * G;
-    if (tid == 0) *smax = 0;
+    if (tid == 0) *st.smax = 0;
     __syncthreads();
 
     // ---- pass A: largest magnitude in the tile (data stays in L1/L2) ----
@@ -214,9 +238,9 @@ __global__ void __launch_bounds__(kPassThreads, 2) fft_pass_split(const IO io, c
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-    if (lane == 0) atomicMax(smax, __float_as_int(lmax));
+    if (lane == 0) atomicMax(st.smax, __float_as_int(lmax));
     __syncthreads();
-    const float tmax = __int_as_float(*smax) * static_cast<float>(T);
+    const float tmax = __int_as_float(*st.smax) * static_cast<float>(T);
     // sigma: largest value after the radix-T stage maps to <= 2^14
     int sigma = 0;
     if (tmax > 0.f && isfinite(tmax)) {
@@ -244,7 +268,7 @@ __global__ void __launch_bounds__(kPassThreads, 2) fft_pass_split(const IO io, c
 #pragma unroll
         for (int u = 0; u < U; ++u) {
           const int it = base + u * kPassThreads;
-          if (it >= ITEMS) break;
+          if (ITEMS % (kPassThreads * U) != 0 && it >= ITEMS) continue;
           const int g = it / QPL;
           const int j0 = (it % QPL) * 4;
           float2 v[T][4];
@@ -298,7 +322,7 @@ __global__ void __launch_bounds__(kPassThreads, 2) fft_pass_split(const IO io, c
 #pragma unroll
         for (int u = 0; u < U; ++u) {
           const int it = base + u * kPassThreads;
-          if (it >= ITEMS) break;
+          if (ITEMS % (kPassThreads * U) != 0 && it >= ITEMS) continue;
           const int j = it / GQ;
           const int g0 = (it % GQ) * 4;
           float2 v[T][4];
@@ -350,10 +374,10 @@ __global__ void __launch_bounds__(kPassThreads, 2) fft_pass_split(const IO io, c
       if (tid == 0) {
         tc_fence_after_sync();
         const uint32_t arh = smem_u32(P.rh), aih = smem_u32(P.ih), arl = smem_u32(P.rl), ail = smem_u32(P.il);
-        const uint64_t bh0 = make_sdesc(smem_u32(bhi), 128u, 512u, kLayoutNone);
-        const uint64_t bh1 = make_sdesc(smem_u32(bhi) + 256u, 128u, 512u, kLayoutNone);
-        const uint64_t bl0 = make_sdesc(smem_u32(blo), 128u, 512u, kLayoutNone);
-        const uint64_t bl1 = make_sdesc(smem_u32(blo) + 256u, 128u, 512u, kLayoutNone);
+        const uint64_t bh0 = make_sdesc(smem_u32(st.bhi), 128u, 512u, kLayoutNone);
+        const uint64_t bh1 = make_sdesc(smem_u32(st.bhi) + 256u, 128u, 512u, kLayoutNone);
+        const uint64_t bl0 = make_sdesc(smem_u32(st.blo), 128u, 512u, kLayoutNone);
+        const uint64_t bl1 = make_sdesc(smem_u32(st.blo) + 256u, 128u, 512u, kLayoutNone);
 #pragma unroll
         for (int grp = 0; grp < NG; ++grp) {
           const uint32_t o = grp * 2048u;
@@ -361,7 +385,7 @@ __global__ void __launch_bounds__(kPassThreads, 2) fft_pass_split(const IO io, c
           const uint64_t a_ih = make_sdesc(aih + o, 1024u, KSTRIDE, kLayoutSw128);
           const uint64_t a_rl = make_sdesc(arl + o, 1024u, KSTRIDE, kLayoutSw128);
           const uint64_t a_il = make_sdesc(ail + o, 1024u, KSTRIDE, kLayoutSw128);
-          const uint32_t dmain = tbase + grp * 64u, dcorr = dmain + 32u;
+          const uint32_t dmain = st.tbase + grp * 64u, dcorr = dmain + 32u;
           umma_f16(dmain, a_rh, bh0, IDESC, 0u);
           umma_f16(dmain, a_ih, bh1, IDESC, 1u);
           umma_f16(dcorr, a_rh, bl0, IDESC, 0u);
@@ -369,17 +393,17 @@ __global__ void __launch_bounds__(kPassThreads, 2) fft_pass_split(const IO io, c
           umma_f16(dcorr, a_rl, bh0, IDESC, 1u);
           umma_f16(dcorr, a_il, bh1, IDESC, 1u);
         }
-        umma_commit(mbar);
+        umma_commit(st.mbar);
       }
-      bool to = !mbar_wait_bounded(mbar, phase & 1u);
+      bool to = !mbar_wait_bounded(st.mbar, st.phase & 1u);
       if (to && lane == 0) atomicOr(core.err, kErrMmaTimeout);
-      phase++;
+      st.phase++;
       if (__syncthreads_or(to)) {
         timed_out = true;
         return;
       }
       tc_fence_after_sync();
-      split_stage_epilogue<L, G, LINE_MINOR, s, IO>(P, core.tw, tbase, warp, lane, io, line0, out_scale);
+      split_stage_epilogue<L, G, LINE_MINOR, s, IO>(P, core.tw, st.tbase, warp, lane, io, line0, out_scale);
       fence_proxy_async_smem();
       tc_fence_before_sync();
       __syncthreads();
@@ -387,17 +411,27 @@ __global__ void __launch_bounds__(kPassThreads, 2) fft_pass_split(const IO io, c
     [&]<int... Is>(std::integer_sequence<int, Is...>) {
       (run_stage(std::integral_constant<int, Is>{}), ...);
     }(std::make_integer_sequence<int, S>{});
-    if (timed_out) break;
-  }
+    return !timed_out;
+}
 
-  tc_fence_before_sync();
-  __syncthreads();
-  if (warp == 0) tmem_dealloc(tbase, TMEM_COLS);
+// ---------------------------------------------------------------------------
+// Split-precision pass kernel: persistent CTAs over the tiles of one pass.
+// ---------------------------------------------------------------------------
+template <int L, int G, bool LINE_MINOR, int SIGN, class IO>
+__global__ void __launch_bounds__(kPassThreads, 2) fft_pass_split(const IO io, const PassCore core) {
+  constexpr uint32_t TMEM_COLS = split_tmem_cols<L, G>();
+  static_assert(TMEM_COLS >= 32 && (TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM columns");
+  SplitState st;
+  split_setup<TMEM_COLS>(st, core.bmat);
+  const long long ntiles = (io.total_lines + G - 1) / G;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+    if (!split_tile<L, G, LINE_MINOR, SIGN, IO>(st, io, core, tile * G)) break;
+  split_teardown<TMEM_COLS>(st);
 }
 
 template <int L, int G>
 constexpr int split_smem_bytes() {
-  return 4 * (G * L / 16) * 32 + 4096 + 64 + 1024;
+  return static_cast<int>(kSplitPlaneOffset) + 4 * (G * L / 16) * 32 + 1024;
 }
 
 // Interleaved complex float in and out, arbitrary strides (in elements).

@@ -536,7 +536,7 @@ __device__ __forceinline__ bool pass_tile(PassState& st, const IO& io, const Pas
 #pragma unroll
         for (int u = 0; u < U; ++u) {
           const int it = base + u * kPassThreads;
-          if (it >= ITEMS) break;
+          if (ITEMS % (kPassThreads * U) != 0 && it >= ITEMS) continue;
           const int g = it / QPL;
           const int j0 = (it % QPL) * 4;
           float2 v[T][4];
@@ -588,7 +588,7 @@ __device__ __forceinline__ bool pass_tile(PassState& st, const IO& io, const Pas
 #pragma unroll
         for (int u = 0; u < U; ++u) {
           const int it = base + u * kPassThreads;
-          if (it >= ITEMS) break;
+          if (ITEMS % (kPassThreads * U) != 0 && it >= ITEMS) continue;
           const int j = it / GQ;
           const int g0 = (it % GQ) * 4;
           float2 v[T][4];

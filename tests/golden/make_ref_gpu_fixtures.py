@@ -4,11 +4,15 @@ Runs the reference's tcFFT kernels -- cubins compiled from its source by
 oracle/ref_build.sh (oracle/_ref/ref_tcfft{1d,2d}.cubin) -- through
 oracle/ref_launch.py on seeded uniform[-1,1] FP16 inputs, for both kernel
 wirings (the V100 kernels tcfftCreate assigns and the _A100 kernels), and
-writes one .npz per case: natural-order input, the permuted input the
-reference consumes, and the reference's output.
+writes one .npz per case: the permuted input the reference consumes (the
+natural-order input is its inverse permutation) and the reference's output.
+The committed copies are trimmed to a few lines per case (KEEP_LINES); the
+large cases keep only the A100 wiring.
 
 Usage: python tests/golden/make_ref_gpu_fixtures.py OUT_DIR
-The committed copies live in tests/golden/ref_tcfft_*.npz.
+       python tests/golden/make_ref_gpu_fixtures.py --trim FULL_DIR OUT_DIR
+The second form trims full-size outputs of the first form written earlier
+with TRIM=0. The committed copies live in tests/golden/ref_tcfft_*.npz.
 """
 import os
 import sys
@@ -23,9 +27,29 @@ import ref_launch  # noqa: E402
 
 CASES_1D = [(256, 256), (512, 256), (1024, 256), (131072, 2)]
 CASES_2D = [(256, 256, 2), (512, 512, 2)]
+# lines (transforms) kept per case, and whether the V100 wiring's output is kept
+KEEP_LINES = {"1d_256": (16, True), "1d_512": (16, True), "1d_1024": (16, True), "1d_131072": (1, False),
+              "2d_256": (1, True), "2d_512": (1, False)}
+
+
+def save(res, out_dir, name):
+    if os.environ.get("TRIM", "1") != "0":
+        lines, keep_v100 = KEEP_LINES[name]
+        res = {k: (v[:lines] if v.ndim >= 3 else v) for k, v in res.items()
+               if k != "input" and (keep_v100 or k != "out_V100")}
+    np.savez_compressed(os.path.join(out_dir, "ref_tcfft_%s.npz" % name), **res)
+
+
+def trim(src_dir, out_dir):
+    for name in KEEP_LINES:
+        d = np.load(os.path.join(src_dir, "ref_tcfft_%s.npz" % name))
+        save({k: d[k] for k in d.files}, out_dir, name)
 
 
 def main():
+    if len(sys.argv) == 4 and sys.argv[1] == "--trim":
+        trim(sys.argv[2], sys.argv[3])
+        return
     out_dir = sys.argv[1] if len(sys.argv) > 1 else HERE
     os.makedirs(out_dir, exist_ok=True)
     g = np.load(os.path.join(HERE, "reference_perm.npz"))
@@ -47,7 +71,7 @@ def main():
                "mergings": np.array(mergings[:n_mergings], np.int32)}
         for variant in ("A100", "V100"):
             res["out_" + variant] = ref_launch.run_1d(xp, n, batch, mergings, n_mergings, variant)
-        np.savez_compressed(os.path.join(out_dir, "ref_tcfft_1d_%d.npz" % n), **res)
+        save(res, out_dir, "1d_%d" % n)
         print("1d", n, "done")
     for nx, ny, batch in CASES_2D:
         p2 = g["plan2d_%d" % nx]
@@ -65,7 +89,7 @@ def main():
                "radices_y": np.array(ry, np.int32), "mergings": np.array(mergings, np.int32)}
         for variant in ("A100", "V100"):
             res["out_" + variant] = ref_launch.run_2d(xp, nx, ny, batch, mergings, variant)
-        np.savez_compressed(os.path.join(out_dir, "ref_tcfft_2d_%d.npz" % nx), **res)
+        save(res, out_dir, "2d_%d" % nx)
         print("2d", nx, "done")
 
 

@@ -1,0 +1,46 @@
+"""CPU checks of the reference-output fixtures against the FP64 oracle.
+
+Pins what the reference's own kernels deliver on this architecture, the bar
+the GPU parity tests (test_reference_kernels_gpu.py) hold ours to:
+  * the `_A100` wiring is a correct FFT to FP16 accuracy (relative L2 below
+    REF_REL_MAX for every case);
+  * the V100 wiring that tcfftCreate assigns by default (tcfft_half.cu:1262,
+    tcfft_half_2d.cu) does not compute the FFT here (relative L2 near 1.4):
+    its wmma fragment-layout assumptions do not hold on this GPU, so parity
+    is taken against the A100 wiring.
+"""
+import pytest
+
+import refdata
+
+REF_REL_MAX = 3e-3
+
+
+@pytest.mark.parametrize("n", refdata.CASES_1D)
+def test_reference_1d_a100_wiring_is_fft(orc, n):
+    x, _, _, outs = refdata.load_1d(n)
+    err = orc.rel_l2(outs["A100"], orc.fft1d(x))
+    assert err < REF_REL_MAX, err
+
+
+@pytest.mark.parametrize("n", refdata.CASES_2D)
+def test_reference_2d_a100_wiring_is_fft(orc, n):
+    x, _, _, _, outs = refdata.load_2d(n)
+    err = orc.rel_l2(outs["A100"], orc.fft2d(x))
+    assert err < REF_REL_MAX, err
+
+
+@pytest.mark.parametrize("n", [256, 512, 1024])
+def test_reference_v100_wiring_fails_here(orc, n):
+    x, _, _, outs = refdata.load_1d(n)
+    assert orc.rel_l2(outs["V100"], orc.fft1d(x)) > 0.5
+
+
+def test_fixture_permutation_matches_oracle_gen_rev(orc):
+    # the committed gen_rev tables (printed by the reference) agree with the
+    # oracle's restatement for every 1D case that has one
+    import numpy as np
+    g = refdata._perm()
+    for n in (256, 512, 1024):
+        _, _, radices, _ = refdata.load_1d(n)
+        assert np.array_equal(g["gen_rev_%d" % n], orc.gen_rev(n, radices))
