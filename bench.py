@@ -108,7 +108,9 @@ def dist_init():
     if world > 1:
         import torch.distributed as dist
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-        backend = "nccl"
+        # replicas: no data-path collective; the group only carries the
+        # barrier and the max over ranks (gloo for CPU tests of this plumbing)
+        backend = os.environ.get("TCFFT_DIST_BACKEND", "nccl")
         dist.init_process_group(backend)
     return world, rank, local
 
@@ -124,9 +126,15 @@ def max_over_ranks(world, value):
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world, ms):
+    """Weak scaling: every rank processes units_per_rank in at most ms."""
+    return units_per_rank * world / (ms * 1e-3)
 
 
 def cpu_fft_sample(seconds_target=12.0, threads=0):
@@ -289,7 +297,7 @@ def main():
         p.check()
     ms_total = max_over_ranks(world, ms_total)
     ms_step = ms_total / args.steps
-    value = step_flops * world / (ms_step * 1e-3) / 1e9
+    value = whole_job_rate(step_flops, world, ms_step) / 1e9
     gpu_launches = launches[0]
 
     # --- end to end through the public API with host buffers ---
@@ -320,7 +328,7 @@ def main():
     q1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = max_over_ranks(world, q0.elapsed_time(q1)) / e2e_steps
-    e2e_value = step_flops * world / (e2e_ms * 1e-3) / 1e9
+    e2e_value = whole_job_rate(step_flops, world, e2e_ms) / 1e9
 
     # --- roofline of the dominant transform ---
     dom = max(per_kernel, key=lambda k: k["ms"])
