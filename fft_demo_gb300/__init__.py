@@ -59,6 +59,7 @@ def _declare(L):
         "tcfft_exec_digitrev": (i, [vp, vp, vp, ctypes.POINTER(i), i, vp]),
         "tcfft_exec_digitrev_2d": (i, [vp, vp, vp, ctypes.POINTER(i), i, ctypes.POINTER(i), i, i, vp]),
         "tcfft_check": (i, [vp, vp]),
+        "tcfft_exec_static": (i, [vp, vp, ll, ll, i, f, vp, i]),
         "tcfft_destroy": (i, [vp]),
         "tcfft_get_last_error": (i, []),
         "tcfft_status_string": (ctypes.c_char_p, [i]),
@@ -188,6 +189,21 @@ class Plan:
             self.destroy()
         except Exception:
             pass
+
+
+def exec_static(x, n, batch, out=None, direction=FORWARD, scale=1.0, stream=None, wait=True):
+    """1D FP16 transform with no plan and no device allocation
+    (tcfft_exec_static): 2^15 <= n <= 2^21, scratch shared by every call on
+    the device, so calls that overlap on the GPU race."""
+    need = int(n) * int(batch) * 4
+    for t in (x,) if out is None else (x, out):
+        if not t.is_cuda or t.numel() * t.element_size() != need or not t.is_contiguous():
+            raise TcfftError(INVALID_VALUE, "tensor must be contiguous CUDA with %d bytes" % need)
+    if out is None:
+        out = x
+    _check(lib().tcfft_exec_static(_ptr(x), _ptr(out), int(n), int(batch), int(direction), float(scale),
+                                   _stream_ptr(stream), 1 if wait else 0), "exec_static")
+    return out
 
 
 def plan_1d(n, batch=1, precision=FP16):

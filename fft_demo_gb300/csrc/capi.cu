@@ -15,6 +15,7 @@
 #include <new>
 
 #include "../../include/tcfft_gb300.h"
+#include "capi_internal.cuh"
 #include "passes.cuh"
 #include "tables.cuh"
 
@@ -125,6 +126,25 @@ int ilog2ll(long long v) {
 bool is_pow2(long long v) { return v > 0 && (v & (v - 1)) == 0; }
 
 }  // namespace
+
+namespace tcfft {
+
+tcfftStatus registry_ready() { return ensure_init(); }
+
+const FusedKernel* fused_kernel(int logn, int sign_idx, int* grid_ctas) {
+  if (logn < kFusedMinLog || logn > kFusedMaxLog || sign_idx < 0 || sign_idx > 1) return nullptr;
+  const FusedKernel& fk = g_fused[logn][sign_idx];
+  if (!fk.fn) return nullptr;
+  if (grid_ctas) *grid_ctas = g_num_sms * g_fused_occ[logn][sign_idx];
+  return &fk;
+}
+
+tcfftStatus record_status(tcfftStatus s, int launches) {
+  g_last_launches = launches;
+  return ret(s);
+}
+
+}  // namespace tcfft
 
 struct tcfftPlanImpl {
   int dims = 1;

@@ -98,6 +98,23 @@ tcfftStatus tcfft_check(tcfftPlan plan, void *stream);
 
 tcfftStatus tcfft_destroy(tcfftPlan plan);
 
+/* No counterpart in the reference. 1D FP16 transform without a plan and
+ * without any device allocation, for callers that cannot allocate: the
+ * fused four-step kernel of tcfft_exec runs with its workspace ring,
+ * counters, error word and tables in one file-scope device array of 17 MiB
+ * (fixed at load time; the tables are written on the first call on each
+ * device). out = scale * FFT_direction(in), in == out allowed, 16-byte
+ * aligned device buffers of n * batch interleaved complex halves.
+ * Limits: n = 2^k with 2^15 <= n <= 2^21 (TCFFT_INVALID_SIZE below the
+ * range or for other n, TCFFT_CAPACITY above it) and
+ * ceil(batch / (2^21 / n)) <= 8159 (TCFFT_CAPACITY beyond that).
+ * Every call on a device shares the array, so calls that overlap on the GPU
+ * (other streams, unordered host threads) race; calls on one stream do not.
+ * wait != 0: synchronise `stream` and report a flagged kernel error
+ * (TCFFT_TIMEOUT); wait == 0: asynchronous, errors unreported. */
+tcfftStatus tcfft_exec_static(const void *in, void *out, long long n, long long batch, int direction,
+                              float scale, void *stream, int wait);
+
 /* ------------------------------------------------------------------------
  * 2D FFT convolution
  *   images  [batch][S][sy][sx] real (half for TCFFT_FP16, float for split)
