@@ -22,6 +22,8 @@ FP16, SPLIT_FP32 = 0, 1
 FORWARD, INVERSE = -1, 1
 # tcfftConvMode
 CONV_VALID_CORR, CONV_SAME, CONV_FULL = 0, 1, 2
+# tcfftBatchMode
+BATCH_PERSISTENT, BATCH_PER_SIZE = 0, 1
 
 _lib = None
 
@@ -60,6 +62,13 @@ def _declare(L):
         "tcfft_exec_digitrev_2d": (i, [vp, vp, vp, ctypes.POINTER(i), i, ctypes.POINTER(i), i, i, vp]),
         "tcfft_check": (i, [vp, vp]),
         "tcfft_exec_static": (i, [vp, vp, ll, ll, i, f, vp, i]),
+        "tcfft_batch_plan": (i, [ctypes.POINTER(vp), i, vp, vp, vp, vp, i, i]),
+        "tcfft_batch_set_mode": (i, [vp, i]),
+        "tcfft_batch_set_graph": (i, [vp, i]),
+        "tcfft_batch_exec": (i, [vp, vp, vp, vp]),
+        "tcfft_batch_info": (i, [vp, ctypes.POINTER(i), ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(i)]),
+        "tcfft_batch_check": (i, [vp, vp]),
+        "tcfft_batch_destroy": (i, [vp]),
         "tcfft_destroy": (i, [vp]),
         "tcfft_get_last_error": (i, []),
         "tcfft_status_string": (ctypes.c_char_p, [i]),
@@ -176,7 +185,7 @@ class Plan:
         _check(lib().tcfft_check(self._h, _stream_ptr(stream)), "check")
 
     def set_fused(self, enable):
-        """Large 1D FP16 sizes: one fused launch (default) or two pass launches."""
+        """Large 1D FP16 sizes: one fused launch, or two pass launches (default)."""
         _check(lib().tcfft_plan_set_fused(self._h, 1 if enable else 0), "set_fused")
 
     def destroy(self):
@@ -204,6 +213,69 @@ def exec_static(x, n, batch, out=None, direction=FORWARD, scale=1.0, stream=None
     _check(lib().tcfft_exec_static(_ptr(x), _ptr(out), int(n), int(batch), int(direction), float(scale),
                                    _stream_ptr(stream), 1 if wait else 0), "exec_static")
     return out
+
+
+class Batch:
+    """Many 1D transforms of uneven power-of-two sizes (64 <= n <= 2^20) in
+    one input and one output buffer (tcfft_batch_plan): one persistent
+    launch fed from a device work queue, or the plain per-size path.
+
+    sizes[i], in_off[i], out_off[i]: points and element offsets of
+    transform i (default: packed back to back in list order).
+    """
+
+    def __init__(self, sizes, in_off=None, out_off=None, scale=None, precision=FP16, direction=FORWARD):
+        import numpy as np
+        self.sizes = np.ascontiguousarray(sizes, dtype=np.int64)
+        packed = np.concatenate([[0], np.cumsum(self.sizes)[:-1]]).astype(np.int64)
+        self.in_off = np.ascontiguousarray(packed if in_off is None else in_off, dtype=np.int64)
+        self.out_off = np.ascontiguousarray(packed if out_off is None else out_off, dtype=np.int64)
+        self.scale = None if scale is None else np.ascontiguousarray(scale, dtype=np.float32)
+        self.precision = precision
+        self.total_in = int((self.in_off + self.sizes).max())
+        self.total_out = int((self.out_off + self.sizes).max())
+        self._h = ctypes.c_void_p()
+        sc = None if self.scale is None else self.scale.ctypes.data
+        _check(lib().tcfft_batch_plan(ctypes.byref(self._h), len(self.sizes), self.sizes.ctypes.data,
+                                      self.in_off.ctypes.data, self.out_off.ctypes.data, sc, precision,
+                                      int(direction)), "batch_plan")
+
+    @property
+    def elem_bytes(self):
+        return 4 if self.precision == FP16 else 8
+
+    def set_mode(self, mode):
+        _check(lib().tcfft_batch_set_mode(self._h, int(mode)), "batch_set_mode")
+
+    def set_graph(self, enable):
+        _check(lib().tcfft_batch_set_graph(self._h, 1 if enable else 0), "batch_set_graph")
+
+    def info(self):
+        items, ctas, ws = ctypes.c_int(), ctypes.c_int(), ctypes.c_size_t()
+        _check(lib().tcfft_batch_info(self._h, ctypes.byref(items), ctypes.byref(ws), ctypes.byref(ctas)))
+        return {"items": items.value, "workspace_bytes": ws.value, "ctas": ctas.value}
+
+    def exec(self, x, out, stream=None):
+        for t, need in ((x, self.total_in), (out, self.total_out)):
+            if not t.is_cuda or not t.is_contiguous() or t.numel() * t.element_size() < need * self.elem_bytes:
+                raise TcfftError(INVALID_VALUE, "tensor must be contiguous CUDA with >= %d bytes"
+                                 % (need * self.elem_bytes))
+        _check(lib().tcfft_batch_exec(self._h, _ptr(x), _ptr(out), _stream_ptr(stream)), "batch_exec")
+        return out
+
+    def check(self, stream=None):
+        _check(lib().tcfft_batch_check(self._h, _stream_ptr(stream)), "batch_check")
+
+    def destroy(self):
+        if self._h:
+            lib().tcfft_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
 
 
 def plan_1d(n, batch=1, precision=FP16):

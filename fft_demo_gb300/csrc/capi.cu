@@ -476,7 +476,8 @@ tcfftStatus tcfft_plan_1d(tcfftPlan* plan, long long n, long long batch, int pre
       const bool can_fuse = precision == TCFFT_FP16 && logn >= kFusedMinLog && logn <= kFusedMaxLog &&
                             g_fused[logn][0].fn && g_fused[logn][0].log_n1 == p->log_n1;
       if (s == TCFFT_OK && can_fuse) {
-        // chunks of ~16 MiB; a ring of two workspace slots
+        // fused form available (tcfft_plan_set_fused): chunks of ~16 MiB in a
+        // ring of two workspace slots, allocated when it is switched on
         const long long per_seq = n * 4;
         long long cs = (16ll << 20) / per_seq;
         if (cs < 1) cs = 1;
@@ -484,12 +485,10 @@ tcfftStatus tcfft_plan_1d(tcfftPlan* plan, long long n, long long batch, int pre
         p->chunk_seqs = static_cast<int>(cs);
         p->nchunks = static_cast<int>((batch + cs - 1) / cs);
         p->ring = p->nchunks >= 2 ? 2 : 1;
-        p->ws_bytes = static_cast<size_t>(p->ring) * static_cast<size_t>(cs) * static_cast<size_t>(per_seq);
-        if (cudaMalloc(&p->ring_ws, p->ws_bytes) != cudaSuccess ||
-            cudaMalloc(&p->counters, sizeof(int) * (1 + 2 * static_cast<size_t>(p->nchunks))) != cudaSuccess)
-          s = TCFFT_ALLOC_FAILED;
-        p->fused = true;
-      } else if (s == TCFFT_OK) {
+      }
+      // default: two pass launches through a full-size workspace (faster than
+      // the fused launch on every size measured so far)
+      if (s == TCFFT_OK) {
         p->ws_bytes = static_cast<size_t>(n) * static_cast<size_t>(batch) * (precision == TCFFT_FP16 ? 4u : 8u);
         if (cudaMalloc(&p->ws, p->ws_bytes) != cudaSuccess) s = TCFFT_ALLOC_FAILED;
       }
@@ -536,7 +535,17 @@ tcfftStatus tcfft_plan_2d(tcfftPlan* plan, int nx, int ny, long long batch, int 
 tcfftStatus tcfft_plan_set_fused(tcfftPlan p, int enable) {
   if (!p) return ret(TCFFT_INVALID_VALUE);
   if (enable) {
-    if (!p->ring_ws) return ret(TCFFT_UNSUPPORTED);
+    if (p->chunk_seqs == 0) return ret(TCFFT_UNSUPPORTED);
+    if (!p->ring_ws) {
+      const size_t ring_bytes =
+          static_cast<size_t>(p->ring) * static_cast<size_t>(p->chunk_seqs) * static_cast<size_t>(p->n) * 4u;
+      if (cudaMalloc(&p->ring_ws, ring_bytes) != cudaSuccess) return ret(TCFFT_ALLOC_FAILED);
+      if (cudaMalloc(&p->counters, sizeof(int) * (1 + 2 * static_cast<size_t>(p->nchunks))) != cudaSuccess) {
+        cudaFree(p->ring_ws);
+        p->ring_ws = nullptr;
+        return ret(TCFFT_ALLOC_FAILED);
+      }
+    }
     p->fused = true;
     return ret(TCFFT_OK);
   }

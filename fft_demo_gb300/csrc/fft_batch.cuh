@@ -1,0 +1,327 @@
+// Persistent batch kernel: 1D transforms of uneven sizes in one launch, fed
+// from a device-side work queue.
+//
+// The caller's transforms sit anywhere in one input and one output buffer
+// (element offsets per transform). The host plan sorts them by size and
+// writes a list of work items (tiles):
+//   kItemLines : up to G = 8192 / L whole transforms of one size L <= 2^13,
+//                single pass; transform offsets come from the line tables
+//   kItemP1    : a column-pass tile of one larger transform (four-step pass
+//                1: lines of length n1, outer twiddle W_n, into the plan's
+//                workspace)
+//   kItemP2    : a transposing row-pass tile of the same transform (pass 2:
+//                lines of length n2, workspace -> output)
+// CTAs take items with one atomic counter, in list order. A P2 item waits
+// (bounded) until the transform's counter shows all of its P1 tiles done;
+// every P1 tile bumps that counter after a device-scope fence. The host puts
+// every P2 item after all P1 items of its transform, so a wait only ever
+// targets items that running CTAs already hold, and the chain of waits ends
+// at an item that waits for nothing: the queue cannot deadlock, whether or
+// not every CTA of the grid is resident at once.
+//
+// All tiles hold 512 rows of the 16-column MMA layout (Mt = 512), FP16 or
+// split precision, so one TMEM allocation and one shared-memory carve-out
+// serve every item kind and size.
+#pragma once
+#include "fft_fused.cuh"
+#include "fft_io.cuh"
+#include "fft_split.cuh"
+#include "fft_tile.cuh"
+
+namespace tcfft {
+
+enum : int { kItemLines = 0, kItemP1 = 1, kItemP2 = 2 };
+
+constexpr int kBatchMt = 512;
+constexpr int kBatchMinLineLog = 6, kBatchMaxLineLog = 13;  // single-pass sizes
+constexpr int kBatchMinPassLog = 7, kBatchMaxPassLog = 10;  // four-step pass lengths
+constexpr int kBatchMaxLog = 2 * kBatchMaxPassLog;          // largest transform
+
+struct BatchItem {
+  int kind;
+  int logl;          // pass length of this tile
+  int line0;         // kItemLines: first entry of the line tables; P1/P2: first line in the pass
+  int nlines;        // kItemLines: transforms in this tile
+  int xform;         // P1 / P2: transform index
+  float scale;       // applied on the final store
+  int pad0, pad1;
+};
+
+struct BatchXform {
+  long long in_off, out_off, ws_off;  // element offsets
+  int logn, log_n1, log_n2, tiles1;   // tiles1: P1 tiles of this transform
+};
+
+struct BatchArgs {
+  const void* in;
+  void* out;
+  void* ws;
+  const long long* line_in;  // per single-pass transform, sorted by size: element offsets
+  const long long* line_out;
+  const BatchItem* items;
+  int nitems;
+  const BatchXform* xforms;
+  unsigned int* counter;  // queue head
+  int* done;              // per transform: P1 tiles finished
+  const float2* tw[kBatchMaxLineLog + 1];  // W_L, this direction
+  OuterTwiddle otw[kBatchMaxLog + 1];      // W_n factor tables per log2 n
+  const uint32_t* bmat;                    // DFT16 B image (hi, lo), this direction
+  int* err;
+};
+
+// Whole lines found through per-line offset tables (each line contiguous).
+template <class E>
+struct IoLines {
+  static constexpr bool IN_VEC_L = true;
+  static constexpr bool OUT_VEC_L = true;
+  struct Raw2 {
+    uint4 a, b;
+  };
+  using Raw = typename std::conditional<sizeof(E) == 4, uint4, Raw2>::type;
+
+  const E* in;
+  E* out;
+  const long long* loff_in;
+  const long long* loff_out;
+  long long total_lines;
+  float scale;
+  bool in_contig = false, out_contig = false;  // lines are scattered: no bulk tile copies
+  long long contig_len = 0;
+
+  __device__ __forceinline__ Raw fetch_l(long long line, int l0, bool ok) const {
+    Raw r;
+    if constexpr (sizeof(E) == 4) {
+      r = make_uint4(0, 0, 0, 0);
+      if (ok && line < total_lines) r = ldg_nc_v4(in + __ldg(loff_in + line) + l0);
+    } else {
+      r.a = r.b = make_uint4(0, 0, 0, 0);
+      if (ok && line < total_lines) {
+        const E* p = in + __ldg(loff_in + line) + l0;
+        r.a = ldg_nc_v4(p);
+        r.b = ldg_nc_v4(p + 2);
+      }
+    }
+    return r;
+  }
+  __device__ __forceinline__ Raw fetch_g(long long, int, bool) const { return Raw{}; }
+  __device__ __forceinline__ void decode_l(const Raw& r, long long, int, float2 (&v)[4]) const {
+    if constexpr (sizeof(E) == 4) {
+      unpack_h2x4(r, v);
+    } else {
+      v[0] = make_float2(__uint_as_float(r.a.x), __uint_as_float(r.a.y));
+      v[1] = make_float2(__uint_as_float(r.a.z), __uint_as_float(r.a.w));
+      v[2] = make_float2(__uint_as_float(r.b.x), __uint_as_float(r.b.y));
+      v[3] = make_float2(__uint_as_float(r.b.z), __uint_as_float(r.b.w));
+    }
+  }
+  __device__ __forceinline__ void decode_g(const Raw&, long long, int, float2 (&)[4]) const {}
+  __device__ __forceinline__ void store_row16(long long line, int j, int J, float2 (&v)[16]) const {
+    E* p = out + __ldg(loff_out + line) + j;
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      if constexpr (sizeof(E) == 4)
+        p[c * J] = __floats2half2_rn(v[c].x * scale, v[c].y * scale);
+      else
+        p[c * J] = make_float2(v[c].x * scale, v[c].y * scale);
+    }
+  }
+  __device__ __forceinline__ const E* tile_src(long long) const { return in; }
+  __device__ __forceinline__ E* tile_dst(long long) const { return out; }
+};
+
+template <bool SPLIT>
+struct BatchPrec;
+
+template <>
+struct BatchPrec<false> {
+  using E = half2;
+  using State = PassState;
+  static constexpr uint32_t kTmemCols = kBatchMt / 4;
+  template <bool IN_L, bool OUT_L, bool COH>
+  using Io = IoHalf<IN_L, OUT_L, COH>;
+  template <int L, bool LM, int SIGN, class IO>
+  __device__ static bool tile(State& st, const IO& io, const PassCore& core, long long line0) {
+    return pass_tile<L, kBatchMt * 16 / L, LM, SIGN, IO>(st, io, core, line0);
+  }
+  __device__ static void setup(State& st, const uint32_t* bmat) { pass_setup<kTmemCols>(st, bmat); }
+  __device__ static void teardown(State& st) { pass_teardown<kTmemCols>(st); }
+};
+
+template <>
+struct BatchPrec<true> {
+  using E = float2;
+  using State = SplitState;
+  static constexpr uint32_t kTmemCols = kBatchMt / 2;
+  template <bool IN_L, bool OUT_L, bool COH>
+  using Io = IoFloat<IN_L, OUT_L, COH>;
+  template <int L, bool LM, int SIGN, class IO>
+  __device__ static bool tile(State& st, const IO& io, const PassCore& core, long long line0) {
+    return split_tile<L, kBatchMt * 16 / L, LM, SIGN, IO>(st, io, core, line0);
+  }
+  __device__ static void setup(State& st, const uint32_t* bmat) { split_setup<kTmemCols>(st, bmat); }
+  __device__ static void teardown(State& st) { split_teardown<kTmemCols>(st); }
+};
+
+template <bool SPLIT, int SIGN, int L>
+__device__ __noinline__ bool batch_lines_item(typename BatchPrec<SPLIT>::State& st, const BatchArgs& a,
+                                              const BatchItem& it, const PassCore& core) {
+  using P = BatchPrec<SPLIT>;
+  using E = typename P::E;
+  IoLines<E> io;
+  io.in = static_cast<const E*>(a.in);
+  io.out = static_cast<E*>(a.out);
+  io.loff_in = a.line_in + it.line0;
+  io.loff_out = a.line_out + it.line0;
+  io.total_lines = it.nlines;
+  io.scale = it.scale;
+  return P::template tile<L, false, SIGN>(st, io, core, 0);
+}
+
+template <bool SPLIT, int SIGN, int L>
+__device__ __noinline__ bool batch_p1_item(typename BatchPrec<SPLIT>::State& st, const BatchArgs& a,
+                                           const BatchItem& it, const PassCore& core) {
+  using P = BatchPrec<SPLIT>;
+  using E = typename P::E;
+  const BatchXform xf = a.xforms[it.xform];
+  const long long n = 1ll << xf.logn, n2 = 1ll << xf.log_n2;
+  typename P::template Io<false, false, false> io;
+  io.in = static_cast<const E*>(a.in) + xf.in_off;
+  io.out = static_cast<E*>(a.ws) + xf.ws_off;
+  io.total_lines = n2;
+  io.lps_log2 = xf.log_n2;
+  io.in_seq = io.out_seq = n;
+  io.in_line = io.out_line = 1;
+  io.in_elem = io.out_elem = n2;
+  io.otw = a.otw[xf.logn];
+  io.scale = 1.0f;
+  io.in_contig = io.out_contig = false;
+  io.contig_len = L;
+  return P::template tile<L, true, SIGN>(st, io, core, static_cast<long long>(it.line0));
+}
+
+template <bool SPLIT, int SIGN, int L>
+__device__ __noinline__ bool batch_p2_item(typename BatchPrec<SPLIT>::State& st, const BatchArgs& a,
+                                           const BatchItem& it, const PassCore& core) {
+  using P = BatchPrec<SPLIT>;
+  using E = typename P::E;
+  const BatchXform xf = a.xforms[it.xform];
+  const long long n = 1ll << xf.logn, n1 = 1ll << xf.log_n1, n2 = 1ll << xf.log_n2;
+  typename P::template Io<true, false, true> io;
+  io.in = static_cast<const E*>(a.ws) + xf.ws_off;
+  io.out = static_cast<E*>(a.out) + xf.out_off;
+  io.total_lines = n1;
+  io.lps_log2 = xf.log_n1;
+  io.in_seq = io.out_seq = n;
+  io.in_line = n2;
+  io.in_elem = 1;
+  io.out_line = 1;
+  io.out_elem = n1;
+  io.otw = OuterTwiddle();
+  io.scale = it.scale;
+  io.in_contig = io.out_contig = false;
+  io.contig_len = L;
+  return P::template tile<L, true, SIGN>(st, io, core, static_cast<long long>(it.line0));
+}
+
+template <bool SPLIT, int SIGN>
+__device__ __forceinline__ bool batch_run_item(typename BatchPrec<SPLIT>::State& st, const BatchArgs& a,
+                                               const BatchItem& it) {
+  PassCore core;
+  core.tw = a.tw[it.logl];
+  core.bmat = a.bmat;
+  core.err = a.err;
+  if (it.kind == kItemLines) {
+    switch (it.logl) {
+      case 6: return batch_lines_item<SPLIT, SIGN, 64>(st, a, it, core);
+      case 7: return batch_lines_item<SPLIT, SIGN, 128>(st, a, it, core);
+      case 8: return batch_lines_item<SPLIT, SIGN, 256>(st, a, it, core);
+      case 9: return batch_lines_item<SPLIT, SIGN, 512>(st, a, it, core);
+      case 10: return batch_lines_item<SPLIT, SIGN, 1024>(st, a, it, core);
+      case 11: return batch_lines_item<SPLIT, SIGN, 2048>(st, a, it, core);
+      case 12: return batch_lines_item<SPLIT, SIGN, 4096>(st, a, it, core);
+      case 13: return batch_lines_item<SPLIT, SIGN, 8192>(st, a, it, core);
+      default: break;
+    }
+  } else if (it.kind == kItemP1) {
+    switch (it.logl) {
+      case 7: return batch_p1_item<SPLIT, SIGN, 128>(st, a, it, core);
+      case 8: return batch_p1_item<SPLIT, SIGN, 256>(st, a, it, core);
+      case 9: return batch_p1_item<SPLIT, SIGN, 512>(st, a, it, core);
+      case 10: return batch_p1_item<SPLIT, SIGN, 1024>(st, a, it, core);
+      default: break;
+    }
+  } else if (it.kind == kItemP2) {
+    switch (it.logl) {
+      case 7: return batch_p2_item<SPLIT, SIGN, 128>(st, a, it, core);
+      case 8: return batch_p2_item<SPLIT, SIGN, 256>(st, a, it, core);
+      case 9: return batch_p2_item<SPLIT, SIGN, 512>(st, a, it, core);
+      case 10: return batch_p2_item<SPLIT, SIGN, 1024>(st, a, it, core);
+      default: break;
+    }
+  }
+  if (threadIdx.x == 0) atomicOr(a.err, kErrBadArgs);
+  return true;
+}
+
+template <bool SPLIT, int SIGN>
+__global__ void __launch_bounds__(kPassThreads, SPLIT ? 2 : 3) fft_batch_kernel(const __grid_constant__ BatchArgs a) {
+  using P = BatchPrec<SPLIT>;
+  __shared__ unsigned int s_item;
+  __shared__ int s_ok;
+  typename P::State st;
+  P::setup(st, a.bmat);
+  bool alive = true;
+  while (alive) {
+    if (threadIdx.x == 0) s_item = atomicAdd(a.counter, 1u);
+    __syncthreads();
+    const unsigned int i = s_item;
+    if (i >= static_cast<unsigned int>(a.nitems)) break;
+    const BatchItem it = a.items[i];
+    if (threadIdx.x == 0) {
+      bool ok = true;
+      if (it.kind == kItemP2) ok = wait_counter(a.done + it.xform, a.xforms[it.xform].tiles1);
+      if (!ok) atomicOr(a.err, kErrQueueTimeout);
+      s_ok = ok;
+    }
+    __syncthreads();
+    if (s_ok) alive = batch_run_item<SPLIT, SIGN>(st, a, it);
+    if (it.kind == kItemP1) {
+      // publish: every thread's stores are visible device-wide before the count
+      __threadfence();
+      __syncthreads();
+      if (threadIdx.x == 0) atomicAdd(a.done + it.xform, 1);
+    }
+    __syncthreads();  // s_item / s_ok are rewritten next round
+  }
+  P::teardown(st);
+}
+
+template <bool SPLIT>
+constexpr int batch_smem_bytes() {
+  if constexpr (SPLIT)
+    return split_smem_bytes<64, kBatchMt * 16 / 64>();
+  else
+    return pass_smem_bytes<64, kBatchMt * 16 / 64>();
+}
+
+}  // namespace tcfft
+
+namespace tcfft {
+
+// Registry entries for the batch kernel, per precision and direction
+// (index 0 forward, 1 inverse).
+struct BatchKernel {
+  const void* fn = nullptr;
+  int smem = 0;
+};
+void register_batch_kernels_f16(BatchKernel (&tab)[2]);
+void register_batch_kernels_split(BatchKernel (&tab)[2]);
+
+template <bool SPLIT>
+void fill_batch(BatchKernel (&tab)[2]) {
+  tab[0].fn = reinterpret_cast<const void*>(&fft_batch_kernel<SPLIT, -1>);
+  tab[1].fn = reinterpret_cast<const void*>(&fft_batch_kernel<SPLIT, +1>);
+  tab[0].smem = tab[1].smem = batch_smem_bytes<SPLIT>();
+}
+
+}  // namespace tcfft

@@ -435,7 +435,9 @@ constexpr int split_smem_bytes() {
 }
 
 // Interleaved complex float in and out, arbitrary strides (in elements).
-template <bool IN_L, bool OUT_L>
+// COHERENT: input is read with L2-coherent loads (written by other CTAs of the
+// same launch).
+template <bool IN_L, bool OUT_L, bool COHERENT = false>
 struct IoFloat {
   static constexpr bool IN_VEC_L = IN_L;
   static constexpr bool OUT_VEC_L = OUT_L;
@@ -464,16 +466,16 @@ struct IoFloat {
     Raw r{make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
     if (!ok || line >= total_lines) return r;
     const float2* p = in + in_base(line) + l0;
-    r.a = ldg_nc_v4(p);
-    r.b = ldg_nc_v4(p + 2);
+    r.a = COHERENT ? ldg_cg_v4(p) : ldg_nc_v4(p);
+    r.b = COHERENT ? ldg_cg_v4(p + 2) : ldg_nc_v4(p + 2);
     return r;
   }
   __device__ __forceinline__ Raw fetch_g(long long line0, int l, bool ok) const {
     Raw r{make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
     if (!ok || line0 >= total_lines) return r;
     const float2* p = in + in_base(line0) + static_cast<long long>(l) * in_elem;
-    r.a = ldg_nc_v4(p);
-    r.b = ldg_nc_v4(p + 2);
+    r.a = COHERENT ? ldg_cg_v4(p) : ldg_nc_v4(p);
+    r.b = COHERENT ? ldg_cg_v4(p + 2) : ldg_nc_v4(p + 2);
     return r;
   }
   __device__ __forceinline__ static void unpack(const Raw& r, float2 (&v)[4]) {

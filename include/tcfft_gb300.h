@@ -62,10 +62,11 @@ tcfftStatus tcfft_plan_1d(tcfftPlan *plan, long long n, long long batch, int pre
  * nx, ny = 2^k in [16, 4096]. */
 tcfftStatus tcfft_plan_2d(tcfftPlan *plan, int nx, int ny, long long batch, int precision);
 
-/* 1D FP16 plans with 2^15 <= n <= 2^24 run both four-step passes in one
- * persistent launch that keeps the intermediate in a small L2-resident
- * workspace ring (default). enable = 0 switches the plan to two separate
- * pass launches through a full-size workspace (allocated on first use). */
+/* 1D FP16 plans with 2^15 <= n <= 2^24 can run both four-step passes in
+ * one persistent launch that keeps the intermediate in a small L2-resident
+ * workspace ring (enable = 1; the ring is allocated on first use). The
+ * default, enable = 0, is two pass launches through the plan's full-size
+ * workspace. Both forms give bit-identical results. */
 tcfftStatus tcfft_plan_set_fused(tcfftPlan plan, int enable);
 
 /* Bytes of device workspace the plan holds (allocated at plan time). */
@@ -130,7 +131,8 @@ tcfftStatus tcfft_exec_static(const void *in, void *out, long long n, long long 
  *                          ox = sx; S must be 1 or the channels are summed.
  *   TCFFT_CONV_FULL        full linear convolution; oy = sy+fy-1,
  *                          ox = sx+fx-1 (convolve_direct_fft family,
- *                          fftconvolve2d.cu:184, without its 1/fftSize).
+ *                          fftconvolve2d.cu:184, whose 1/fftSize cancels
+ *                          its unnormalised C2R inverse).
  * The padded transform size P is the smallest power of two without
  * wrap-around inside the output window (P <= 4096 FP16, <= 2048 split).
  * ------------------------------------------------------------------------ */
@@ -155,6 +157,33 @@ tcfftStatus tcfft_conv2d_shape(tcfftConv conv, int *out_rows, int *out_cols, int
 /* Synchronise `stream`, report a flagged device error. */
 tcfftStatus tcfft_conv2d_check(tcfftConv conv, void *stream);
 tcfftStatus tcfft_conv2d_destroy(tcfftConv conv);
+
+/* ------------------------------------------------------------------------
+ * Uneven batches: many 1D transforms of different power-of-two sizes
+ * (64 <= n <= 2^20) anywhere in one input and one output buffer, run by one
+ * persistent launch fed from a device work queue. No counterpart in the
+ * reference, whose plans hold one size and one contiguous batch
+ * (tcfft_half.cu:1235); its per-size form is TCFFT_BATCH_PER_SIZE below.
+ * n[i], in_off[i], out_off[i]: size and element offsets of transform i;
+ * scale: per-transform output scale (NULL = 1). Offsets must keep every
+ * transform 16-byte aligned.
+ * ------------------------------------------------------------------------ */
+typedef struct tcfftBatchImpl *tcfftBatch;
+typedef enum tcfftBatchMode {
+  TCFFT_BATCH_PERSISTENT = 0,  /* one persistent launch (default) */
+  TCFFT_BATCH_PER_SIZE = 1     /* plain path: one tcfft_exec per run of adjacent same-size transforms */
+} tcfftBatchMode;
+tcfftStatus tcfft_batch_plan(tcfftBatch *batch, int count, const long long *n, const long long *in_off,
+                             const long long *out_off, const float *scale, int precision, int direction);
+tcfftStatus tcfft_batch_set_mode(tcfftBatch batch, int mode);
+/* enable != 0: tcfft_batch_exec replays a CUDA graph of its launches,
+ * captured on the first call for these buffers (re-captured when they change). */
+tcfftStatus tcfft_batch_set_graph(tcfftBatch batch, int enable);
+tcfftStatus tcfft_batch_exec(tcfftBatch batch, const void *in, void *out, void *stream);
+/* Work items of the persistent launch, workspace bytes, persistent CTAs. */
+tcfftStatus tcfft_batch_info(tcfftBatch batch, int *items, size_t *workspace_bytes, int *ctas);
+tcfftStatus tcfft_batch_check(tcfftBatch batch, void *stream);
+tcfftStatus tcfft_batch_destroy(tcfftBatch batch);
 
 /* Last status returned on this thread, and a readable name for a status. */
 tcfftStatus tcfft_get_last_error(void);

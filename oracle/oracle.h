@@ -22,7 +22,8 @@
  *   orc_conv2d_same        - 'same'-mode true 2D convolution (odd filters).
  *   orc_conv2d_full        - full linear 2D convolution, one image with
  *                            kernelCount filters (convolve_direct_fft,
- *                            fftconvolve2d.cu:184, without its 1/fftSize).
+ *                            fftconvolve2d.cu:184: its 1/fftSize
+ *                            cancels the unnormalised C2R inverse).
  *   orc_clipped_error      - get_error (main.cpp:118).
  *
  * Parity pins: the FFT against the direct DFT and known-answer vectors; the

@@ -65,3 +65,26 @@ def test_no_device_is_reported(built_lib):
     import fft_demo_gb300 as t
     h = ctypes.c_void_p()
     assert t.lib().tcfft_plan_1d(ctypes.byref(h), 1024, 4, t.FP16) == t.NO_DEVICE
+
+
+def test_batch_plan_validation_without_device(built_lib):
+    import numpy as np
+    import fft_demo_gb300 as t
+    L = t.lib()
+    h = ctypes.c_void_p()
+
+    def plan(sizes, offs, prec=t.FP16, direction=t.FORWARD):
+        n = np.asarray(sizes, np.int64)
+        o = np.asarray(offs, np.int64)
+        return L.tcfft_batch_plan(ctypes.byref(h), len(n), n.ctypes.data, o.ctypes.data, o.ctypes.data,
+                                  None, prec, direction)
+
+    assert plan([32], [0]) == t.INVALID_SIZE          # below 64 points
+    assert plan([1 << 21], [0]) == t.INVALID_SIZE     # above 2^20
+    assert plan([96], [0]) == t.INVALID_SIZE          # not a power of two
+    assert plan([64, 64], [0, 66]) == t.INVALID_VALUE  # FP16 offsets keep 16-byte alignment
+    assert plan([64, 64], [0, 65], t.SPLIT_FP32) == t.INVALID_VALUE
+    assert plan([64], [0], 5) == t.INVALID_VALUE
+    assert plan([64], [0], t.FP16, 0) == t.INVALID_VALUE
+    assert L.tcfft_batch_plan(None, 1, None, None, None, None, t.FP16, t.FORWARD) == t.INVALID_VALUE
+    assert L.tcfft_batch_exec(None, None, None, None) == t.INVALID_VALUE

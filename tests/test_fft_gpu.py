@@ -158,6 +158,7 @@ def test_fused_four_step_matches_two_pass(tc, orc, n, batch):
     g.manual_seed(n)
     x = (torch.rand((batch, n, 2), device="cuda", generator=g) * 2 - 1).half()
     plan = tc.plan_1d(n, batch)
+    plan.set_fused(True)
     y_fused = torch.empty_like(x)
     plan.exec(x, y_fused)
     plan.check()

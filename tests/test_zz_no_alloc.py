@@ -35,6 +35,7 @@ def _input(n, batch, seed):
 
 def _plan_out(tc, x, n, batch, direction, scale):
     plan = tc.plan_1d(n, batch)
+    plan.set_fused(True)
     out = x.clone().zero_()
     plan.exec(x, out, direction=direction, scale=scale)
     plan.check()
