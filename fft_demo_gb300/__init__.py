@@ -63,6 +63,8 @@ def _declare(L):
         "tcfft_check": (i, [vp, vp]),
         "tcfft_exec_static": (i, [vp, vp, ll, ll, i, f, vp, i]),
         "tcfft_batch_plan": (i, [ctypes.POINTER(vp), i, vp, vp, vp, vp, i, i]),
+        "tcfft_batch_plan_mixed": (i, [ctypes.POINTER(vp), i, vp, vp, vp, vp, i, vp, vp, ll, i, i]),
+        "tcfft_batch_exec_mixed": (i, [vp, vp, vp, vp, vp, vp]),
         "tcfft_batch_set_mode": (i, [vp, i]),
         "tcfft_batch_set_graph": (i, [vp, i]),
         "tcfft_batch_exec": (i, [vp, vp, vp, vp]),
@@ -215,30 +217,72 @@ def exec_static(x, n, batch, out=None, direction=FORWARD, scale=1.0, stream=None
     return out
 
 
+class BatchConvDesc(ctypes.Structure):
+    """tcfftBatchConv: one convolution of a batch plan."""
+    _fields_ = [("sy", ctypes.c_int), ("sx", ctypes.c_int), ("fy", ctypes.c_int), ("fx", ctypes.c_int),
+                ("mode", ctypes.c_int), ("img_off", ctypes.c_longlong), ("out_off", ctypes.c_longlong),
+                ("filt_off", ctypes.c_longlong)]
+
+
+def conv_output_shape(sy, sx, fy, fx, mode):
+    if mode == CONV_VALID_CORR:
+        return sy - fy + 1, sx - fx + 1
+    if mode == CONV_SAME:
+        return sy, sx
+    return sy + fy - 1, sx + fx - 1
+
+
 class Batch:
     """Many 1D transforms of uneven power-of-two sizes (64 <= n <= 2^20) in
-    one input and one output buffer (tcfft_batch_plan): one persistent
-    launch fed from a device work queue, or the plain per-size path.
+    one input and one output buffer, and optionally 2D convolutions
+    (tcfft_batch_plan_mixed): one persistent launch fed from a device work
+    queue, or the plain per-size path.
 
     sizes[i], in_off[i], out_off[i]: points and element offsets of
     transform i (default: packed back to back in list order).
+    convs: list of (sy, sx, fy, fx, mode) -- images, outputs and filters are
+    packed back to back in list order in their own buffers; `filters` holds
+    the fy x fx float filters (a CUDA float tensor or a numpy array).
     """
 
-    def __init__(self, sizes, in_off=None, out_off=None, scale=None, precision=FP16, direction=FORWARD):
+    def __init__(self, sizes=(), in_off=None, out_off=None, scale=None, precision=FP16, direction=FORWARD,
+                 convs=(), filters=None):
         import numpy as np
         self.sizes = np.ascontiguousarray(sizes, dtype=np.int64)
-        packed = np.concatenate([[0], np.cumsum(self.sizes)[:-1]]).astype(np.int64)
+        packed = np.concatenate([[0], np.cumsum(self.sizes)[:-1]]).astype(np.int64) if len(self.sizes) else \
+            np.zeros(0, np.int64)
         self.in_off = np.ascontiguousarray(packed if in_off is None else in_off, dtype=np.int64)
         self.out_off = np.ascontiguousarray(packed if out_off is None else out_off, dtype=np.int64)
         self.scale = None if scale is None else np.ascontiguousarray(scale, dtype=np.float32)
         self.precision = precision
-        self.total_in = int((self.in_off + self.sizes).max())
-        self.total_out = int((self.out_off + self.sizes).max())
+        self.total_in = int((self.in_off + self.sizes).max()) if len(self.sizes) else 0
+        self.total_out = int((self.out_off + self.sizes).max()) if len(self.sizes) else 0
+        descs = (BatchConvDesc * max(1, len(convs)))()
+        img = out = filt = 0
+        self.conv_shapes = []
+        for k, (sy, sx, fy, fx, mode) in enumerate(convs):
+            oy, ox = conv_output_shape(sy, sx, fy, fx, mode)
+            descs[k] = BatchConvDesc(sy, sx, fy, fx, mode, img, out, filt)
+            self.conv_shapes.append(((sy, sx), (oy, ox), img, out, filt))
+            img += sy * sx
+            out += oy * ox
+            filt += fy * fx
+        self.conv_in_elems, self.conv_out_elems, self.filter_elems = img, out, filt
+        fptr = None
+        if len(convs):
+            if hasattr(filters, "data_ptr"):
+                fptr = filters.data_ptr()
+            else:
+                self._filters_host = np.ascontiguousarray(filters, dtype=np.float32).ravel()
+                fptr = self._filters_host.ctypes.data
         self._h = ctypes.c_void_p()
         sc = None if self.scale is None else self.scale.ctypes.data
-        _check(lib().tcfft_batch_plan(ctypes.byref(self._h), len(self.sizes), self.sizes.ctypes.data,
-                                      self.in_off.ctypes.data, self.out_off.ctypes.data, sc, precision,
-                                      int(direction)), "batch_plan")
+        _check(lib().tcfft_batch_plan_mixed(
+            ctypes.byref(self._h), len(self.sizes), self.sizes.ctypes.data if len(self.sizes) else None,
+            self.in_off.ctypes.data if len(self.sizes) else None,
+            self.out_off.ctypes.data if len(self.sizes) else None, sc, len(convs),
+            ctypes.cast(descs, ctypes.c_void_p) if len(convs) else None, fptr, filt, precision, int(direction)),
+            "batch_plan")
 
     @property
     def elem_bytes(self):
@@ -255,12 +299,19 @@ class Batch:
         _check(lib().tcfft_batch_info(self._h, ctypes.byref(items), ctypes.byref(ws), ctypes.byref(ctas)))
         return {"items": items.value, "workspace_bytes": ws.value, "ctas": ctas.value}
 
-    def exec(self, x, out, stream=None):
-        for t, need in ((x, self.total_in), (out, self.total_out)):
-            if not t.is_cuda or not t.is_contiguous() or t.numel() * t.element_size() < need * self.elem_bytes:
-                raise TcfftError(INVALID_VALUE, "tensor must be contiguous CUDA with >= %d bytes"
-                                 % (need * self.elem_bytes))
-        _check(lib().tcfft_batch_exec(self._h, _ptr(x), _ptr(out), _stream_ptr(stream)), "batch_exec")
+    def exec(self, x=None, out=None, conv_in=None, conv_out=None, stream=None):
+        rb = self.elem_bytes // 2
+        checks = []
+        if len(self.sizes):
+            checks += [(x, self.total_in * self.elem_bytes), (out, self.total_out * self.elem_bytes)]
+        if self.conv_shapes:
+            checks += [(conv_in, self.conv_in_elems * rb), (conv_out, self.conv_out_elems * rb)]
+        for t, need in checks:
+            if t is None or not t.is_cuda or not t.is_contiguous() or t.numel() * t.element_size() < need:
+                raise TcfftError(INVALID_VALUE, "tensor must be contiguous CUDA with >= %d bytes" % need)
+        p = lambda t: None if t is None else _ptr(t)  # noqa: E731
+        _check(lib().tcfft_batch_exec_mixed(self._h, p(x), p(out), p(conv_in), p(conv_out),
+                                            _stream_ptr(stream)), "batch_exec")
         return out
 
     def check(self, stream=None):

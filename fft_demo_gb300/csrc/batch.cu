@@ -76,6 +76,16 @@ int batch_log_n1(int logn) {
   return a;
 }
 
+struct Buffers {
+  const void* in;
+  void* out;
+  const void* conv_in;
+  void* conv_out;
+  bool operator==(const Buffers& o) const {
+    return in == o.in && out == o.out && conv_in == o.conv_in && conv_out == o.conv_out;
+  }
+};
+
 constexpr int kMinLog = kBatchMinLineLog;  // 64 points
 constexpr int kMaxLog = kBatchMaxLog;      // 2^20 points
 
@@ -92,17 +102,21 @@ struct tcfftBatchImpl {
   std::vector<long long> n, in_off, out_off;
   std::vector<float> scale;
   // persistent launch
-  int nitems = 0, nxforms = 0, ctas = 0;
+  int nitems = 0, nxforms = 0, nctrs = 1, ctas = 0;
   size_t ws_bytes = 0;
   void* ws = nullptr;
   void* arena = nullptr;  // tables, line tables, items, transforms
   int* ctr = nullptr;     // [0] queue head, [1 ..] per-transform done counters
   int* err = nullptr;
   BatchArgs args{};
+  // convolutions: descriptors, a plan-owned copy of the filters, spectra
+  std::vector<tcfftBatchConv> conv_desc;
+  float* filters = nullptr;
+  void* kspec = nullptr;
+  std::map<int, tcfftConv> conv_plans;  // plain path: one plan per convolution
   // graph replay
   cudaGraphExec_t graph = nullptr;
-  const void* graph_in = nullptr;
-  void* graph_out = nullptr;
+  Buffers graph_io{};
   int graph_mode = -1;
   int graph_launches = 0;
   // plain per-size path: plans per (log2 n, run length)
@@ -118,16 +132,92 @@ namespace {
 
 struct Built {
   std::vector<long long> line_in, line_out;
-  std::vector<BatchItem> items;
+  std::vector<BatchItem> items;       // main launch
+  std::vector<BatchItem> prep_items;  // filter-spectrum launch (plan time)
   std::vector<BatchXform> xforms;
-  size_t ws_elems = 0;
+  std::vector<BatchConv> convs;
+  size_t ws_elems = 0, kspec_elems = 0;
+  int nctrs = 0;  // dependency counters
 };
 
-// Work list: single-pass transforms grouped by size into tiles of
-// G = 8192 / L lines; four-step transforms as P1 tiles and, `lag` items
-// later, their P2 tiles; single-pass tiles are spread evenly in between.
+// Padded size and output window of a convolution (the rule of
+// tcfft_conv2d_plan: the smallest power of two without wrap-around inside
+// the output window).
+bool conv_geometry(const tcfftBatchConv& d, BatchConv& cv) {
+  long long need;
+  cv.flip = 0;
+  if (d.mode == TCFFT_CONV_VALID_CORR) {
+    if (d.fy > d.sy || d.fx > d.sx) return false;
+    need = std::max(d.sy, d.sx);
+    cv.oy = d.sy - d.fy + 1;
+    cv.ox = d.sx - d.fx + 1;
+    cv.r0 = d.fy - 1;
+    cv.c0 = d.fx - 1;
+    cv.flip = 1;
+  } else if (d.mode == TCFFT_CONV_SAME) {
+    if (d.fy % 2 == 0 || d.fx % 2 == 0) return false;
+    need = std::max(d.sy + (d.fy - 1) / 2, d.sx + (d.fx - 1) / 2);
+    cv.oy = d.sy;
+    cv.ox = d.sx;
+    cv.r0 = (d.fy - 1) / 2;
+    cv.c0 = (d.fx - 1) / 2;
+  } else if (d.mode == TCFFT_CONV_FULL) {
+    need = std::max(d.sy + d.fy - 1, d.sx + d.fx - 1);
+    cv.oy = d.sy + d.fy - 1;
+    cv.ox = d.sx + d.fx - 1;
+    cv.r0 = 0;
+    cv.c0 = 0;
+  } else {
+    return false;
+  }
+  int l = kBatchMinConvLog;
+  while ((1ll << l) < need) ++l;
+  if (l > kBatchMaxConvLog) return false;
+  cv.logP = l;
+  cv.sy = d.sy;
+  cv.sx = d.sx;
+  cv.fy = d.fy;
+  cv.fx = d.fx;
+  return true;
+}
+
+BatchItem make_item(int kind, int logl, int line0, int obj, float scale) {
+  BatchItem it{};
+  it.kind = kind;
+  it.logl = logl;
+  it.line0 = line0;
+  it.obj = obj;
+  it.scale = scale;
+  it.wait_ctr = -1;
+  it.signal_ctr = -1;
+  return it;
+}
+
+// Tiles of one pass over `lines` lines of length 2^logl.
+void add_tiles(std::vector<BatchItem>& v, int kind, int logl, int lines, int obj, float scale, int wait_ctr,
+               int wait_target, int signal_ctr) {
+  const int g = kBatchMt * 16 >> logl;
+  for (int t = 0; t * g < lines; ++t) {
+    BatchItem it = make_item(kind, logl, t * g, obj, scale);
+    it.wait_ctr = wait_ctr;
+    it.wait_target = wait_target;
+    it.signal_ctr = signal_ctr;
+    v.push_back(it);
+  }
+}
+
+int tiles_of(int logl, int lines) {
+  const int g = kBatchMt * 16 >> logl;
+  return (lines + g - 1) / g;
+}
+
+// Work list: single-pass 1D transforms grouped by size into tiles of
+// G = 8192 / L lines; every multi-stage job (four-step transform,
+// convolution) emits its first stage, then each later stage `lag` items after
+// the stage before; single-pass tiles are spread evenly in between.
 Built build_items(const tcfftBatchImpl& b, int lag) {
   Built out;
+  out.nctrs = 1;  // [0] is the queue head
   std::vector<BatchItem> line_items;
   for (int logl = kBatchMinLineLog; logl <= kBatchMaxLineLog; ++logl) {
     const int G = kBatchMt * 16 >> logl;
@@ -143,12 +233,8 @@ Built build_items(const tcfftBatchImpl& b, int lag) {
           end = j;
           break;
         }
-      BatchItem it{};
-      it.kind = kItemLines;
-      it.logl = logl;
-      it.line0 = static_cast<int>(out.line_in.size());
+      BatchItem it = make_item(kItemLines, logl, static_cast<int>(out.line_in.size()), 0, b.scale[ids[k]]);
       it.nlines = static_cast<int>(end - k);
-      it.scale = b.scale[ids[k]];
       for (size_t j = k; j < end; ++j) {
         out.line_in.push_back(b.in_off[ids[j]]);
         out.line_out.push_back(b.out_off[ids[j]]);
@@ -157,11 +243,8 @@ Built build_items(const tcfftBatchImpl& b, int lag) {
       k = end;
     }
   }
-  // four-step transforms
-  struct Four {
-    std::vector<BatchItem> p1, p2;
-  };
-  std::vector<Four> fours;
+  using Stages = std::vector<std::vector<BatchItem>>;
+  std::vector<Stages> jobs;
   for (int i = 0; i < b.count; ++i) {
     const int logn = ilog2_exact(b.n[i]);
     if (logn <= kBatchMaxLineLog) continue;
@@ -173,54 +256,77 @@ Built build_items(const tcfftBatchImpl& b, int lag) {
     xf.log_n1 = batch_log_n1(logn);
     xf.log_n2 = logn - xf.log_n1;
     out.ws_elems += static_cast<size_t>(b.n[i]);
-    const int g1 = kBatchMt * 16 >> xf.log_n1, g2 = kBatchMt * 16 >> xf.log_n2;
-    const int lines1 = 1 << xf.log_n2, lines2 = 1 << xf.log_n1;
-    xf.tiles1 = (lines1 + g1 - 1) / g1;
-    Four f;
-    for (int t = 0; t < xf.tiles1; ++t) {
-      BatchItem it{};
-      it.kind = kItemP1;
-      it.logl = xf.log_n1;
-      it.line0 = t * g1;
-      it.xform = static_cast<int>(out.xforms.size());
-      it.scale = 1.0f;
-      f.p1.push_back(it);
-    }
-    for (int t = 0; t < (lines2 + g2 - 1) / g2; ++t) {
-      BatchItem it{};
-      it.kind = kItemP2;
-      it.logl = xf.log_n2;
-      it.line0 = t * g2;
-      it.xform = static_cast<int>(out.xforms.size());
-      it.scale = b.scale[i];
-      f.p2.push_back(it);
-    }
+    xf.tiles1 = tiles_of(xf.log_n1, 1 << xf.log_n2);
+    const int obj = static_cast<int>(out.xforms.size());
+    const int ctr = out.nctrs++;
+    Stages st(2);
+    add_tiles(st[0], kItemP1, xf.log_n1, 1 << xf.log_n2, obj, 1.0f, -1, 0, ctr);
+    add_tiles(st[1], kItemP2, xf.log_n2, 1 << xf.log_n1, obj, b.scale[i], ctr, xf.tiles1, -1);
     out.xforms.push_back(xf);
-    fours.push_back(std::move(f));
+    jobs.push_back(std::move(st));
   }
-  // merge: P1 of each four-step transform, its P2 `lag` items later, single
-  // pass tiles spread evenly in between
+  for (size_t c = 0; c < b.conv_desc.size(); ++c) {
+    const tcfftBatchConv& d = b.conv_desc[c];
+    BatchConv cv{};
+    conv_geometry(d, cv);  // validated at plan entry
+    const int P = 1 << cv.logP;
+    const long long rows = std::max({cv.sy, cv.oy, cv.fy});
+    cv.img_off = d.img_off;
+    cv.out_off = d.out_off;
+    cv.filt_off = d.filt_off;
+    cv.x_off = static_cast<long long>(out.ws_elems);
+    out.ws_elems += static_cast<size_t>(rows) * P;
+    cv.y_off = static_cast<long long>(out.ws_elems);
+    out.ws_elems += static_cast<size_t>(P) * P;
+    cv.k_off = static_cast<long long>(out.kspec_elems);
+    out.kspec_elems += static_cast<size_t>(P) * P;
+    const int obj = static_cast<int>(out.convs.size());
+    const float inv_p = 1.0f / static_cast<float>(P);
+    // filter spectrum (separate launch at plan time)
+    const int fc = out.nctrs++;
+    add_tiles(out.prep_items, kItemFiltRow, cv.logP, cv.fy, obj, 1.0f, -1, 0, fc);
+    add_tiles(out.prep_items, kItemFiltCol, cv.logP, P, obj, 1.0f, fc, tiles_of(cv.logP, cv.fy), -1);
+    // the convolution
+    const int c1 = out.nctrs++, c2 = out.nctrs++, c3 = out.nctrs++;
+    Stages st(4);
+    add_tiles(st[0], kItemConvRow, cv.logP, cv.sy, obj, inv_p, -1, 0, c1);
+    add_tiles(st[1], kItemConvCol, cv.logP, P, obj, inv_p, c1, tiles_of(cv.logP, cv.sy), c2);
+    add_tiles(st[2], kItemConvInv, cv.logP, P, obj, 1.0f, c2, tiles_of(cv.logP, P), c3);
+    add_tiles(st[3], kItemConvOut, cv.logP, cv.oy, obj, 1.0f, c3, tiles_of(cv.logP, P), -1);
+    out.convs.push_back(cv);
+    jobs.push_back(std::move(st));
+  }
+  // merge
   size_t total = line_items.size();
-  for (const Four& f : fours) total += f.p1.size() + f.p2.size();
+  for (const Stages& j : jobs)
+    for (const auto& g : j) total += g.size();
   out.items.reserve(total);
-  std::deque<std::pair<size_t, const std::vector<BatchItem>*>> pending;
-  size_t li = 0;
-  const double per_four = fours.empty() ? 0.0 : static_cast<double>(line_items.size()) / fours.size();
-  double line_credit = 0.0;
+  struct Pending {
+    size_t ready;
+    size_t job, stage;
+  };
+  std::deque<Pending> pending;  // ready positions are nondecreasing
+  auto emit_stage = [&](size_t job, size_t stage) {
+    for (const BatchItem& it : jobs[job][stage]) out.items.push_back(it);
+    if (stage + 1 < jobs[job].size()) pending.push_back({out.items.size() + static_cast<size_t>(lag), job, stage + 1});
+  };
   auto release = [&](bool all) {
-    while (!pending.empty() && (all || pending.front().first <= out.items.size())) {
-      for (const BatchItem& it : *pending.front().second) out.items.push_back(it);
+    while (!pending.empty() && (all || pending.front().ready <= out.items.size())) {
+      const Pending p = pending.front();
       pending.pop_front();
+      emit_stage(p.job, p.stage);
     }
   };
-  for (const Four& f : fours) {
+  size_t li = 0;
+  const double per_job = jobs.empty() ? 0.0 : static_cast<double>(line_items.size()) / jobs.size();
+  double credit = 0.0;
+  for (size_t j = 0; j < jobs.size(); ++j) {
     release(false);
-    for (const BatchItem& it : f.p1) out.items.push_back(it);
-    pending.emplace_back(out.items.size() + static_cast<size_t>(lag), &f.p2);
-    line_credit += per_four;
-    while (line_credit >= 1.0 && li < line_items.size()) {
+    emit_stage(j, 0);
+    credit += per_job;
+    while (credit >= 1.0 && li < line_items.size()) {
       out.items.push_back(line_items[li++]);
-      line_credit -= 1.0;
+      credit -= 1.0;
       release(false);
     }
   }
@@ -228,7 +334,7 @@ Built build_items(const tcfftBatchImpl& b, int lag) {
     out.items.push_back(line_items[li++]);
     release(false);
   }
-  release(true);
+  while (!pending.empty()) release(true);
   return out;
 }
 
@@ -240,7 +346,10 @@ void free_batch(tcfftBatchImpl* b) {
   if (!b) return;
   if (b->graph) cudaGraphExecDestroy(b->graph);
   for (auto& kv : b->plans) tcfft_destroy(kv.second);
+  for (auto& kv : b->conv_plans) tcfft_conv2d_destroy(kv.second);
   cudaFree(b->ws);
+  cudaFree(b->kspec);
+  cudaFree(b->filters);
   cudaFree(b->arena);
   cudaFree(b->ctr);
   cudaFree(b->err);
@@ -256,11 +365,13 @@ tcfftStatus build_persistent(tcfftBatchImpl* b) {
   Built bl = build_items(*b, lag);
   b->nitems = static_cast<int>(bl.items.size());
   b->nxforms = static_cast<int>(bl.xforms.size());
+  b->nctrs = bl.nctrs;
   b->ctas = g_bk_ctas[pr][b->sign_idx];
   const int sign = b->sign_idx == 0 ? -1 : 1;
   // which tables are needed
   bool need_tw[kBatchMaxLineLog + 1] = {}, need_otw[kBatchMaxLog + 1] = {};
   for (const BatchItem& it : bl.items) need_tw[it.logl] = true;
+  for (const BatchItem& it : bl.prep_items) need_tw[it.logl] = true;
   for (const BatchXform& xf : bl.xforms) need_otw[xf.logn] = true;
   // arena layout (256-byte aligned pieces)
   size_t at = 0;
@@ -290,13 +401,19 @@ tcfftStatus build_persistent(tcfftBatchImpl* b) {
   at = align_up(at + sizeof(BatchItem) * bl.items.size(), 256);
   const size_t off_xf = at;
   at = align_up(at + sizeof(BatchXform) * bl.xforms.size(), 256);
+  const size_t off_conv = at;
+  at = align_up(at + sizeof(BatchConv) * bl.convs.size(), 256);
+  const size_t off_prep = at;
+  at = align_up(at + sizeof(BatchItem) * bl.prep_items.size(), 256);
   if (cudaMalloc(&b->arena, at) != cudaSuccess) return TCFFT_ALLOC_FAILED;
-  if (cudaMalloc(&b->ctr, sizeof(int) * (1 + static_cast<size_t>(b->nxforms))) != cudaSuccess ||
+  if (cudaMalloc(&b->ctr, sizeof(int) * static_cast<size_t>(b->nctrs)) != cudaSuccess ||
       cudaMalloc(&b->err, sizeof(int)) != cudaSuccess)
     return TCFFT_ALLOC_FAILED;
   if (cudaMemset(b->err, 0, sizeof(int)) != cudaSuccess) return TCFFT_LAUNCH_FAILED;
   b->ws_bytes = bl.ws_elems * b->elem_bytes;
   if (b->ws_bytes && cudaMalloc(&b->ws, b->ws_bytes) != cudaSuccess) return TCFFT_ALLOC_FAILED;
+  const size_t kspec_bytes = bl.kspec_elems * b->elem_bytes;
+  if (kspec_bytes && cudaMalloc(&b->kspec, kspec_bytes) != cudaSuccess) return TCFFT_ALLOC_FAILED;
   unsigned char* A = static_cast<unsigned char*>(b->arena);
   // FP64-generated tables, rounded once
   cudaError_t e = gen_dft16_bmat(reinterpret_cast<uint16_t*>(A + off_bmat), sign, 0, 0);
@@ -320,6 +437,8 @@ tcfftStatus build_persistent(tcfftBatchImpl* b) {
   put(off_lout, bl.line_out.data(), sizeof(long long) * bl.line_out.size());
   put(off_items, bl.items.data(), sizeof(BatchItem) * bl.items.size());
   put(off_xf, bl.xforms.data(), sizeof(BatchXform) * bl.xforms.size());
+  put(off_conv, bl.convs.data(), sizeof(BatchConv) * bl.convs.size());
+  put(off_prep, bl.prep_items.data(), sizeof(BatchItem) * bl.prep_items.size());
   if (cudaMemcpy(A + host_begin, host.data(), host.size(), cudaMemcpyHostToDevice) != cudaSuccess)
     return TCFFT_LAUNCH_FAILED;
   BatchArgs& a = b->args;
@@ -330,8 +449,11 @@ tcfftStatus build_persistent(tcfftBatchImpl* b) {
   a.items = reinterpret_cast<const BatchItem*>(A + off_items);
   a.nitems = b->nitems;
   a.xforms = reinterpret_cast<const BatchXform*>(A + off_xf);
+  a.convs = reinterpret_cast<const BatchConv*>(A + off_conv);
+  a.kspec = b->kspec;
+  a.filters = b->filters;
   a.counter = reinterpret_cast<unsigned int*>(b->ctr);
-  a.done = b->ctr + 1;
+  a.ctrs = b->ctr;
   for (int l = 0; l <= kBatchMaxLineLog; ++l)
     if (need_tw[l]) a.tw[l] = reinterpret_cast<const float2*>(A + off_tw[l]);
   for (int l = 0; l <= kBatchMaxLog; ++l)
@@ -343,7 +465,23 @@ tcfftStatus build_persistent(tcfftBatchImpl* b) {
     }
   a.bmat = reinterpret_cast<const uint32_t*>(A + off_bmat);
   a.err = b->err;
-  return cudaDeviceSynchronize() == cudaSuccess ? TCFFT_OK : TCFFT_LAUNCH_FAILED;
+  if (!bl.prep_items.empty()) {
+    // filter spectra: the same kernel over the filter items, once
+    BatchArgs pa = a;
+    pa.items = reinterpret_cast<const BatchItem*>(A + off_prep);
+    pa.nitems = static_cast<int>(bl.prep_items.size());
+    if (cudaMemset(b->ctr, 0, sizeof(int) * static_cast<size_t>(b->nctrs)) != cudaSuccess)
+      return TCFFT_LAUNCH_FAILED;
+    const int grid = std::min(b->ctas, pa.nitems);
+    void* params[] = {&pa};
+    if (cudaLaunchKernel(g_bk[pr][0].fn, dim3(static_cast<unsigned>(grid)), dim3(kPassThreads), params,
+                         static_cast<size_t>(g_bk[pr][0].smem), nullptr) != cudaSuccess)
+      return TCFFT_LAUNCH_FAILED;
+  }
+  if (cudaDeviceSynchronize() != cudaSuccess) return TCFFT_LAUNCH_FAILED;
+  int flag = 0;
+  if (cudaMemcpy(&flag, b->err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return TCFFT_LAUNCH_FAILED;
+  return flag ? TCFFT_TIMEOUT : TCFFT_OK;
 }
 
 // Runs of adjacent same-size, same-scale transforms for the plain path, and
@@ -369,14 +507,16 @@ tcfftStatus build_per_size(tcfftBatchImpl* b) {
   return TCFFT_OK;
 }
 
-tcfftStatus launch_persistent(tcfftBatchImpl* b, const void* in, void* out, cudaStream_t st, int* launches) {
+tcfftStatus launch_persistent(tcfftBatchImpl* b, const Buffers& io, cudaStream_t st, int* launches) {
   const int pr = b->precision == TCFFT_FP16 ? 0 : 1;
-  if (cudaMemsetAsync(b->ctr, 0, sizeof(int) * (1 + static_cast<size_t>(b->nxforms)), st) != cudaSuccess)
+  if (cudaMemsetAsync(b->ctr, 0, sizeof(int) * static_cast<size_t>(b->nctrs), st) != cudaSuccess)
     return TCFFT_LAUNCH_FAILED;
   if (b->nitems == 0) return TCFFT_OK;
   BatchArgs a = b->args;
-  a.in = in;
-  a.out = out;
+  a.in = io.in;
+  a.out = io.out;
+  a.conv_in = io.conv_in;
+  a.conv_out = io.conv_out;
   const int grid = std::min(b->ctas, b->nitems);
   void* params[] = {&a};
   if (cudaLaunchKernel(g_bk[pr][b->sign_idx].fn, dim3(static_cast<unsigned>(grid)), dim3(kPassThreads), params,
@@ -386,40 +526,121 @@ tcfftStatus launch_persistent(tcfftBatchImpl* b, const void* in, void* out, cuda
   return TCFFT_OK;
 }
 
-tcfftStatus launch_per_size(tcfftBatchImpl* b, const void* in, void* out, cudaStream_t st, int* launches) {
+// Plain path: one tcfft_exec per run of adjacent same-size transforms and one
+// convolution plan (filters resident) per convolution, as a caller of the
+// per-size API would write it.
+tcfftStatus launch_per_size(tcfftBatchImpl* b, const Buffers& io, cudaStream_t st, int* launches) {
   const int direction = b->sign_idx == 0 ? TCFFT_FORWARD : TCFFT_INVERSE;
   for (const tcfftBatchImpl::Run& r : b->runs) {
     tcfftPlan p = b->plans[std::make_pair(r.logn, r.len)];
-    const unsigned char* src = static_cast<const unsigned char*>(in) + b->in_off[r.first] * b->elem_bytes;
-    unsigned char* dst = static_cast<unsigned char*>(out) + b->out_off[r.first] * b->elem_bytes;
+    const unsigned char* src = static_cast<const unsigned char*>(io.in) + b->in_off[r.first] * b->elem_bytes;
+    unsigned char* dst = static_cast<unsigned char*>(io.out) + b->out_off[r.first] * b->elem_bytes;
     const tcfftStatus s = tcfft_exec(p, src, dst, direction, b->scale[r.first], st);
     if (s != TCFFT_OK) return s;
     *launches += tcfft_last_launch_count();
   }
+  const size_t rb = b->precision == TCFFT_FP16 ? 2 : 4;  // bytes per real element
+  for (size_t c = 0; c < b->conv_desc.size(); ++c) {
+    const tcfftBatchConv& d = b->conv_desc[c];
+    const auto itp = b->conv_plans.find(static_cast<int>(c));
+    if (itp == b->conv_plans.end()) return TCFFT_INVALID_VALUE;  // made by tcfft_batch_set_mode
+    const unsigned char* src = static_cast<const unsigned char*>(io.conv_in) + d.img_off * rb;
+    unsigned char* dst = static_cast<unsigned char*>(io.conv_out) + d.out_off * rb;
+    const tcfftStatus s = tcfft_conv2d_exec(itp->second, src, dst, 1, st);
+    if (s != TCFFT_OK) return s;
+    *launches += 5;  // row, column, pointwise, column, row
+  }
   return TCFFT_OK;
 }
 
-tcfftStatus launch_all(tcfftBatchImpl* b, const void* in, void* out, cudaStream_t st, int* launches) {
-  return b->mode == TCFFT_BATCH_PERSISTENT ? launch_persistent(b, in, out, st, launches)
-                                           : launch_per_size(b, in, out, st, launches);
+tcfftStatus launch_all(tcfftBatchImpl* b, const Buffers& io, cudaStream_t st, int* launches) {
+  return b->mode == TCFFT_BATCH_PERSISTENT ? launch_persistent(b, io, st, launches)
+                                           : launch_per_size(b, io, st, launches);
+}
+
+// Plain-path convolution plans, one per convolution with its filter resident
+// (made before any capture: plan creation allocates).
+tcfftStatus make_conv_plans(tcfftBatchImpl* b) {
+  for (size_t c = 0; c < b->conv_desc.size(); ++c) {
+    if (b->conv_plans.count(static_cast<int>(c))) continue;
+    const tcfftBatchConv& d = b->conv_desc[c];
+    tcfftConv cp = nullptr;
+    tcfftStatus s = tcfft_conv2d_plan(&cp, 1, 1, d.sy, d.sx, d.fy, d.fx, d.mode, b->precision, 1);
+    if (s == TCFFT_OK) s = tcfft_conv2d_set_filters(cp, b->filters + d.filt_off, nullptr);
+    if (s == TCFFT_OK) s = tcfft_conv2d_check(cp, nullptr);
+    if (s != TCFFT_OK) {
+      if (cp) tcfft_conv2d_destroy(cp);
+      return s;
+    }
+    b->conv_plans.emplace(static_cast<int>(c), cp);
+  }
+  return TCFFT_OK;
+}
+
+tcfftStatus exec_buffers(tcfftBatchImpl* b, const Buffers& io, cudaStream_t st) {
+  int launches = 0;
+  if (!b->use_graph) {
+    const tcfftStatus s = launch_all(b, io, st, &launches);
+    return record_status(s, launches);
+  }
+  if (!b->graph || !(b->graph_io == io) || b->graph_mode != b->mode) {
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    cudaStream_t cap = nullptr;
+    if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess)
+      return record_status(TCFFT_LAUNCH_FAILED, 0);
+    tcfftStatus s = TCFFT_OK;
+    if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) s = TCFFT_LAUNCH_FAILED;
+    int captured = 0;
+    if (s == TCFFT_OK) s = launch_all(b, io, cap, &captured);
+    cudaGraph_t g = nullptr;
+    const cudaError_t end = cudaStreamEndCapture(cap, &g);
+    if (s == TCFFT_OK && (end != cudaSuccess || !g)) s = TCFFT_LAUNCH_FAILED;
+    if (s == TCFFT_OK && cudaGraphInstantiate(&b->graph, g, 0) != cudaSuccess) {
+      b->graph = nullptr;
+      s = TCFFT_LAUNCH_FAILED;
+    }
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(cap);
+    if (s != TCFFT_OK) return record_status(s, 0);
+    b->graph_io = io;
+    b->graph_mode = b->mode;
+    b->graph_launches = captured;
+  }
+  if (cudaGraphLaunch(b->graph, st) != cudaSuccess) return record_status(TCFFT_LAUNCH_FAILED, 0);
+  return record_status(TCFFT_OK, b->graph_launches);
 }
 
 }  // namespace
 
 extern "C" {
 
-tcfftStatus tcfft_batch_plan(tcfftBatch* batch, int count, const long long* n, const long long* in_off,
-                             const long long* out_off, const float* scale, int precision, int direction) {
+tcfftStatus tcfft_batch_plan_mixed(tcfftBatch* batch, int count, const long long* n, const long long* in_off,
+                                   const long long* out_off, const float* scale, int nconv,
+                                   const tcfftBatchConv* convs, const float* filters, long long filter_floats,
+                                   int precision, int direction) {
   if (!batch) return record_status(TCFFT_INVALID_VALUE, 0);
   *batch = nullptr;
-  if (count < 1 || !n || !in_off || !out_off) return record_status(TCFFT_INVALID_VALUE, 0);
+  if (count < 0 || nconv < 0 || count + nconv < 1) return record_status(TCFFT_INVALID_VALUE, 0);
+  if (count > 0 && (!n || !in_off || !out_off)) return record_status(TCFFT_INVALID_VALUE, 0);
+  if (nconv > 0 && (!convs || !filters || filter_floats < 1)) return record_status(TCFFT_INVALID_VALUE, 0);
   if (precision != TCFFT_FP16 && precision != TCFFT_SPLIT_FP32) return record_status(TCFFT_INVALID_VALUE, 0);
   if (direction != TCFFT_FORWARD && direction != TCFFT_INVERSE) return record_status(TCFFT_INVALID_VALUE, 0);
+  // convolutions run as forward transforms only; their plan is forward
+  if (nconv > 0 && direction != TCFFT_FORWARD) return record_status(TCFFT_INVALID_VALUE, 0);
   const long long align_elems = precision == TCFFT_FP16 ? 4 : 2;  // 16 bytes
   for (int i = 0; i < count; ++i) {
     const int l = ilog2_exact(n[i]);
     if (l < kMinLog || l > kMaxLog) return record_status(TCFFT_INVALID_SIZE, 0);
     if (in_off[i] < 0 || out_off[i] < 0 || in_off[i] % align_elems || out_off[i] % align_elems)
+      return record_status(TCFFT_INVALID_VALUE, 0);
+  }
+  for (int c = 0; c < nconv; ++c) {
+    const tcfftBatchConv& d = convs[c];
+    BatchConv cv{};
+    if (d.sy < 1 || d.sx < 1 || d.fy < 1 || d.fx < 1 || !conv_geometry(d, cv)) return record_status(TCFFT_INVALID_SIZE, 0);
+    if (d.img_off < 0 || d.out_off < 0 || d.filt_off < 0 ||
+        d.filt_off + static_cast<long long>(d.fy) * d.fx > filter_floats)
       return record_status(TCFFT_INVALID_VALUE, 0);
   }
   tcfftStatus s = registry_ready();
@@ -432,12 +653,23 @@ tcfftStatus tcfft_batch_plan(tcfftBatch* batch, int count, const long long* n, c
   b->sign_idx = direction == TCFFT_FORWARD ? 0 : 1;
   b->count = count;
   b->elem_bytes = precision == TCFFT_FP16 ? 4 : 8;
-  b->n.assign(n, n + count);
-  b->in_off.assign(in_off, in_off + count);
-  b->out_off.assign(out_off, out_off + count);
-  b->scale.assign(static_cast<size_t>(count), 1.0f);
-  if (scale) b->scale.assign(scale, scale + count);
-  s = build_persistent(b);
+  if (count > 0) {
+    b->n.assign(n, n + count);
+    b->in_off.assign(in_off, in_off + count);
+    b->out_off.assign(out_off, out_off + count);
+    b->scale.assign(static_cast<size_t>(count), 1.0f);
+    if (scale) b->scale.assign(scale, scale + count);
+  }
+  if (nconv > 0) {
+    b->conv_desc.assign(convs, convs + nconv);
+    // plan-owned copy of the filters: the spectra are made now, the plain
+    // path's per-convolution plans later
+    if (cudaMalloc(&b->filters, sizeof(float) * static_cast<size_t>(filter_floats)) != cudaSuccess ||
+        cudaMemcpy(b->filters, filters, sizeof(float) * static_cast<size_t>(filter_floats),
+                   cudaMemcpyDefault) != cudaSuccess)
+      s = TCFFT_ALLOC_FAILED;
+  }
+  if (s == TCFFT_OK) s = build_persistent(b);
   if (s == TCFFT_OK) s = build_per_size(b);
   if (s != TCFFT_OK) {
     free_batch(b);
@@ -447,9 +679,23 @@ tcfftStatus tcfft_batch_plan(tcfftBatch* batch, int count, const long long* n, c
   return record_status(TCFFT_OK, 0);
 }
 
+tcfftStatus tcfft_batch_plan(tcfftBatch* batch, int count, const long long* n, const long long* in_off,
+                             const long long* out_off, const float* scale, int precision, int direction) {
+  if (count < 1) {
+    if (batch) *batch = nullptr;
+    return record_status(TCFFT_INVALID_VALUE, 0);
+  }
+  return tcfft_batch_plan_mixed(batch, count, n, in_off, out_off, scale, 0, nullptr, nullptr, 0, precision,
+                                direction);
+}
+
 tcfftStatus tcfft_batch_set_mode(tcfftBatch b, int mode) {
   if (!b || (mode != TCFFT_BATCH_PERSISTENT && mode != TCFFT_BATCH_PER_SIZE))
     return record_status(TCFFT_INVALID_VALUE, 0);
+  if (mode == TCFFT_BATCH_PER_SIZE) {
+    const tcfftStatus s = make_conv_plans(b);
+    if (s != TCFFT_OK) return record_status(s, 0);
+  }
   b->mode = mode;
   return record_status(TCFFT_OK, 0);
 }
@@ -460,43 +706,20 @@ tcfftStatus tcfft_batch_set_graph(tcfftBatch b, int enable) {
   return record_status(TCFFT_OK, 0);
 }
 
-tcfftStatus tcfft_batch_exec(tcfftBatch b, const void* in, void* out, void* stream) {
-  if (!b || !in || !out) return record_status(TCFFT_INVALID_VALUE, 0);
+tcfftStatus tcfft_batch_exec_mixed(tcfftBatch b, const void* in, void* out, const void* conv_in, void* conv_out,
+                                   void* stream) {
+  if (!b) return record_status(TCFFT_INVALID_VALUE, 0);
+  if (b->count > 0 && (!in || !out)) return record_status(TCFFT_INVALID_VALUE, 0);
+  if (!b->conv_desc.empty() && (!conv_in || !conv_out)) return record_status(TCFFT_INVALID_VALUE, 0);
   if ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u)
     return record_status(TCFFT_INVALID_VALUE, 0);
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  int launches = 0;
-  if (!b->use_graph) {
-    const tcfftStatus s = launch_all(b, in, out, st, &launches);
-    return record_status(s, launches);
-  }
-  if (!b->graph || b->graph_in != in || b->graph_out != out || b->graph_mode != b->mode) {
-    if (b->graph) cudaGraphExecDestroy(b->graph);
-    b->graph = nullptr;
-    cudaStream_t cap = nullptr;
-    if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess)
-      return record_status(TCFFT_LAUNCH_FAILED, 0);
-    tcfftStatus s = TCFFT_OK;
-    if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) s = TCFFT_LAUNCH_FAILED;
-    int captured = 0;
-    if (s == TCFFT_OK) s = launch_all(b, in, out, cap, &captured);
-    cudaGraph_t g = nullptr;
-    const cudaError_t end = cudaStreamEndCapture(cap, &g);
-    if (s == TCFFT_OK && (end != cudaSuccess || !g)) s = TCFFT_LAUNCH_FAILED;
-    if (s == TCFFT_OK && cudaGraphInstantiate(&b->graph, g, 0) != cudaSuccess) {
-      b->graph = nullptr;
-      s = TCFFT_LAUNCH_FAILED;
-    }
-    if (g) cudaGraphDestroy(g);
-    cudaStreamDestroy(cap);
-    if (s != TCFFT_OK) return record_status(s, 0);
-    b->graph_in = in;
-    b->graph_out = out;
-    b->graph_mode = b->mode;
-    b->graph_launches = captured;
-  }
-  if (cudaGraphLaunch(b->graph, st) != cudaSuccess) return record_status(TCFFT_LAUNCH_FAILED, 0);
-  return record_status(TCFFT_OK, b->graph_launches);
+  return exec_buffers(b, Buffers{in, out, conv_in, conv_out}, static_cast<cudaStream_t>(stream));
+}
+
+tcfftStatus tcfft_batch_exec(tcfftBatch b, const void* in, void* out, void* stream) {
+  if (!b || !in || !out) return record_status(TCFFT_INVALID_VALUE, 0);
+  if (!b->conv_desc.empty()) return record_status(TCFFT_INVALID_VALUE, 0);
+  return tcfft_batch_exec_mixed(b, in, out, nullptr, nullptr, stream);
 }
 
 tcfftStatus tcfft_batch_info(tcfftBatch b, int* items, size_t* workspace_bytes, int* ctas) {
@@ -517,6 +740,10 @@ tcfftStatus tcfft_batch_check(tcfftBatch b, void* stream) {
     return record_status(TCFFT_LAUNCH_FAILED, 0);
   for (auto& kv : b->plans) {
     const tcfftStatus s = tcfft_check(kv.second, stream);
+    if (s != TCFFT_OK) return record_status(s, 0);
+  }
+  for (auto& kv : b->conv_plans) {
+    const tcfftStatus s = tcfft_conv2d_check(kv.second, stream);
     if (s != TCFFT_OK) return record_status(s, 0);
   }
   if (flag & (kErrMmaTimeout | kErrQueueTimeout)) return record_status(TCFFT_TIMEOUT, 0);

@@ -1,9 +1,9 @@
-// Persistent batch kernel: 1D transforms of uneven sizes in one launch, fed
-// from a device-side work queue.
+// Persistent batch kernel: 1D transforms and 2D convolutions of uneven sizes
+// in one launch, fed from a device-side work queue.
 //
 // The caller's transforms sit anywhere in one input and one output buffer
-// (element offsets per transform). The host plan sorts them by size and
-// writes a list of work items (tiles):
+// (element offsets per transform); convolutions read real images from a
+// second pair of buffers. The host plan writes a list of work items (tiles):
 //   kItemLines : up to G = 8192 / L whole transforms of one size L <= 2^13,
 //                single pass; transform offsets come from the line tables
 //   kItemP1    : a column-pass tile of one larger transform (four-step pass
@@ -11,13 +11,15 @@
 //                workspace)
 //   kItemP2    : a transposing row-pass tile of the same transform (pass 2:
 //                lines of length n2, workspace -> output)
-// CTAs take items with one atomic counter, in list order. A P2 item waits
-// (bounded) until the transform's counter shows all of its P1 tiles done;
-// every P1 tile bumps that counter after a device-scope fence. The host puts
-// every P2 item after all P1 items of its transform, so a wait only ever
-// targets items that running CTAs already hold, and the chain of waits ends
-// at an item that waits for nothing: the queue cannot deadlock, whether or
-// not every CTA of the grid is resident at once.
+//   kItemConv* : the four stages of a convolution (see BatchConv)
+// CTAs take items with one atomic counter, in list order. An item may wait
+// (bounded) until a dependency counter reaches a target -- a P2 tile for all
+// P1 tiles of its transform, a conv stage for all tiles of the stage before
+// -- and may bump a counter when done, after a device-scope fence. The host
+// puts every item after all items it waits for, so a wait only ever targets
+// items that running CTAs already hold, and the chain of waits ends at an
+// item that waits for nothing: the queue cannot deadlock, whether or not
+// every CTA of the grid is resident at once.
 //
 // All tiles hold 512 rows of the 16-column MMA layout (Mt = 512), FP16 or
 // split precision, so one TMEM allocation and one shared-memory carve-out
@@ -26,30 +28,64 @@
 #include "fft_fused.cuh"
 #include "fft_io.cuh"
 #include "fft_split.cuh"
+#include "conv_io.cuh"
 #include "fft_tile.cuh"
 
 namespace tcfft {
 
-enum : int { kItemLines = 0, kItemP1 = 1, kItemP2 = 2 };
+enum : int {
+  kItemLines = 0,    // single-pass 1D tile
+  kItemP1 = 1,       // four-step pass 1 tile
+  kItemP2 = 2,       // four-step pass 2 tile
+  kItemConvRow = 3,  // conv: forward FFT of real rows (zero-padded to P)
+  kItemConvCol = 4,  // conv: forward FFT of columns, times the filter spectrum
+  kItemConvInv = 5,  // conv: second column FFT, rows of the output window kept
+  kItemConvOut = 6,  // conv: row FFT, real part of the output window's columns
+  kItemFiltRow = 7,  // filter spectrum: forward FFT of the (flipped) filter's rows
+  kItemFiltCol = 8,  // filter spectrum: forward FFT of columns -> K
+};
 
 constexpr int kBatchMt = 512;
 constexpr int kBatchMinLineLog = 6, kBatchMaxLineLog = 13;  // single-pass sizes
 constexpr int kBatchMinPassLog = 7, kBatchMaxPassLog = 10;  // four-step pass lengths
 constexpr int kBatchMaxLog = 2 * kBatchMaxPassLog;          // largest transform
+constexpr int kBatchMinConvLog = 6, kBatchMaxConvLog = 11;  // padded conv sizes P
 
 struct BatchItem {
   int kind;
-  int logl;          // pass length of this tile
-  int line0;         // kItemLines: first entry of the line tables; P1/P2: first line in the pass
-  int nlines;        // kItemLines: transforms in this tile
-  int xform;         // P1 / P2: transform index
-  float scale;       // applied on the final store
-  int pad0, pad1;
+  int logl;         // pass length of this tile
+  int line0;        // kItemLines: first entry of the line tables; others: first line in the pass
+  int nlines;       // kItemLines: transforms in this tile
+  int obj;          // transform (P1 / P2) or convolution (conv items) index
+  float scale;      // applied on the tile's store
+  int wait_ctr;     // counter to wait for before starting (-1: none) ...
+  int wait_target;  // ... until it reaches this value
+  int signal_ctr;   // counter bumped when the tile is done (-1: none)
+  int pad;
 };
 
 struct BatchXform {
   long long in_off, out_off, ws_off;  // element offsets
   int logn, log_n1, log_n2, tiles1;   // tiles1: P1 tiles of this transform
+};
+
+// One 2D convolution of a real sy x sx image with a resident filter spectrum
+// K (P x P, unnormalised DFT of the zero-padded, possibly flipped filter).
+// Stages: rows -> X (sy x P, scale 1/P); columns of X -> Y = conj(Xf * K)
+// (P x P, scale 1/P); columns of Y -> Z (the oy output rows, P wide);
+// rows of Z -> out (real part of columns [c0, c0 + ox)). Since
+// IDFT(y) = conj(DFT(conj(y))), storing conj(Xf * K) lets both inverse
+// stages run as forward transforms, and Re(conj z) = Re(z) makes the final
+// conjugation vanish. Z reuses X's space (X is dead once all column tiles of
+// stage 2 are done, which stage 3 waits for).
+// K itself comes from kItemFiltRow / kItemFiltCol tiles (the same passes on
+// the fy x fx float filter, scale 1, rows into X's space, columns into K).
+struct BatchConv {
+  long long img_off, out_off;  // real elements in the conv input / output buffers
+  long long x_off, y_off;      // elements in the workspace
+  long long k_off;             // elements in the filter-spectrum buffer
+  long long filt_off;          // floats in the filter buffer
+  int sy, sx, oy, ox, r0, c0, logP, flip, fy, fx, pad0, pad1;
 };
 
 struct BatchArgs {
@@ -61,8 +97,13 @@ struct BatchArgs {
   const BatchItem* items;
   int nitems;
   const BatchXform* xforms;
+  const BatchConv* convs;
+  const void* conv_in;   // real images (half for FP16, float for split)
+  void* conv_out;        // real outputs
+  void* kspec;            // filter spectra (E)
+  const float* filters;   // fy x fx float filters (spectrum items)
   unsigned int* counter;  // queue head
-  int* done;              // per transform: P1 tiles finished
+  int* ctrs;              // dependency counters
   const float2* tw[kBatchMaxLineLog + 1];  // W_L, this direction
   OuterTwiddle otw[kBatchMaxLog + 1];      // W_n factor tables per log2 n
   const uint32_t* bmat;                    // DFT16 B image (hi, lo), this direction
@@ -182,7 +223,7 @@ __device__ __noinline__ bool batch_p1_item(typename BatchPrec<SPLIT>::State& st,
                                            const BatchItem& it, const PassCore& core) {
   using P = BatchPrec<SPLIT>;
   using E = typename P::E;
-  const BatchXform xf = a.xforms[it.xform];
+  const BatchXform xf = a.xforms[it.obj];
   const long long n = 1ll << xf.logn, n2 = 1ll << xf.log_n2;
   typename P::template Io<false, false, false> io;
   io.in = static_cast<const E*>(a.in) + xf.in_off;
@@ -204,7 +245,7 @@ __device__ __noinline__ bool batch_p2_item(typename BatchPrec<SPLIT>::State& st,
                                            const BatchItem& it, const PassCore& core) {
   using P = BatchPrec<SPLIT>;
   using E = typename P::E;
-  const BatchXform xf = a.xforms[it.xform];
+  const BatchXform xf = a.xforms[it.obj];
   const long long n = 1ll << xf.logn, n1 = 1ll << xf.log_n1, n2 = 1ll << xf.log_n2;
   typename P::template Io<true, false, true> io;
   io.in = static_cast<const E*>(a.ws) + xf.ws_off;
@@ -221,6 +262,119 @@ __device__ __noinline__ bool batch_p2_item(typename BatchPrec<SPLIT>::State& st,
   io.in_contig = io.out_contig = false;
   io.contig_len = L;
   return P::template tile<L, true, SIGN>(st, io, core, static_cast<long long>(it.line0));
+}
+
+// Stage 2 of a convolution: the column pass of IoColMaskCrop (rows >= sy
+// read as zero) whose store writes conj(scale * v * K) for the full P rows.
+template <class E>
+struct IoColMulConj : IoColMaskCrop<E> {
+  const E* K;  // P x P filter spectrum (row stride P)
+  __device__ __forceinline__ void store_row16(long long line, int j, int J, float2 (&v)[16]) const {
+    const long long col = line & ((1ll << this->lps_log2) - 1);
+    E* p = this->out + col;
+    const E* k = K + col;
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+      const long long off = static_cast<long long>(j + c * J) * this->P;
+      const float2 w = from_elem(k[off]);
+      const float re = (v[c].x * w.x - v[c].y * w.y) * this->scale;
+      const float im = (v[c].x * w.y + v[c].y * w.x) * this->scale;
+      p[off] = to_elem<E>(make_float2(re, -im));
+    }
+  }
+};
+
+template <class T>
+__device__ __forceinline__ T zeroed() {
+  T t;
+  memset(&t, 0, sizeof(T));
+  return t;
+}
+
+template <bool SPLIT, int L>
+__device__ __noinline__ bool batch_conv_item(typename BatchPrec<SPLIT>::State& st, const BatchArgs& a,
+                                             const BatchItem& it, const PassCore& core) {
+  using P = BatchPrec<SPLIT>;
+  using E = typename P::E;
+  using R = typename std::conditional<SPLIT, float, __half>::type;
+  const BatchConv cv = a.convs[it.obj];
+  E* ws = static_cast<E*>(a.ws);
+  const long long line0 = it.line0;
+  if (it.kind == kItemConvRow) {
+    auto io = zeroed<IoRealRowIn<R, E>>();
+    io.in = static_cast<const R*>(a.conv_in) + cv.img_off;
+    io.out = ws + cv.x_off;
+    io.total_lines = cv.sy;
+    io.sy = cv.sy;
+    io.sx = cv.sx;
+    io.P = L;
+    io.in_image_stride = static_cast<long long>(cv.sy) * cv.sx;
+    io.flip = 0;  // images are never flipped; correlation flips the filter
+    io.scale = it.scale;
+    return P::template tile<L, false, -1>(st, io, core, line0);
+  }
+  if (it.kind == kItemConvCol) {
+    auto io = zeroed<IoColMulConj<E>>();
+    io.in = ws + cv.x_off;
+    io.out = ws + cv.y_off;
+    io.total_lines = L;
+    io.P = L;
+    io.lps_log2 = cv.logP;
+    io.valid_rows = cv.sy;
+    io.r0 = 0;
+    io.nr = L;
+    io.scale = it.scale;
+    io.K = static_cast<const E*>(a.kspec) + cv.k_off;
+    return P::template tile<L, true, -1>(st, io, core, line0);
+  }
+  if (it.kind == kItemFiltRow) {
+    auto io = zeroed<IoRealRowIn<float, E>>();
+    io.in = a.filters + cv.filt_off;
+    io.out = ws + cv.x_off;
+    io.total_lines = cv.fy;
+    io.sy = cv.fy;
+    io.sx = cv.fx;
+    io.P = L;
+    io.in_image_stride = static_cast<long long>(cv.fy) * cv.fx;
+    io.flip = cv.flip;
+    io.scale = 1.0f;
+    return P::template tile<L, false, -1>(st, io, core, line0);
+  }
+  if (it.kind == kItemFiltCol) {
+    auto io = zeroed<IoColMaskCrop<E>>();
+    io.in = ws + cv.x_off;
+    io.out = static_cast<E*>(a.kspec) + cv.k_off;
+    io.total_lines = L;
+    io.P = L;
+    io.lps_log2 = cv.logP;
+    io.valid_rows = cv.fy;
+    io.r0 = 0;
+    io.nr = L;
+    io.scale = 1.0f;
+    return P::template tile<L, true, -1>(st, io, core, line0);
+  }
+  if (it.kind == kItemConvInv) {
+    auto io = zeroed<IoColMaskCrop<E>>();
+    io.in = ws + cv.y_off;
+    io.out = ws + cv.x_off;
+    io.total_lines = L;
+    io.P = L;
+    io.lps_log2 = cv.logP;
+    io.valid_rows = L;
+    io.r0 = cv.r0;
+    io.nr = cv.oy;
+    io.scale = it.scale;
+    return P::template tile<L, true, -1>(st, io, core, line0);
+  }
+  auto io = zeroed<IoRowCropReal<E, R>>();
+  io.in = ws + cv.x_off;
+  io.out = static_cast<R*>(a.conv_out) + cv.out_off;
+  io.total_lines = cv.oy;
+  io.P = L;
+  io.c0 = cv.c0;
+  io.nc = cv.ox;
+  io.scale = it.scale;
+  return P::template tile<L, false, -1>(st, io, core, line0);
 }
 
 template <bool SPLIT, int SIGN>
@@ -258,6 +412,17 @@ __device__ __forceinline__ bool batch_run_item(typename BatchPrec<SPLIT>::State&
       case 10: return batch_p2_item<SPLIT, SIGN, 1024>(st, a, it, core);
       default: break;
     }
+  } else if constexpr (SIGN == -1) {
+    // convolution stages: all forward transforms (see BatchConv)
+    switch (it.logl) {
+      case 6: return batch_conv_item<SPLIT, 64>(st, a, it, core);
+      case 7: return batch_conv_item<SPLIT, 128>(st, a, it, core);
+      case 8: return batch_conv_item<SPLIT, 256>(st, a, it, core);
+      case 9: return batch_conv_item<SPLIT, 512>(st, a, it, core);
+      case 10: return batch_conv_item<SPLIT, 1024>(st, a, it, core);
+      case 11: return batch_conv_item<SPLIT, 2048>(st, a, it, core);
+      default: break;
+    }
   }
   if (threadIdx.x == 0) atomicOr(a.err, kErrBadArgs);
   return true;
@@ -279,17 +444,17 @@ __global__ void __launch_bounds__(kPassThreads, SPLIT ? 2 : 3) fft_batch_kernel(
     const BatchItem it = a.items[i];
     if (threadIdx.x == 0) {
       bool ok = true;
-      if (it.kind == kItemP2) ok = wait_counter(a.done + it.xform, a.xforms[it.xform].tiles1);
+      if (it.wait_ctr >= 0) ok = wait_counter(a.ctrs + it.wait_ctr, it.wait_target);
       if (!ok) atomicOr(a.err, kErrQueueTimeout);
       s_ok = ok;
     }
     __syncthreads();
     if (s_ok) alive = batch_run_item<SPLIT, SIGN>(st, a, it);
-    if (it.kind == kItemP1) {
+    if (it.signal_ctr >= 0) {
       // publish: every thread's stores are visible device-wide before the count
       __threadfence();
       __syncthreads();
-      if (threadIdx.x == 0) atomicAdd(a.done + it.xform, 1);
+      if (threadIdx.x == 0) atomicAdd(a.ctrs + it.signal_ctr, 1);
     }
     __syncthreads();  // s_item / s_ok are rewritten next round
   }

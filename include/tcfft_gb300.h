@@ -175,11 +175,27 @@ typedef enum tcfftBatchMode {
 } tcfftBatchMode;
 tcfftStatus tcfft_batch_plan(tcfftBatch *batch, int count, const long long *n, const long long *in_off,
                              const long long *out_off, const float *scale, int precision, int direction);
+/* 2D convolutions in the same persistent launch (forward plans only): one
+ * real sy x sx image (half for TCFFT_FP16, float for split) convolved with
+ * one fy x fx float filter, tcfftConvMode semantics of tcfft_conv2d_plan,
+ * padded size P <= 2048. Offsets are in elements of the conv input / output
+ * buffers and of `filters` (device or host floats, filter_floats in total;
+ * copied, and the spectra made, at plan time). */
+typedef struct tcfftBatchConv {
+  int sy, sx, fy, fx, mode;
+  long long img_off, out_off, filt_off;
+} tcfftBatchConv;
+tcfftStatus tcfft_batch_plan_mixed(tcfftBatch *batch, int count, const long long *n, const long long *in_off,
+                                   const long long *out_off, const float *scale, int nconv,
+                                   const tcfftBatchConv *convs, const float *filters, long long filter_floats,
+                                   int precision, int direction);
 tcfftStatus tcfft_batch_set_mode(tcfftBatch batch, int mode);
 /* enable != 0: tcfft_batch_exec replays a CUDA graph of its launches,
  * captured on the first call for these buffers (re-captured when they change). */
 tcfftStatus tcfft_batch_set_graph(tcfftBatch batch, int enable);
 tcfftStatus tcfft_batch_exec(tcfftBatch batch, const void *in, void *out, void *stream);
+tcfftStatus tcfft_batch_exec_mixed(tcfftBatch batch, const void *in, void *out, const void *conv_in,
+                                   void *conv_out, void *stream);
 /* Work items of the persistent launch, workspace bytes, persistent CTAs. */
 tcfftStatus tcfft_batch_info(tcfftBatch batch, int *items, size_t *workspace_bytes, int *ctas);
 tcfftStatus tcfft_batch_check(tcfftBatch batch, void *stream);

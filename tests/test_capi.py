@@ -88,3 +88,23 @@ def test_batch_plan_validation_without_device(built_lib):
     assert plan([64], [0], t.FP16, 0) == t.INVALID_VALUE
     assert L.tcfft_batch_plan(None, 1, None, None, None, None, t.FP16, t.FORWARD) == t.INVALID_VALUE
     assert L.tcfft_batch_exec(None, None, None, None) == t.INVALID_VALUE
+
+
+def test_mixed_batch_validation_without_device(built_lib):
+    import fft_demo_gb300 as t
+    L = t.lib()
+    h = ctypes.c_void_p()
+    d = (t.BatchConvDesc * 1)()
+    filt = (ctypes.c_float * 16)()
+
+    def plan(desc, direction=t.FORWARD, floats=16):
+        d[0] = desc
+        return L.tcfft_batch_plan_mixed(ctypes.byref(h), 0, None, None, None, None, 1,
+                                        ctypes.cast(d, ctypes.c_void_p), ctypes.cast(filt, ctypes.c_void_p),
+                                        floats, t.SPLIT_FP32, direction)
+
+    assert plan(t.BatchConvDesc(64, 64, 4, 3, t.CONV_SAME, 0, 0, 0)) == t.INVALID_SIZE   # even filter, same mode
+    assert plan(t.BatchConvDesc(8, 8, 9, 9, t.CONV_VALID_CORR, 0, 0, 0)) == t.INVALID_SIZE
+    assert plan(t.BatchConvDesc(3000, 64, 3, 3, t.CONV_SAME, 0, 0, 0)) == t.INVALID_SIZE  # P > 2048
+    assert plan(t.BatchConvDesc(64, 64, 5, 5, t.CONV_SAME, 0, 0, 0)) == t.INVALID_VALUE   # filter past the buffer
+    assert plan(t.BatchConvDesc(64, 64, 3, 3, t.CONV_SAME, 0, 0, 0), t.INVERSE) == t.INVALID_VALUE
