@@ -212,6 +212,28 @@ def run_reference(args, world, rank):
     return 0
 
 
+def run_case(spec):
+    """A small, fixed workload for ncu: REPS execs of one plan on seeded data."""
+    import torch
+    import fft_demo_gb300 as tc
+    parts = spec.split(",")
+    n, batch = int(parts[0]), int(parts[1])
+    reps = int(parts[2]) if len(parts) > 2 else 3
+    prec = tc.SPLIT_FP32 if len(parts) > 3 and parts[3] == "split" else tc.FP16
+    dt = torch.float16 if prec == tc.FP16 else torch.float32
+    g = torch.Generator(device="cuda")
+    g.manual_seed(1)
+    x = (torch.rand((batch, n, 2), device="cuda", generator=g) * 2 - 1).to(dt)
+    y = torch.empty_like(x)
+    plan = tc.plan_1d(n, batch, prec)
+    for _ in range(reps):
+        plan.exec(x, y)
+    plan.check()
+    torch.cuda.synchronize()
+    print(json.dumps({"case": spec, "launches_per_exec": tc.last_launch_count()}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -219,7 +241,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--case", default=None,
+                    help="profiling case N,BATCH[,REPS[,PREC]]: REPS forward transforms of one size, no timing "
+                         "(PREC fp16 or split); the target of the ncu captures kept under profiles/")
     args = ap.parse_args()
+    if args.case:
+        return run_case(args.case)
     args.warmup = max(args.warmup, 3)
 
     world, rank, local = dist_init()
