@@ -244,9 +244,20 @@ def main():
     ap.add_argument("--case", default=None,
                     help="profiling case N,BATCH[,REPS[,PREC]]: REPS forward transforms of one size, no timing "
                          "(PREC fp16 or split); the target of the ncu captures kept under profiles/")
+    ap.add_argument("--workload", default="large-1d",
+                    choices=["large-1d", "small", "2d-conv", "uneven", "serving"],
+                    help="large-1d: the headline run (default); the others print one JSON line each "
+                         "(fft_demo_gb300/workloads.py)")
     args = ap.parse_args()
     if args.case:
         return run_case(args.case)
+    if args.workload != "large-1d":
+        from fft_demo_gb300 import workloads
+        peak, kind = load_peaks()
+        res = workloads.WORKLOADS[args.workload](peak)
+        res.update({"peak_gbs": peak, "peak_kind": kind, "data": "synthetic (seeded)", "n_gpus": 1})
+        print(json.dumps(res), flush=True)
+        return 0
     args.warmup = max(args.warmup, 3)
 
     world, rank, local = dist_init()

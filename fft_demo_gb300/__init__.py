@@ -66,6 +66,11 @@ def _declare(L):
         "tcfft_batch_plan_mixed": (i, [ctypes.POINTER(vp), i, vp, vp, vp, vp, i, vp, vp, ll, i, i]),
         "tcfft_batch_exec_mixed": (i, [vp, vp, vp, vp, vp, vp]),
         "tcfft_batch_set_mode": (i, [vp, i]),
+        "tcfft_queue_create": (i, [ctypes.POINTER(vp), i, ctypes.c_size_t, ctypes.c_size_t]),
+        "tcfft_queue_set_filter": (i, [vp, i, vp, i, i]),
+        "tcfft_queue_submit": (i, [vp, i, vp, vp, vp, vp, i, vp, vp, vp, vp, vp, vp]),
+        "tcfft_queue_check": (i, [vp, vp]),
+        "tcfft_queue_destroy": (i, [vp]),
         "tcfft_batch_set_graph": (i, [vp, i]),
         "tcfft_batch_exec": (i, [vp, vp, vp, vp]),
         "tcfft_batch_info": (i, [vp, ctypes.POINTER(i), ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(i)]),
@@ -320,6 +325,65 @@ class Batch:
     def destroy(self):
         if self._h:
             lib().tcfft_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class QueueConvDesc(ctypes.Structure):
+    """tcfftQueueConv: one convolution request of a queue submit."""
+    _fields_ = [("sy", ctypes.c_int), ("sx", ctypes.c_int), ("filter_id", ctypes.c_int), ("mode", ctypes.c_int),
+                ("img_off", ctypes.c_longlong), ("out_off", ctypes.c_longlong)]
+
+
+class Queue:
+    """Serving queue (tcfft_queue_*): forward 1D FFTs and convolutions with
+    pooled filters, batched into one persistent launch per submit, with
+    tables, filter spectra, workspace and staging resident on the device.
+    One stream per queue."""
+
+    def __init__(self, precision=FP16, workspace_bytes=1 << 30, staging_bytes=8 << 20):
+        self.precision = precision
+        self._h = ctypes.c_void_p()
+        _check(lib().tcfft_queue_create(ctypes.byref(self._h), precision, int(workspace_bytes),
+                                        int(staging_bytes)), "queue_create")
+
+    def set_filter(self, fid, filt):
+        """filt: fy x fx floats (numpy array or CUDA float tensor)."""
+        import numpy as np
+        if hasattr(filt, "data_ptr"):
+            fy, fx = filt.shape
+            ptr = filt.data_ptr()
+        else:
+            f = np.ascontiguousarray(filt, dtype=np.float32)
+            fy, fx = f.shape
+            ptr = f.ctypes.data
+        _check(lib().tcfft_queue_set_filter(self._h, int(fid), ptr, int(fy), int(fx)), "queue_set_filter")
+
+    def submit(self, n=(), in_off=(), out_off=(), convs=(), x=None, out=None, conv_in=None, conv_out=None,
+               stream=None):
+        """n/in_off/out_off: 1D transforms; convs: (sy, sx, filter_id, mode, img_off, out_off) tuples."""
+        import numpy as np
+        n = np.ascontiguousarray(n, dtype=np.int64)
+        io = np.ascontiguousarray(in_off, dtype=np.int64)
+        oo = np.ascontiguousarray(out_off, dtype=np.int64)
+        cd = (QueueConvDesc * max(1, len(convs)))(*[QueueConvDesc(*c) for c in convs])
+        p = lambda t: None if t is None else t.data_ptr()  # noqa: E731
+        _check(lib().tcfft_queue_submit(self._h, len(n), n.ctypes.data if len(n) else None,
+                                        io.ctypes.data if len(n) else None, oo.ctypes.data if len(n) else None,
+                                        None, len(convs), ctypes.cast(cd, ctypes.c_void_p) if len(convs) else None,
+                                        p(x), p(out), p(conv_in), p(conv_out), _stream_ptr(stream)), "queue_submit")
+
+    def check(self, stream=None):
+        _check(lib().tcfft_queue_check(self._h, _stream_ptr(stream)), "queue_check")
+
+    def destroy(self):
+        if self._h:
+            lib().tcfft_queue_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

@@ -83,8 +83,8 @@ struct BatchXform {
 struct BatchConv {
   long long img_off, out_off;  // real elements in the conv input / output buffers
   long long x_off, y_off;      // elements in the workspace
-  long long k_off;             // elements in the filter-spectrum buffer
-  long long filt_off;          // floats in the filter buffer
+  void* kspec;                 // P x P filter spectrum (E)
+  const float* filt;           // fy x fx float filter (spectrum items)
   int sy, sx, oy, ox, r0, c0, logP, flip, fy, fx, pad0, pad1;
 };
 
@@ -100,8 +100,6 @@ struct BatchArgs {
   const BatchConv* convs;
   const void* conv_in;   // real images (half for FP16, float for split)
   void* conv_out;        // real outputs
-  void* kspec;            // filter spectra (E)
-  const float* filters;   // fy x fx float filters (spectrum items)
   unsigned int* counter;  // queue head
   int* ctrs;              // dependency counters
   const float2* tw[kBatchMaxLineLog + 1];  // W_L, this direction
@@ -324,12 +322,12 @@ __device__ __noinline__ bool batch_conv_item(typename BatchPrec<SPLIT>::State& s
     io.r0 = 0;
     io.nr = L;
     io.scale = it.scale;
-    io.K = static_cast<const E*>(a.kspec) + cv.k_off;
+    io.K = static_cast<const E*>(cv.kspec);
     return P::template tile<L, true, -1>(st, io, core, line0);
   }
   if (it.kind == kItemFiltRow) {
     auto io = zeroed<IoRealRowIn<float, E>>();
-    io.in = a.filters + cv.filt_off;
+    io.in = cv.filt;
     io.out = ws + cv.x_off;
     io.total_lines = cv.fy;
     io.sy = cv.fy;
@@ -343,7 +341,7 @@ __device__ __noinline__ bool batch_conv_item(typename BatchPrec<SPLIT>::State& s
   if (it.kind == kItemFiltCol) {
     auto io = zeroed<IoColMaskCrop<E>>();
     io.in = ws + cv.x_off;
-    io.out = static_cast<E*>(a.kspec) + cv.k_off;
+    io.out = static_cast<E*>(cv.kspec);
     io.total_lines = L;
     io.P = L;
     io.lps_log2 = cv.logP;

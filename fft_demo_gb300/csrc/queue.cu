@@ -1,0 +1,320 @@
+// Serving queue: continuous batching of 1D FFT and 2D convolution requests
+// into the persistent batch kernel (fft_batch.cuh), with everything a
+// request needs kept resident on the device: twiddle and DFT tables for
+// every supported size, a pool of filters and their spectra per padded size
+// (made on first use), a workspace arena and two staging slots for the work
+// lists, so that a submit allocates nothing except a new filter spectrum.
+//
+// A submit builds the work list on the host, copies it from pinned staging
+// memory with one cudaMemcpyAsync, and makes one launch (two when a filter
+// spectrum is new). Slot k's staging is rewritten only after the launch that
+// used it two submits ago has finished, so host work on submit i+1 overlaps
+// the GPU work of submit i. All submits of a queue share its workspace and
+// counters: use one stream per queue.
+//
+// No counterpart in the reference, whose entry points run one plan's size
+// per call (tcfftExec, tcfft_half.cu:1177; fft_conv2d_half::conv2d_forward,
+// tensorcore_fft_conv2d.cpp:283).
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <map>
+#include <new>
+#include <utility>
+#include <vector>
+
+#include "../../include/tcfft_gb300.h"
+#include "batch_host.cuh"
+#include "capi_internal.cuh"
+
+using namespace tcfft;
+using namespace tcfft::bh;
+
+struct tcfftQueueImpl {
+  int precision = TCFFT_FP16;
+  int pr = 0;
+  size_t eb = 4;  // bytes per complex element
+  void* tables = nullptr;
+  BatchArgs base{};
+  void* ws = nullptr;
+  size_t ws_elems = 0;
+  int* ctr = nullptr;
+  size_t ctr_cap = 0;
+  int* err = nullptr;
+  struct Slot {
+    unsigned char* dev = nullptr;
+    unsigned char* host = nullptr;
+    cudaEvent_t ev = nullptr;
+    bool pending = false;
+  };
+  Slot slot[2];
+  int cur = 0;
+  size_t slot_bytes = 0;
+  struct Filter {
+    float* dev = nullptr;
+    int fy = 0, fx = 0;
+    std::map<std::pair<int, int>, void*> spec;  // (log2 P, flip) -> spectrum
+  };
+  std::map<int, Filter> filters;
+};
+
+namespace {
+
+void free_queue(tcfftQueueImpl* q) {
+  if (!q) return;
+  for (auto& s : q->slot) {
+    if (s.ev) cudaEventSynchronize(s.ev);
+    if (s.ev) cudaEventDestroy(s.ev);
+    cudaFree(s.dev);
+    cudaFreeHost(s.host);
+  }
+  for (auto& kv : q->filters) {
+    cudaFree(kv.second.dev);
+    for (auto& sp : kv.second.spec) cudaFree(sp.second);
+  }
+  cudaFree(q->tables);
+  cudaFree(q->ws);
+  cudaFree(q->ctr);
+  cudaFree(q->err);
+  delete q;
+}
+
+// Forward tables for every size the batch kernel runs.
+tcfftStatus make_tables(tcfftQueueImpl* q) {
+  size_t off_tw[kBatchMaxLineLog + 1] = {}, off_lo[kBatchMaxLog + 1] = {}, off_hi[kBatchMaxLog + 1] = {};
+  size_t at = 4096;  // DFT16 B image (hi, lo) first
+  for (int l = kBatchMinLineLog; l <= kBatchMaxLineLog; ++l) {
+    off_tw[l] = at;
+    at = align_up(at + (sizeof(float2) << l), 256);
+  }
+  for (int l = kBatchMaxLineLog + 1; l <= kBatchMaxLog; ++l) {
+    const int sh = (l + 1) / 2;
+    off_lo[l] = at;
+    at = align_up(at + (sizeof(float2) << sh), 256);
+    off_hi[l] = at;
+    at = align_up(at + (sizeof(float2) << (l - sh)), 256);
+  }
+  if (cudaMalloc(&q->tables, at) != cudaSuccess) return TCFFT_ALLOC_FAILED;
+  unsigned char* A = static_cast<unsigned char*>(q->tables);
+  cudaError_t e = gen_dft16_bmat(reinterpret_cast<uint16_t*>(A), -1, 0, 0);
+  if (e == cudaSuccess) e = gen_dft16_bmat(reinterpret_cast<uint16_t*>(A) + 1024, -1, 1, 0);
+  BatchArgs& a = q->base;
+  for (int l = kBatchMinLineLog; l <= kBatchMaxLineLog && e == cudaSuccess; ++l) {
+    e = gen_twiddles(reinterpret_cast<float2*>(A + off_tw[l]), 1ll << l, l, 0, -1, 0);
+    a.tw[l] = reinterpret_cast<const float2*>(A + off_tw[l]);
+  }
+  for (int l = kBatchMaxLineLog + 1; l <= kBatchMaxLog && e == cudaSuccess; ++l) {
+    const int sh = (l + 1) / 2;
+    e = gen_twiddles(reinterpret_cast<float2*>(A + off_lo[l]), 1ll << sh, l, 0, -1, 0);
+    if (e == cudaSuccess) e = gen_twiddles(reinterpret_cast<float2*>(A + off_hi[l]), 1ll << (l - sh), l, sh, -1, 0);
+    a.otw[l].lo = reinterpret_cast<const float2*>(A + off_lo[l]);
+    a.otw[l].hi = reinterpret_cast<const float2*>(A + off_hi[l]);
+    a.otw[l].shift = sh;
+    a.otw[l].logn = l;
+  }
+  a.bmat = reinterpret_cast<const uint32_t*>(A);
+  return e == cudaSuccess ? TCFFT_OK : TCFFT_LAUNCH_FAILED;
+}
+
+}  // namespace
+
+extern "C" {
+
+tcfftStatus tcfft_queue_create(tcfftQueue* queue, int precision, size_t workspace_bytes, size_t staging_bytes) {
+  if (!queue) return record_status(TCFFT_INVALID_VALUE, 0);
+  *queue = nullptr;
+  if (precision != TCFFT_FP16 && precision != TCFFT_SPLIT_FP32) return record_status(TCFFT_INVALID_VALUE, 0);
+  if (workspace_bytes < (1u << 20) || staging_bytes < (1u << 16)) return record_status(TCFFT_INVALID_SIZE, 0);
+  tcfftStatus s = batch_registry_ready();
+  if (s != TCFFT_OK) return record_status(s, 0);
+  tcfftQueueImpl* q = new (std::nothrow) tcfftQueueImpl();
+  if (!q) return record_status(TCFFT_ALLOC_FAILED, 0);
+  q->precision = precision;
+  q->pr = precision == TCFFT_FP16 ? 0 : 1;
+  q->eb = precision == TCFFT_FP16 ? 4 : 8;
+  q->ws_elems = workspace_bytes / q->eb;
+  q->slot_bytes = align_up(staging_bytes, 256);
+  q->ctr_cap = q->slot_bytes / sizeof(BatchItem) + 1;  // every counter belongs to at least one item
+  s = make_tables(q);
+  if (s == TCFFT_OK && (cudaMalloc(&q->ws, q->ws_elems * q->eb) != cudaSuccess ||
+                        cudaMalloc(&q->ctr, sizeof(int) * q->ctr_cap) != cudaSuccess ||
+                        cudaMalloc(&q->err, sizeof(int)) != cudaSuccess))
+    s = TCFFT_ALLOC_FAILED;
+  if (s == TCFFT_OK && cudaMemset(q->err, 0, sizeof(int)) != cudaSuccess) s = TCFFT_LAUNCH_FAILED;
+  for (auto& sl : q->slot) {
+    if (s != TCFFT_OK) break;
+    if (cudaMalloc(&sl.dev, q->slot_bytes) != cudaSuccess ||
+        cudaHostAlloc(reinterpret_cast<void**>(&sl.host), q->slot_bytes, cudaHostAllocDefault) != cudaSuccess ||
+        cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess)
+      s = TCFFT_ALLOC_FAILED;
+  }
+  if (s == TCFFT_OK && cudaDeviceSynchronize() != cudaSuccess) s = TCFFT_LAUNCH_FAILED;
+  if (s != TCFFT_OK) {
+    free_queue(q);
+    return record_status(s, 0);
+  }
+  q->base.ws = q->ws;
+  q->base.err = q->err;
+  q->base.ctrs = q->ctr;
+  q->base.counter = reinterpret_cast<unsigned int*>(q->ctr);
+  *queue = q;
+  return record_status(TCFFT_OK, 0);
+}
+
+tcfftStatus tcfft_queue_set_filter(tcfftQueue q, int id, const float* filter, int fy, int fx) {
+  if (!q || !filter || fy < 1 || fx < 1) return record_status(TCFFT_INVALID_VALUE, 0);
+  if (q->filters.count(id)) return record_status(TCFFT_INVALID_VALUE, 0);  // ids are set once
+  tcfftQueueImpl::Filter f;
+  f.fy = fy;
+  f.fx = fx;
+  const size_t bytes = sizeof(float) * static_cast<size_t>(fy) * fx;
+  if (cudaMalloc(&f.dev, bytes) != cudaSuccess) return record_status(TCFFT_ALLOC_FAILED, 0);
+  if (cudaMemcpy(f.dev, filter, bytes, cudaMemcpyDefault) != cudaSuccess) {
+    cudaFree(f.dev);
+    return record_status(TCFFT_LAUNCH_FAILED, 0);
+  }
+  q->filters.emplace(id, f);
+  return record_status(TCFFT_OK, 0);
+}
+
+tcfftStatus tcfft_queue_submit(tcfftQueue q, int count, const long long* n, const long long* in_off,
+                               const long long* out_off, const float* scale, int nconv, const tcfftQueueConv* convs,
+                               const void* in, void* out, const void* conv_in, void* conv_out, void* stream) {
+  if (!q || count < 0 || nconv < 0) return record_status(TCFFT_INVALID_VALUE, 0);
+  if (count > 0 && (!n || !in_off || !out_off || !in || !out)) return record_status(TCFFT_INVALID_VALUE, 0);
+  if (nconv > 0 && (!convs || !conv_in || !conv_out)) return record_status(TCFFT_INVALID_VALUE, 0);
+  if ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u)
+    return record_status(TCFFT_INVALID_VALUE, 0);
+  if (count + nconv == 0) return record_status(TCFFT_OK, 0);
+  const long long align_elems = q->precision == TCFFT_FP16 ? 4 : 2;
+  for (int i = 0; i < count; ++i) {
+    const int l = ilog2_exact(n[i]);
+    if (l < kBatchMinLineLog || l > kBatchMaxLog) return record_status(TCFFT_INVALID_SIZE, 0);
+    if (in_off[i] < 0 || out_off[i] < 0 || in_off[i] % align_elems || out_off[i] % align_elems)
+      return record_status(TCFFT_INVALID_VALUE, 0);
+  }
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  BatchSpec spec;
+  std::vector<float> ones;
+  if (count > 0 && !scale) {
+    ones.assign(static_cast<size_t>(count), 1.0f);
+    scale = ones.data();
+  }
+  spec.count = count;
+  spec.n = n;
+  spec.in_off = in_off;
+  spec.out_off = out_off;
+  spec.scale = scale;
+  // convolutions: geometry and spectra (a new (filter, P) spectrum is made
+  // by this submit's first launch)
+  for (int c = 0; c < nconv; ++c) {
+    const tcfftQueueConv& r = convs[c];
+    auto fit = q->filters.find(r.filter_id);
+    if (fit == q->filters.end()) return record_status(TCFFT_INVALID_VALUE, 0);
+    tcfftBatchConv d{r.sy, r.sx, fit->second.fy, fit->second.fx, r.mode, r.img_off, r.out_off, 0};
+    BatchConv cv{};
+    if (r.sy < 1 || r.sx < 1 || !conv_geometry(d, cv)) return record_status(TCFFT_INVALID_SIZE, 0);
+    if (r.img_off < 0 || r.out_off < 0) return record_status(TCFFT_INVALID_VALUE, 0);
+    cv.img_off = r.img_off;
+    cv.out_off = r.out_off;
+    cv.filt = fit->second.dev;
+    const auto key = std::make_pair(cv.logP, cv.flip);
+    char prep = 0;
+    auto sit = fit->second.spec.find(key);
+    if (sit == fit->second.spec.end()) {
+      void* k = nullptr;
+      if (cudaMalloc(&k, q->eb << (2 * cv.logP)) != cudaSuccess) return record_status(TCFFT_ALLOC_FAILED, 0);
+      sit = fit->second.spec.emplace(key, k).first;
+      prep = 1;
+    }
+    cv.kspec = sit->second;
+    spec.convs.push_back(cv);
+    spec.conv_prep.push_back(prep);
+  }
+  // one prep pass per new spectrum, even if several requests share it
+  for (size_t j = 0; j < spec.convs.size(); ++j)
+    for (size_t i = 0; i < j; ++i)
+      if (spec.conv_prep[i] && spec.convs[i].kspec == spec.convs[j].kspec) spec.conv_prep[j] = 0;
+  const int ctas = batch_ctas(q->pr, 0);
+  Built bl = build_items(spec, 2 * ctas);
+  if (bl.ws_elems > q->ws_elems || static_cast<size_t>(bl.nctrs) > q->ctr_cap)
+    return record_status(TCFFT_CAPACITY, 0);
+  // work lists -> staging slot
+  size_t at = 0;
+  auto place = [&](size_t bytes) {
+    const size_t o = at;
+    at = align_up(at + bytes, 256);
+    return o;
+  };
+  const size_t o_lin = place(sizeof(long long) * bl.line_in.size());
+  const size_t o_lout = place(sizeof(long long) * bl.line_out.size());
+  const size_t o_items = place(sizeof(BatchItem) * bl.items.size());
+  const size_t o_prep = place(sizeof(BatchItem) * bl.prep_items.size());
+  const size_t o_xf = place(sizeof(BatchXform) * bl.xforms.size());
+  const size_t o_cv = place(sizeof(BatchConv) * bl.convs.size());
+  if (at > q->slot_bytes) return record_status(TCFFT_CAPACITY, 0);
+  tcfftQueueImpl::Slot& sl = q->slot[q->cur];
+  if (sl.pending && cudaEventSynchronize(sl.ev) != cudaSuccess) return record_status(TCFFT_LAUNCH_FAILED, 0);
+  sl.pending = false;
+  auto put = [&](size_t o, const void* src, size_t bytes) {
+    if (bytes) std::memcpy(sl.host + o, src, bytes);
+  };
+  put(o_lin, bl.line_in.data(), sizeof(long long) * bl.line_in.size());
+  put(o_lout, bl.line_out.data(), sizeof(long long) * bl.line_out.size());
+  put(o_items, bl.items.data(), sizeof(BatchItem) * bl.items.size());
+  put(o_prep, bl.prep_items.data(), sizeof(BatchItem) * bl.prep_items.size());
+  put(o_xf, bl.xforms.data(), sizeof(BatchXform) * bl.xforms.size());
+  put(o_cv, bl.convs.data(), sizeof(BatchConv) * bl.convs.size());
+  if (cudaMemcpyAsync(sl.dev, sl.host, at, cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return record_status(TCFFT_LAUNCH_FAILED, 0);
+  BatchArgs a = q->base;
+  a.in = in;
+  a.out = out;
+  a.conv_in = conv_in;
+  a.conv_out = conv_out;
+  a.line_in = reinterpret_cast<const long long*>(sl.dev + o_lin);
+  a.line_out = reinterpret_cast<const long long*>(sl.dev + o_lout);
+  a.xforms = reinterpret_cast<const BatchXform*>(sl.dev + o_xf);
+  a.convs = reinterpret_cast<const BatchConv*>(sl.dev + o_cv);
+  const BatchKernel& k = batch_kernel(q->pr, 0);
+  int launches = 0;
+  auto launch = [&](size_t o, size_t nitems) -> bool {
+    BatchArgs la = a;
+    la.items = reinterpret_cast<const BatchItem*>(sl.dev + o);
+    la.nitems = static_cast<int>(nitems);
+    if (cudaMemsetAsync(q->ctr, 0, sizeof(int) * static_cast<size_t>(bl.nctrs), st) != cudaSuccess) return false;
+    const int grid = static_cast<int>(std::min<size_t>(static_cast<size_t>(ctas), nitems));
+    void* params[] = {&la};
+    if (cudaLaunchKernel(k.fn, dim3(static_cast<unsigned>(grid)), dim3(kPassThreads), params,
+                         static_cast<size_t>(k.smem), st) != cudaSuccess)
+      return false;
+    ++launches;
+    return true;
+  };
+  if (!bl.prep_items.empty() && !launch(o_prep, bl.prep_items.size())) return record_status(TCFFT_LAUNCH_FAILED, 0);
+  if (!bl.items.empty() && !launch(o_items, bl.items.size())) return record_status(TCFFT_LAUNCH_FAILED, launches);
+  if (cudaEventRecord(sl.ev, st) != cudaSuccess) return record_status(TCFFT_LAUNCH_FAILED, launches);
+  sl.pending = true;
+  q->cur ^= 1;
+  return record_status(TCFFT_OK, launches);
+}
+
+tcfftStatus tcfft_queue_check(tcfftQueue q, void* stream) {
+  if (!q) return record_status(TCFFT_INVALID_VALUE, 0);
+  if (cudaStreamSynchronize(static_cast<cudaStream_t>(stream)) != cudaSuccess)
+    return record_status(TCFFT_LAUNCH_FAILED, 0);
+  int flag = 0;
+  if (cudaMemcpy(&flag, q->err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemset(q->err, 0, sizeof(int)) != cudaSuccess)
+    return record_status(TCFFT_LAUNCH_FAILED, 0);
+  if (flag & (kErrMmaTimeout | kErrQueueTimeout)) return record_status(TCFFT_TIMEOUT, 0);
+  return record_status(flag ? TCFFT_INVALID_VALUE : TCFFT_OK, 0);
+}
+
+tcfftStatus tcfft_queue_destroy(tcfftQueue q) {
+  if (!q) return record_status(TCFFT_INVALID_VALUE, 0);
+  free_queue(q);
+  return record_status(TCFFT_OK, 0);
+}
+
+}  // extern "C"

@@ -1,0 +1,347 @@
+"""Continuous-batching request loop over the serving queue (tcfft_queue_*).
+
+Requests arrive as a Poisson stream and mix forward 1D FFTs (n = 2^k, k
+uniform on [6, 20]) and 'same'-mode 2D convolutions (square images, sides
+log-uniform over 64 .. 1024, filters from a resident pool of 64 with odd
+sides 3 .. 63), FP16 and split precision interleaved at random. Request
+inputs are resident in HBM (a pool of seeded payloads per size, as if an
+upstream GPU stage produced them); every batch's outputs are copied to
+pinned host memory, and a request completes when that copy has.
+
+Each loop turn, per precision, the requests that have arrived are admitted
+in arrival order while they fit the device budget (an output ring and the
+queue's workspace, all inside the HBM cap) and go to the GPU as one submit:
+one persistent launch (tcfft_queue_submit) plus one device-to-host copy.
+At most two submits per precision are in flight, so the host builds batch
+i+1 while the GPU runs batch i.
+
+Latency = completion (a CUDA event after the batch's output copy, on a
+clock aligned with the host's) minus arrival; reported as p50 / p99 with
+req/s, GFLOP/s (5 N log2 N per 1D FFT; 5 P^2 log2 P^2 per 2D transform, two
+per convolution plus the pointwise product) and per-request relative-L2
+error against the FP64 oracle for a sample of requests, per precision and
+kind. FP16 convolution errors run higher than FP16 FFT errors for these
+filters: the spectra are rounded relative to |image| * |filter|, while the
+output of a zero-mean filter is much smaller than that.
+"""
+import argparse
+import collections
+import json
+import math
+import os
+import sys
+import time
+
+import numpy as np
+
+import fft_demo_gb300 as tc
+
+KMIN, KMAX = 6, 20
+IMAGE_SIDES = (64, 128, 256, 512, 1024)
+N_FILTERS = 64
+
+
+def conv_padded(s, f):
+    need = s + (f - 1) // 2
+    p = 64
+    while p < need:
+        p *= 2
+    return p
+
+
+def make_workload(seed, rate, seconds, conv_fraction=0.5):
+    rng = np.random.default_rng(seed)
+    count = int(rate * seconds)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, count))
+    is_conv = rng.random(count) < conv_fraction
+    prec = np.where(rng.random(count) < 0.5, tc.FP16, tc.SPLIT_FP32)
+    k = rng.integers(KMIN, KMAX + 1, count)
+    side = rng.choice(IMAGE_SIDES, count)
+    fid = rng.integers(0, N_FILTERS, count)
+    return {"arrival": arrivals, "conv": is_conv, "prec": prec, "k": k, "side": side, "fid": fid}
+
+
+def make_filters(seed):
+    rng = np.random.default_rng(seed + 1)
+    sizes = rng.choice(np.arange(3, 64, 2), N_FILTERS)
+    out = []
+    for f in sizes:
+        w = rng.standard_normal((f, f))
+        out.append((w / np.abs(w).sum()).astype(np.float32))
+    return out
+
+
+def request_flops(wl, i, filters):
+    if wl["conv"][i]:
+        p = conv_padded(int(wl["side"][i]), filters[wl["fid"][i]].shape[0])
+        return 2 * 5 * p * p * math.log2(p * p) + 6 * p * p
+    n = 1 << int(wl["k"][i])
+    return 5 * n * math.log2(n)
+
+
+MAX_ITEMS = 250000  # work items per submit (the staging slot holds ~400k)
+
+
+def lane_limit(lane, first_need):
+    """Where the next batch may end in the lane's output ring (it starts at
+    lane.head, possibly moved to 0); None when even the first request does
+    not fit yet. In-flight batches occupy [start, end) regions in order."""
+    if not lane.inflight:
+        lane.head = 0
+        return lane.ring_elems
+    tail = lane.inflight[0][1]
+    if lane.head >= tail:  # free: [head, end) and [0, tail)
+        if lane.head + first_need <= lane.ring_elems:
+            return lane.ring_elems
+        if first_need < tail:
+            lane.head = 0
+            return tail - 1
+        return None
+    return tail - 1 if lane.head + first_need < tail else None
+
+
+class Lane:
+    """One precision: its queue, input pools, output ring and in-flight batches."""
+
+    def __init__(self, prec, filters, seed, ring_bytes, ws_bytes, staging_bytes, pool_per_size):
+        import torch
+        self.prec = prec
+        self.eb = 4 if prec == tc.FP16 else 8  # complex element bytes
+        self.dt = torch.float16 if prec == tc.FP16 else torch.float32
+        self.q = tc.Queue(prec, ws_bytes, staging_bytes)
+        for i, w in enumerate(filters):
+            self.q.set_filter(i, w)
+        self.ws_bytes = ws_bytes
+        rng = np.random.default_rng(seed)
+        # input pools, one device arena: 1D complex payloads and real images
+        self.pool = {}
+        chunks, at = [], 0
+        for kk in range(KMIN, KMAX + 1):
+            for j in range(pool_per_size):
+                n = 1 << kk
+                a = rng.uniform(-1, 1, (n, 2)).astype(np.float32)
+                self.pool[("fft", kk, j)] = (at, a)
+                chunks.append(a.ravel())
+                at += a.size
+        for s in IMAGE_SIDES:
+            for j in range(pool_per_size):
+                a = rng.uniform(0, 1, (s, s)).astype(np.float32)
+                self.pool[("img", s, j)] = (at, a)
+                chunks.append(a.ravel())
+                at += a.size
+        self.arena = torch.from_numpy(np.concatenate(chunks)).to(self.dt).cuda()
+        # host copies of the payloads as rounded to the storage type (oracle input)
+        host = self.arena.float().cpu().numpy()
+        self.pool = {key: (off, host[off:off + a.size].reshape(a.shape)) for key, (off, a) in self.pool.items()}
+        self.ring_elems = ring_bytes // (self.eb // 2)  # in real elements of the storage type
+        self.ring = torch.empty(self.ring_elems, dtype=self.dt, device="cuda")
+        self.host_out = torch.empty(self.ring_elems, dtype=self.dt, pin_memory=True)
+        self.head = 0       # next free real element of the ring
+        self.inflight = collections.deque()  # (event, ring_start, ring_end, requests)
+        self.stream = torch.cuda.Stream()
+
+
+def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, sample_every=97,
+        pool_per_size=2, max_batch=1024, verbose=False):
+    import torch
+    filters = make_filters(seed)
+    wl = make_workload(seed, rate, seconds, conv_fraction)
+    nreq = len(wl["arrival"])
+    cap = int(hbm_cap_gb * (1 << 30))
+    # HBM budget inside the cap: per precision an output ring and a workspace;
+    # the input pools and filter spectra are counted against it too
+    ws_bytes = min(6 << 30, cap // 8)
+    ring_bytes = min(6 << 30, cap // 8)
+    lanes = {p: Lane(p, filters, seed + 10 * p, ring_bytes, ws_bytes, 16 << 20, pool_per_size)
+             for p in (tc.FP16, tc.SPLIT_FP32)}
+    spectra = sum(N_FILTERS * sum(conv_padded(s, 63) ** 2 for s in IMAGE_SIDES) * l.eb for l in lanes.values())
+    resident = spectra + sum(l.arena.numel() * l.arena.element_size() + ring_bytes + ws_bytes
+                             for l in lanes.values())
+    if resident > cap:
+        raise RuntimeError("device budget %.1f GB exceeds the %.1f GB cap" % (resident / 1e9, cap / 1e9))
+    # per-request device footprint: output + workspace
+    out_elems = np.zeros(nreq, np.int64)  # real elements of the storage type
+    ws_elems = np.zeros(nreq, np.int64)   # complex elements of workspace
+    for i in range(nreq):
+        if wl["conv"][i]:
+            s = int(wl["side"][i])
+            f = filters[wl["fid"][i]].shape[0]
+            p = conv_padded(s, f)
+            out_elems[i] = s * s
+            ws_elems[i] = (max(s, f) + p) * p
+        else:
+            n = 1 << int(wl["k"][i])
+            out_elems[i] = 2 * n
+            ws_elems[i] = n if n > 8192 else 0
+    out_elems = (out_elems + 63) // 64 * 64  # 128-byte alignment for FP16, 256 for split
+    # work items of the persistent launch per request (tiles of 8192 points)
+    items_est = np.zeros(nreq, np.int64)
+    for i in range(nreq):
+        if wl["conv"][i]:
+            s_ = int(wl["side"][i])
+            p_ = conv_padded(s_, filters[wl["fid"][i]].shape[0])
+            items_est[i] = (2 * s_ + 2 * p_) * p_ // 8192 + 8
+        else:
+            items_est[i] = 2 * (1 << int(wl["k"][i])) // 8192 + 1
+    # warm-up: every filter spectrum per padded size, and the kernel
+    for lane in lanes.values():
+        convs = []
+        at = 0
+        for fidx, w in enumerate(filters):
+            for s in IMAGE_SIDES:
+                convs.append((s, s, fidx, tc.CONV_SAME, lane.pool[("img", s, 0)][0], at))
+                at += s * s
+        # in several submits (workspace limit)
+        for j in range(0, len(convs), 16):
+            part = convs[j:j + 16]
+            base = part[0][5]
+            part = [(a, b, c, d, e, f - base) for (a, b, c, d, e, f) in part]
+            lane.q.submit(convs=part, conv_in=lane.arena, conv_out=lane.ring, stream=lane.stream)
+        lane.q.check(lane.stream)
+    torch.cuda.synchronize()
+
+    lat = np.full(nreq, np.nan)
+    samples = []
+    e0 = torch.cuda.Event(enable_timing=True)
+    pending = collections.deque(range(nreq))
+    launches = 0
+    done = 0
+    t0 = time.perf_counter()
+    for lane in lanes.values():
+        lane.e0 = torch.cuda.Event(enable_timing=True)
+        lane.e0.record(lane.stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    busy_flops = 0.0
+    waiting = {p: collections.deque() for p in lanes}
+    while done < nreq:
+        now = time.perf_counter() - t0
+        # retire finished batches
+        for p, lane in lanes.items():
+            while lane.inflight and lane.inflight[0][0].query():
+                ev, start, end, reqs = lane.inflight.popleft()
+                t_done = lane.e0.elapsed_time(ev) * 1e-3
+                for (i, off) in reqs:
+                    lat[i] = t_done - wl["arrival"][i]
+                    if i % sample_every == 0:
+                        samples.append((i, lane.host_out[off:off + out_elems[i]].float().numpy().copy()))
+                done += len(reqs)
+        # arrivals -> per-precision waiting lines
+        while pending and wl["arrival"][pending[0]] <= now:
+            i = pending.popleft()
+            waiting[int(wl["prec"][i])].append(i)
+        for p, lane in lanes.items():
+            if not waiting[p] or len(lane.inflight) >= 2:
+                continue
+            # admit in arrival order while the output ring, the workspace
+            # and the staging slot (work items) allow
+            limit = lane_limit(lane, int(out_elems[waiting[p][0]]))
+            if limit is None:
+                continue
+            reqs, ws_used, nitems = [], 0, 0
+            pos = lane.head
+            while waiting[p] and len(reqs) < max_batch:
+                i = waiting[p][0]
+                need = int(out_elems[i])
+                if pos + need > limit or ws_used + ws_elems[i] * lane.eb > lane.ws_bytes or \
+                        nitems + items_est[i] > MAX_ITEMS:
+                    break
+                waiting[p].popleft()
+                reqs.append((i, pos))
+                pos += need
+                ws_used += ws_elems[i] * lane.eb
+                nitems += items_est[i]
+            start = lane.head
+            lane.head = pos
+            if not reqs:
+                continue
+            ffts = [(i, off) for (i, off) in reqs if not wl["conv"][i]]
+            cvs = [(i, off) for (i, off) in reqs if wl["conv"][i]]
+            n = [1 << int(wl["k"][i]) for i, _ in ffts]
+            in_off = [lane.pool[("fft", int(wl["k"][i]), i % pool_per_size)][0] // 2 for i, _ in ffts]
+            out_off = [off // 2 for _, off in ffts]
+            convs = [(int(wl["side"][i]), int(wl["side"][i]), int(wl["fid"][i]), tc.CONV_SAME,
+                      lane.pool[("img", int(wl["side"][i]), i % pool_per_size)][0], off) for i, off in cvs]
+            lane.q.submit(n, in_off, out_off, convs, lane.arena, lane.ring, lane.arena, lane.ring,
+                          stream=lane.stream)
+            launches += tc.last_launch_count()
+            with torch.cuda.stream(lane.stream):
+                lane.host_out[start:lane.head].copy_(lane.ring[start:lane.head], non_blocking=True)
+                ev = torch.cuda.Event(enable_timing=True)
+                ev.record(lane.stream)
+            lane.inflight.append((ev, start, lane.head, reqs))
+            busy_flops += sum(request_flops(wl, i, filters) for i, _ in reqs)
+            if verbose:
+                print("t=%.4f p=%d batch=%d" % (now, p, len(reqs)), file=sys.stderr)
+    t_end = max(lane.e0.elapsed_time(lane.inflight[-1][0]) * 1e-3 if lane.inflight else 0.0
+                for lane in lanes.values())
+    for lane in lanes.values():
+        lane.q.check(lane.stream)
+    wall = np.nanmax(lat + wl["arrival"]) - wl["arrival"][0]
+    return {"requests": nreq, "lat": lat, "samples": samples, "wall_s": wall, "launches": launches,
+            "hbm_resident_bytes": resident,
+            "flops": busy_flops, "wl": wl, "filters": filters, "lanes": lanes, "pool_per_size": pool_per_size,
+            "t_end": t_end}
+
+
+def errors(res, max_samples=60):
+    """Relative L2 vs the FP64 oracle for sampled requests, per precision."""
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
+    import pyoracle as orc
+    wl, filters, lanes = res["wl"], res["filters"], res["lanes"]
+    out = {(p, kind): [] for p in (tc.FP16, tc.SPLIT_FP32) for kind in ("fft", "conv")}
+    for i, y in res["samples"][:max_samples]:
+        p = int(wl["prec"][i])
+        lane = lanes[p]
+        j = i % res["pool_per_size"]
+        if wl["conv"][i]:
+            s = int(wl["side"][i])
+            img = lane.pool[("img", s, j)][1].astype(np.float64)
+            ref = orc.conv2d_same(img, filters[wl["fid"][i]].astype(np.float64))
+            out[(p, "conv")].append(orc.rel_l2(y[:s * s].reshape(s, s), ref))
+        else:
+            kk = int(wl["k"][i])
+            x = lane.pool[("fft", kk, j)][1].astype(np.float64)
+            ref = orc.fft1d(x[:, 0] + 1j * x[:, 1])
+            n = 1 << kk
+            yy = y[:2 * n].reshape(n, 2)
+            out[(p, "fft")].append(orc.rel_l2(yy[:, 0] + 1j * yy[:, 1], ref))
+    return out
+
+
+def summarize(res, errs):
+    lat = res["lat"]
+    ok = lat[~np.isnan(lat)]
+    worst = {"rel_l2_%s_%s_max" % ("fp16" if p == tc.FP16 else "split", kind): (float(max(v)) if v else None)
+             for (p, kind), v in errs.items()}
+    return {
+        **worst,
+        "requests": int(res["requests"]),
+        "req_per_s": float(len(ok) / res["wall_s"]),
+        "p50_ms": float(np.percentile(ok, 50) * 1e3),
+        "p99_ms": float(np.percentile(ok, 99) * 1e3),
+        "max_ms": float(ok.max() * 1e3),
+        "gflops": float(res["flops"] / res["wall_s"] / 1e9),
+        "launches": int(res["launches"]),
+        "hbm_resident_gb": float(res["hbm_resident_bytes"] / 1e9),
+        "error_samples": int(sum(len(v) for v in errs.values())),
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--rate", type=float, default=20000.0)
+    ap.add_argument("--seconds", type=float, default=1.0)
+    ap.add_argument("--seed", type=int, default=5)
+    ap.add_argument("--conv-fraction", type=float, default=0.5)
+    ap.add_argument("--hbm-cap-gb", type=float, default=60.0)
+    args = ap.parse_args()
+    res = run(args.rate, args.seconds, args.seed, args.conv_fraction, args.hbm_cap_gb)
+    out = summarize(res, errors(res))
+    out.update({"rate": args.rate, "seconds": args.seconds, "conv_fraction": args.conv_fraction,
+                "hbm_cap_gb": args.hbm_cap_gb})
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

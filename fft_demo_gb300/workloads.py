@@ -1,0 +1,211 @@
+"""The measured workloads besides the headline large-1D run of bench.py.
+
+  small    : N = 256, batch 4096, FP16, forward then inverse (scale 1/N) per
+             step; warm (one 4 MiB buffer, L2-resident) and cold (64 distinct
+             buffers, 256 MiB, rotated)
+  2d-conv  : FP16 2D FFT 1024 x 1024, batch 16; 'same' convolution of a
+             2048 x 2048 FP16 image (uniform[0,1]) with a 31 x 31 filter
+             (N(0,1) entries scaled to unit L1 norm), P = 4096
+  uneven   : 10,000 1D FFTs with n = 2^k, k uniform on [6, 16], plus 512
+             'same' convolutions (image side uniform over 64 .. 1024, filter
+             side over {3, 7, 15, 31}); split precision (FP32 storage) and
+             FP16; one persistent launch against the plain per-size path
+             (one launch chain per transform, one convolution plan per
+             convolution), with and without CUDA-graph replay
+  serving  : fft_demo_gb300/serve.py at 20k requests/s
+
+Each returns a dict for bench.py's JSON line. Inputs are seeded synthetic
+data of the stated shapes (no dataset is involved). Device time is taken
+with CUDA events on the launching stream after warm-up.
+"""
+import math
+import os
+import sys
+
+import numpy as np
+
+import fft_demo_gb300 as tc
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(os.path.dirname(HERE), "oracle"))
+
+
+def _timed(fn, reps, warm=3, stream=None):
+    import torch
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    s = torch.cuda.Event(enable_timing=True)
+    e = torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(reps):
+        fn()
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / reps
+
+
+def _f1d(n):
+    return 5.0 * n * math.log2(n)
+
+
+def small(peak_gbs):
+    import torch
+    import pyoracle as orc
+    n, b = 256, 4096
+    g = torch.Generator(device="cuda")
+    g.manual_seed(0)
+    bufs = [(torch.rand((b, n, 2), device="cuda", generator=g) * 2 - 1).half() for _ in range(64)]
+    outs = [torch.empty_like(x) for x in bufs]
+    fwd = tc.plan_1d(n, b)
+    res = {}
+    state = {"i": 0}
+
+    def step_cold():
+        i = state["i"] % 64
+        state["i"] += 1
+        fwd.exec(bufs[i], outs[i])
+        fwd.exec(outs[i], bufs[i], direction=tc.INVERSE, scale=1.0 / n)
+
+    def step_warm():
+        fwd.exec(bufs[0], outs[0])
+        fwd.exec(outs[0], bufs[0], direction=tc.INVERSE, scale=1.0 / n)
+
+    x0 = bufs[1].double().cpu().numpy()
+    fwd.exec(bufs[1], outs[1])
+    fwd.check()
+    y = outs[1].double().cpu().numpy()
+    xc = x0[..., 0] + 1j * x0[..., 1]
+    err_f = orc.rel_l2(y[..., 0] + 1j * y[..., 1], orc.fft1d(xc))
+    for name, fn in (("cold", step_cold), ("warm", step_warm)):
+        ms = _timed(fn, 200)
+        res[name] = {"ms_per_step": ms, "gflops": 2 * _f1d(n) * b / ms / 1e6,
+                     "gbs": 2 * 2 * n * b * 4 / ms / 1e6}
+    res["cold"]["hbm_frac"] = res["cold"]["gbs"] / peak_gbs
+    res["rel_l2_forward"] = err_f
+    fwd.exec(bufs[1], outs[1])
+    fwd.exec(outs[1], bufs[1], direction=tc.INVERSE, scale=1.0 / n)
+    fwd.check()
+    z = bufs[1].double().cpu().numpy()
+    res["rel_l2_roundtrip"] = orc.rel_l2(z[..., 0] + 1j * z[..., 1], xc)
+    return {"workload": "small-1d-fp16 N=256 batch=4096 forward+inverse", **res}
+
+
+def two_d_conv(peak_gbs):
+    import torch
+    import pyoracle as orc
+    out = {}
+    # 2D FFT 1024 x 1024, batch 16
+    nx = ny = 1024
+    b = 16
+    g = torch.Generator(device="cuda")
+    g.manual_seed(3)
+    x = (torch.rand((b, nx, ny, 2), device="cuda", generator=g) * 2 - 1).half()
+    y = torch.empty_like(x)
+    plan = tc.plan_2d(nx, ny, b)
+    ms = _timed(lambda: plan.exec(x, y), 50)
+    plan.check()
+    xs = x[:1].double().cpu().numpy()
+    ys = y[:1].double().cpu().numpy()
+    err = orc.rel_l2(ys[..., 0] + 1j * ys[..., 1], orc.fft2d(xs[..., 0] + 1j * xs[..., 1]))
+    gb = 2 * nx * ny * b * 4 / ms / 1e6
+    out["fft2d"] = {"ms": ms, "gflops": _f1d(nx * ny) * b / ms / 1e6, "gbs": gb, "hbm_frac": gb / peak_gbs,
+                    "launches": tc.last_launch_count(), "rel_l2": err}
+    # 'same' conv 2048 x 2048 with a 31 x 31 filter
+    s, f = 2048, 31
+    rng = np.random.default_rng(3)
+    w = rng.standard_normal((f, f))
+    w /= np.abs(w).sum()
+    img = torch.from_numpy(rng.uniform(0, 1, (1, 1, s, s)).astype(np.float32)).half().cuda()
+    conv = tc.Conv2d(1, 1, s, s, f, f, mode=tc.CONV_SAME, precision=tc.FP16)
+    conv.set_filters(torch.from_numpy(w.astype(np.float32).reshape(1, 1, f, f)).cuda())
+    res = torch.empty((1, 1, s, s), dtype=torch.float16, device="cuda")
+    ms = _timed(lambda: conv.exec(img, res), 20)
+    conv.check()
+    launches = 5  # row, column, pointwise, column, row passes
+    ref = orc.conv2d_same(img.double().cpu().numpy()[0, 0], w)
+    err = orc.rel_l2(res.double().cpu().numpy()[0, 0], ref)
+    p = 4096
+    flops = 2 * _f1d(p * p) + 6 * p * p
+    out["conv_same_2048_f31"] = {"ms": ms, "conv_per_s": 1e3 / ms, "gflops": flops / ms / 1e6, "padded": p,
+                                 "launches": launches, "rel_l2": err}
+    return {"workload": "2d-fft 1024x1024x16 fp16; conv same 2048^2 * 31^2 fp16", **out}
+
+
+def uneven(peak_gbs, count=10000, nconv=512, seed=4):
+    import torch
+    import pyoracle as orc
+    rng = np.random.default_rng(seed)
+    sizes = (1 << rng.integers(6, 17, count)).astype(np.int64)
+    sides = rng.choice([64, 128, 256, 512, 1024], nconv)
+    fsz = rng.choice([3, 7, 15, 31], nconv)
+    convs = [(int(a), int(a), int(c), int(c), tc.CONV_SAME) for a, c in zip(sides, fsz)]
+    filt_host = []
+    for c in fsz:
+        w = rng.standard_normal(c * c)
+        filt_host.append(w / np.abs(w).sum())
+    filt_host = np.concatenate(filt_host).astype(np.float32)
+    filters = torch.from_numpy(filt_host).cuda()
+    flops_1d = float(sum(_f1d(int(n)) for n in sizes))
+    flops_conv = 0.0
+    for a, c in zip(sides, fsz):
+        p = 64
+        while p < a + (c - 1) // 2:
+            p *= 2
+        flops_conv += 2 * _f1d(p * p) + 6 * p * p
+    out = {"count_1d": count, "count_conv": nconv}
+    for prec, name in ((tc.SPLIT_FP32, "split"), (tc.FP16, "fp16")):
+        dt = torch.float16 if prec == tc.FP16 else torch.float32
+        b = tc.Batch(sizes, precision=prec, convs=convs, filters=filters)
+        x = (torch.rand((b.total_in, 2), device="cuda") * 2 - 1).to(dt)
+        y = torch.zeros_like(x)
+        ci = torch.rand(b.conv_in_elems, device="cuda").to(dt)
+        co = torch.zeros(b.conv_out_elems, device="cuda", dtype=dt)
+        r = dict(b.info())
+        for mode, mname in ((tc.BATCH_PERSISTENT, "persistent"), (tc.BATCH_PER_SIZE, "per_size")):
+            b.set_mode(mode)
+            for graph in (False, True):
+                b.set_graph(graph)
+                ms = _timed(lambda: b.exec(x, y, ci, co), 3 if mode == tc.BATCH_PER_SIZE else 10)
+                r["%s_%s" % (mname, "graph" if graph else "eager")] = {
+                    "ms": ms, "gflops": (flops_1d + flops_conv) / ms / 1e6, "launches": tc.last_launch_count()}
+        b.set_mode(tc.BATCH_PERSISTENT)
+        b.set_graph(False)
+        b.exec(x, y, ci, co)
+        b.check()
+        # accuracy on a sample: 20 transforms and 6 convolutions
+        xh = x.double().cpu().numpy()
+        yh = y.double().cpu().numpy()
+        e1 = 0.0
+        for i in range(0, count, count // 20):
+            n = int(sizes[i])
+            xs = xh[b.in_off[i]:b.in_off[i] + n]
+            ys = yh[b.out_off[i]:b.out_off[i] + n]
+            e1 = max(e1, orc.rel_l2(ys[:, 0] + 1j * ys[:, 1], orc.fft1d(xs[:, 0] + 1j * xs[:, 1])))
+        cih = ci.double().cpu().numpy()
+        coh = co.double().cpu().numpy()
+        ec = 0.0
+        for k in range(0, nconv, nconv // 6):
+            (sy, sx), (oy, ox), io, oo, fo = b.conv_shapes[k]
+            fs = convs[k][2]
+            ref = orc.conv2d_same(cih[io:io + sy * sx].reshape(sy, sx),
+                                  filt_host[fo:fo + fs * fs].astype(np.float64).reshape(fs, fs))
+            ec = max(ec, orc.rel_l2(coh[oo:oo + oy * ox].reshape(oy, ox), ref))
+        r["rel_l2_1d_max"] = e1
+        r["rel_l2_conv_max"] = ec
+        r["speedup_vs_per_size_eager"] = r["per_size_eager"]["ms"] / r["persistent_eager"]["ms"]
+        r["speedup_vs_per_size_graph"] = r["per_size_graph"]["ms"] / r["persistent_graph"]["ms"]
+        out[name] = r
+        b.destroy()
+    return {"workload": "uneven batch: 10000 1D FFTs 2^6..2^16 + 512 same convs", **out}
+
+
+def serving(peak_gbs, rate=20000.0, seconds=1.0):
+    from fft_demo_gb300 import serve
+    res = serve.run(rate=rate, seconds=seconds)
+    out = serve.summarize(res, serve.errors(res))
+    return {"workload": "serving: Poisson %.0f req/s, %.1f s, 1D FFT 2^6..2^20 + same convs, FP16/split"
+            % (rate, seconds), **out}
+
+
+WORKLOADS = {"small": small, "2d-conv": two_d_conv, "uneven": uneven, "serving": serving}

@@ -201,6 +201,32 @@ tcfftStatus tcfft_batch_info(tcfftBatch batch, int *items, size_t *workspace_byt
 tcfftStatus tcfft_batch_check(tcfftBatch batch, void *stream);
 tcfftStatus tcfft_batch_destroy(tcfftBatch batch);
 
+/* ------------------------------------------------------------------------
+ * Serving queue (no counterpart in the reference): continuous batching of
+ * forward 1D FFTs (64 <= n <= 2^20) and 2D convolutions (filters from a
+ * resident pool, padded size <= 2048) into the persistent batch kernel.
+ * Tables, the filter pool and its spectra (made per padded size on first
+ * use), a workspace arena of workspace_bytes and two staging slots of
+ * staging_bytes stay resident; a submit builds the work list on the host,
+ * copies it with one async copy and launches once (twice when a filter
+ * spectrum is new). Submits share the workspace: one stream per queue.
+ * TCFFT_CAPACITY: the submit needs more workspace or staging; split it.
+ * ------------------------------------------------------------------------ */
+typedef struct tcfftQueueImpl *tcfftQueue;
+typedef struct tcfftQueueConv {
+  int sy, sx, filter_id, mode;
+  long long img_off, out_off; /* real elements in conv_in / conv_out */
+} tcfftQueueConv;
+tcfftStatus tcfft_queue_create(tcfftQueue *queue, int precision, size_t workspace_bytes, size_t staging_bytes);
+/* Adds filter `id` (fy x fx floats, host or device; copied). */
+tcfftStatus tcfft_queue_set_filter(tcfftQueue queue, int id, const float *filter, int fy, int fx);
+tcfftStatus tcfft_queue_submit(tcfftQueue queue, int count, const long long *n, const long long *in_off,
+                               const long long *out_off, const float *scale, int nconv,
+                               const tcfftQueueConv *convs, const void *in, void *out, const void *conv_in,
+                               void *conv_out, void *stream);
+tcfftStatus tcfft_queue_check(tcfftQueue queue, void *stream);
+tcfftStatus tcfft_queue_destroy(tcfftQueue queue);
+
 /* Last status returned on this thread, and a readable name for a status. */
 tcfftStatus tcfft_get_last_error(void);
 const char *tcfft_status_string(tcfftStatus status);
