@@ -56,6 +56,7 @@ def _declare(L):
         "tcfft_plan_set_fused": (i, [vp, i]),
         "tcfft_tune_set": (i, [i, i, i, i]),
         "tcfft_tune_get": (i, [i, i, i, ctypes.POINTER(i)]),
+        "tcfft_tune_split": (i, [i, i, i]),
         "tcfft_pass_info": (i, [i, i, i, i, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)]),
         "tcfft_exec": (i, [vp, vp, vp, i, f, vp]),
         "tcfft_exec_digitrev": (i, [vp, vp, vp, ctypes.POINTER(i), i, vp]),

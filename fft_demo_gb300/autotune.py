@@ -7,6 +7,9 @@ CUDA events, keeps the fastest and writes the choices to a JSON cache keyed by
 device name, precision, pass kind and log2 of the pass length. Loading the
 cache re-applies the choices through tcfft_tune_set.
 
+For four-step sizes tune_split also searches the column/row split (the
+radix schedule of the two passes), tuning both passes' tiles per split.
+
 Cache path: $TCFFT_TUNE_CACHE, default ~/.cache/tcfft_gb300/tune.json.
 """
 import ctypes
@@ -31,8 +34,9 @@ def _device_name():
     return torch.cuda.get_device_name(0)
 
 
-def passes_of(n, precision, dims=1, shape2d=None):
-    """(pass kind, log2 length) of each pass the library runs for a transform."""
+def passes_of(n, precision, dims=1, shape2d=None, split=None):
+    """(pass kind, log2 length) of each pass the library runs for a transform
+    (split: the four-step column-pass log2 length, None = built-in)."""
     if dims == 2:
         nx, ny = shape2d
         return [(PASS_ROW, int(math.log2(ny))), (PASS_COL, int(math.log2(nx)))]
@@ -44,7 +48,54 @@ def passes_of(n, precision, dims=1, shape2d=None):
     a = min(logn // 2, 10)
     if logn - a > pass_max:
         a = logn - pass_max
+    if split is not None:
+        a = split
     return [(PASS_COL, a), (PASS_ROWT, logn - a)]
+
+
+def set_split(precision, logn, log_n1):
+    _check(lib().tcfft_tune_split(precision, logn, log_n1), "tune_split")
+
+
+def tune_split(n, batch, precision=FP16, candidates=None, reps=10, verbose=False):
+    """Four-step sizes: try every column/row split whose passes have kernels,
+    tune the tiles of both passes for each, keep the fastest. Returns
+    (log_n1, {(kind, logl): tile}, ms)."""
+    import torch
+    logn = int(math.log2(n))
+    pass_max = 12 if precision == FP16 else 11
+    if candidates is None:
+        candidates = [a for a in range(4, 13) if logn - a <= pass_max and logn - a >= 4]
+    dt = torch.float16 if precision == FP16 else torch.float32
+    x = (torch.rand((n * batch, 2), device="cuda") * 2 - 1).to(dt)
+    y = torch.empty_like(x)
+    best = (None, None, float("inf"))
+    for a in candidates:
+        if lib().tcfft_tune_split(precision, logn, a) != 0:
+            continue
+        choices = {}
+        plan = plan_1d(n, batch, precision)
+        for kind, logl in passes_of(n, precision, split=a):
+            bt, bms = None, float("inf")
+            for t in variants(precision, kind, logl):
+                set_tile(precision, kind, logl, t)
+                ms = _time_exec(plan, x, y, reps)
+                if ms < bms:
+                    bt, bms = t, ms
+            set_tile(precision, kind, logl, bt)
+            choices[(kind, logl)] = bt
+        ms = _time_exec(plan, x, y, reps)
+        plan.destroy()
+        if verbose:
+            print("  split 2^%d x 2^%d: %.4f ms %s" % (a, logn - a, ms, choices))
+        if ms < best[2]:
+            best = (a, choices, ms)
+        for kind, logl in passes_of(n, precision, split=a):
+            set_tile(precision, kind, logl, -1)
+    set_split(precision, logn, best[0])
+    for (kind, logl), t in best[1].items():
+        set_tile(precision, kind, logl, t)
+    return best
 
 
 def variants(precision, kind, logl):
@@ -104,7 +155,7 @@ def tune(n, batch, precision=FP16, shape2d=None, reps=10, verbose=False):
     return chosen
 
 
-def save(choices, precision, path=None):
+def save(choices, precision, path=None, splits=None):
     path = path or cache_path()
     data = {}
     if os.path.exists(path):
@@ -115,6 +166,8 @@ def save(choices, precision, path=None):
     dev = data.setdefault(_device_name(), {})
     for (kind, logl), tile in choices.items():
         dev["%d/%d/%d" % (precision, kind, logl)] = tile
+    for logn, a in (splits or {}).items():
+        dev["split/%d/%d" % (precision, logn)] = a
     os.makedirs(os.path.dirname(path), exist_ok=True)
     with open(path, "w") as f:
         json.dump(data, f, indent=1, sort_keys=True)
@@ -132,8 +185,13 @@ def load(path=None):
         return 0
     lib().tcfft_tune_set.argtypes = [ctypes.c_int] * 4
     n = 0
-    for key, tile in data.items():
-        prec, kind, logl = (int(v) for v in key.split("/"))
-        if lib().tcfft_tune_set(prec, kind, logl, int(tile)) == 0:
+    for key, val in data.items():
+        parts = key.split("/")
+        if parts[0] == "split":
+            if lib().tcfft_tune_split(int(parts[1]), int(parts[2]), int(val)) == 0:
+                n += 1
+            continue
+        prec, kind, logl = (int(v) for v in parts)
+        if lib().tcfft_tune_set(prec, kind, logl, int(val)) == 0:
             n += 1
     return n

@@ -41,11 +41,24 @@ int g_num_sms = 0;
 // Tile variant per (precision, pass kind, log2 length); -1 = built-in choice.
 // Written by tcfft_tune_set (the autotuner), read at every launch.
 int g_tune[kNumPrec][kNumPassKinds][kMaxLogL + 1];
+// Four-step split per (precision, log2 n): log2 of the column-pass length,
+// -1 = built-in choice. Written by tcfft_tune_split, read at plan creation.
+constexpr int kMaxLogN = 24;
+int g_split[kNumPrec][kMaxLogN + 1];
 std::once_flag g_tune_once;
 void tune_reset() {
   for (auto& a : g_tune)
     for (auto& b : a)
       for (int& c : b) c = -1;
+  for (auto& a : g_split)
+    for (int& c : a) c = -1;
+}
+
+bool pass_built(int prec, int kind, int logl) {
+  if (logl < 0 || logl > kMaxLogL) return false;
+  for (int t = 0; t < kNumTileSel; ++t)
+    if (g_tab[prec][kind][logl][t][0].fn) return true;
+  return false;
 }
 
 void init_registry() {
@@ -455,6 +468,10 @@ tcfftStatus tcfft_plan_1d(tcfftPlan* plan, long long n, long long batch, int pre
       // column pass length 2^a, row pass length 2^(logn - a), both <= 2^pass_max
       int a = logn / 2 < 10 ? logn / 2 : 10;
       if (logn - a > pass_max) a = logn - pass_max;
+      std::call_once(g_tune_once, tune_reset);
+      const int pr = precision == TCFFT_FP16 ? kPrecF16 : kPrecSplit;
+      const int tuned = g_split[pr][logn];
+      if (tuned >= 0 && pass_built(pr, kPassCol, tuned) && pass_built(pr, kPassRowT, logn - tuned)) a = tuned;
       p->log_n1 = a;
       p->log_n2 = logn - a;
       s = ensure_twiddle(p, p->log_n1);
@@ -715,6 +732,18 @@ tcfftStatus tcfft_tune_set(int precision, int pass_kind, int log2_len, int tile)
   if (s != TCFFT_OK) return ret(s);
   if (tile >= 0 && !g_tab[precision][pass_kind][log2_len][tile][0].fn) return ret(TCFFT_UNSUPPORTED);
   g_tune[precision][pass_kind][log2_len] = tile;
+  return ret(TCFFT_OK);
+}
+
+tcfftStatus tcfft_tune_split(int precision, int log2_n, int log2_n1) {
+  if (precision < 0 || precision >= kNumPrec || log2_n < 0 || log2_n > kMaxLogN || log2_n1 < -1)
+    return ret(TCFFT_INVALID_VALUE);
+  std::call_once(g_tune_once, tune_reset);
+  tcfftStatus s = ensure_init();
+  if (s != TCFFT_OK) return ret(s);
+  if (log2_n1 >= 0 && (!pass_built(precision, kPassCol, log2_n1) || !pass_built(precision, kPassRowT, log2_n - log2_n1)))
+    return ret(TCFFT_UNSUPPORTED);
+  g_split[precision][log2_n] = log2_n1;
   return ret(TCFFT_OK);
 }
 

@@ -193,12 +193,20 @@ __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const f
   constexpr bool LAST = (s == Sh::S - 1);
 #pragma unroll 1
   for (int grp = warp >> 2; grp < NG; grp += kPassThreads / 128) {
-    uint32_t d[32];
-    tmem_ld_x32(tbase + (static_cast<uint32_t>(32 * (warp & 3)) << 16) + grp * 32u, d);
-    tmem_ld_wait();
     const int m = grp * 128 + 32 * (warp & 3) + lane;
     int g, j;
     Tl::unpos(m, g, j);
+    // twiddle reads of the next stage issued before the TMEM load, so their
+    // latency overlaps it (they depend on the row only)
+    float2 w_pre = make_float2(1.f, 0.f), wstep_pre = make_float2(1.f, 0.f);
+    if constexpr (!LAST) {
+      const int rp_ = ((j / Ns) * 16 * Ns + j % Ns) / J;
+      w_pre = __ldg(tw + rp_ * (j % Ns) * (L / (256 * Ns)));
+      wstep_pre = __ldg(tw + rp_ * (L / 256));
+    }
+    uint32_t d[32];
+    tmem_ld_x32(tbase + (static_cast<uint32_t>(32 * (warp & 3)) << 16) + grp * 32u, d);
+    tmem_ld_wait();
     if constexpr (LAST) {
       // final outputs X[j + c*J] of line line0 + g
       const long long line = line0 + g;
@@ -226,16 +234,15 @@ __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const f
       const int rp = lp0 / J;
       const int jp0 = lp0 % J;
       // twiddle of the next stage: W_{256 Ns}^{r' (c Ns + b)} = W_L^{e0 + c*de}
-      const int e0 = rp * b * (L / (256 * Ns));
-      const int de = rp * (L / 256);
+      // with e0 = r' b L / (256 Ns), de = r' L / 256 (read above as w_pre, wstep_pre)
       const uint32_t krow = (static_cast<uint32_t>(rp) >> 3) * Tl::KSTRIDE + (rp & 7) * 128u;
       if constexpr (Ns == 1 && !LINE_MINOR) {
         // 16 outputs -> 16 consecutive columns: two 16-byte stores per plane
         uint32_t pr[8], pi[8];
         // twiddles by recurrence: two table reads per row (FP32 error ~1e-6,
         // far below the FP16 rounding that follows)
-        float2 w = __ldg(tw + e0);
-        const float2 wstep = __ldg(tw + de);
+        float2 w = w_pre;
+        const float2 wstep = wstep_pre;
 #pragma unroll
         for (int c = 0; c < 16; c += 2) {
           const float2 w0 = w;
@@ -261,8 +268,8 @@ __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const f
         *reinterpret_cast<uint4*>(re + off1) = sw ? rlo : rhi;
         *reinterpret_cast<uint4*>(im + off1) = sw ? ilo : ihi;
       } else {
-        float2 w = __ldg(tw + e0);
-        const float2 wstep = __ldg(tw + de);
+        float2 w = w_pre;
+        const float2 wstep = wstep_pre;
         // column step between consecutive outputs: Ns (line-major) or Ns*G
         // (line-minor); when it is a multiple of 64 (one swizzle atom) the
         // swizzled offset moves by a compile-time amount per output
@@ -276,6 +283,24 @@ __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const f
             const float2 x = cmulf(make_float2(__uint_as_float(d[c]), __uint_as_float(d[16 + c])), w);
             w = cmulf(w, wstep);
             st_pair(re, im, off0 + static_cast<uint32_t>(c) * (CSTEP / 64u) * 1024u, x);
+          }
+        } else if constexpr (CSTEP >= 8 && (CSTEP & (CSTEP - 1)) == 0) {
+          // the column moves by CSTEP < 64 per output: the swizzled offsets
+          // repeat with period PER = 64 / CSTEP, shifted by one 1 KiB atom
+          // per period, so PER offsets computed once serve all 16 outputs
+          constexpr int PER = static_cast<int>(64u / CSTEP);
+          const uint32_t mp0 = static_cast<uint32_t>(Tl::pos(g, jp0));
+          uint32_t offs[PER];
+#pragma unroll
+          for (int k = 0; k < PER; ++k) {
+            const uint32_t mp = mp0 + static_cast<uint32_t>(k) * CSTEP;
+            offs[k] = krow + (mp >> 6) * 1024u + ((((mp & 63u) >> 3) ^ (rp & 7)) << 4) + (mp & 7u) * 2u;
+          }
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            const float2 x = cmulf(make_float2(__uint_as_float(d[c]), __uint_as_float(d[16 + c])), w);
+            w = cmulf(w, wstep);
+            st_pair(re, im, offs[c % PER] + static_cast<uint32_t>(c / PER) * 1024u, x);
           }
         } else {
 #pragma unroll

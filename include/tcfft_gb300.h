@@ -245,6 +245,11 @@ typedef enum tcfftTile { TCFFT_TILE_SMALL = 0, TCFFT_TILE_BIG = 1, TCFFT_TILE_MI
 /* tile = -1 restores the built-in choice. */
 tcfftStatus tcfft_tune_set(int precision, int pass_kind, int log2_len, int tile);
 tcfftStatus tcfft_tune_get(int precision, int pass_kind, int log2_len, int *tile);
+/* Four-step split for 1D plans of 2^log2_n points made after this call:
+ * column passes of 2^log2_n1 points, then transposing passes of
+ * 2^(log2_n - log2_n1); -1 restores the built-in choice. TCFFT_UNSUPPORTED
+ * when either pass length has no kernel. */
+tcfftStatus tcfft_tune_split(int precision, int log2_n, int log2_n1);
 /* Geometry of a pass variant: lines per tile, co-resident CTAs per SM, SMs. */
 tcfftStatus tcfft_pass_info(int precision, int pass_kind, int log2_len, int tile, int *lines_per_tile,
                             int *ctas_per_sm, int *num_sms);
