@@ -212,10 +212,24 @@ def run_reference(args, world, rank):
     return 0
 
 
+TUNING = os.path.join(REPO, "fft_demo_gb300", "tuning", "gb300.json")
+
+
+def load_tuning():
+    """Apply the tile and four-step-split choices the autotuner measured on
+    GB300 (python -m fft_demo_gb300.autotune --out fft_demo_gb300/tuning/gb300.json)."""
+    try:
+        from fft_demo_gb300 import autotune
+        return autotune.load(TUNING)
+    except Exception:
+        return 0
+
+
 def run_case(spec):
     """A small, fixed workload for ncu: REPS execs of one plan on seeded data."""
     import torch
     import fft_demo_gb300 as tc
+    load_tuning()
     parts = spec.split(",")
     n, batch = int(parts[0]), int(parts[1])
     reps = int(parts[2]) if len(parts) > 2 else 3
@@ -252,6 +266,7 @@ def main():
     if args.case:
         return run_case(args.case)
     if args.workload != "large-1d":
+        load_tuning()
         from fft_demo_gb300 import workloads
         peak, kind = load_peaks()
         res = workloads.WORKLOADS[args.workload](peak)
@@ -263,6 +278,7 @@ def main():
     world, rank, local = dist_init()
     if args.impl == "reference":
         return run_reference(args, world, rank)
+    tuned = load_tuning()
 
     import numpy as np
     import torch
@@ -393,7 +409,8 @@ def main():
             "data": "synthetic uniform[-1,1] (seeded), inputs larger than L2 (1 GiB per size)",
             "config": {"workload": "large-1d-fp16", "sizes": [[n, b] for n, b in SIZES],
                        "precision": "fp16 storage, fp32 accumulate", "l2": "inputs > L2",
-                       "step_bytes_algorithmic": step_bytes},
+                       "step_bytes_algorithmic": step_bytes,
+                       "tuning": "fft_demo_gb300/tuning/gb300.json (%d entries)" % tuned},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak_gbs, "unit": "GB/s",
                          "frac": achieved / peak_gbs, "traffic": traffic,
                          "kernel": "N=%d transform (%d launch%s)" % (

@@ -100,7 +100,7 @@ def tune_split(n, batch, precision=FP16, candidates=None, reps=10, verbose=False
 
 def variants(precision, kind, logl):
     out = []
-    for t in (TILE_SMALL, TILE_BIG, TILE_MID):
+    for t in TILE_NAMES:
         g, c, s = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         st = lib().tcfft_pass_info(precision, kind, logl, t, ctypes.byref(g), ctypes.byref(c),
                                    ctypes.byref(s))
@@ -195,3 +195,40 @@ def load(path=None):
         if lib().tcfft_tune_set(prec, kind, logl, int(val)) == 0:
             n += 1
     return n
+
+
+def main():
+    """Tune the common sizes and write a tuning file:
+    python -m fft_demo_gb300.autotune [--out PATH] [--quick]"""
+    import argparse
+    import torch
+    from . import SPLIT_FP32
+    ap = argparse.ArgumentParser(description="tune tile variants and four-step splits on this GPU")
+    ap.add_argument("--out", default=None, help="tuning file (default: the per-user cache)")
+    ap.add_argument("--quick", action="store_true", help="fewer sizes (the bench's)")
+    args = ap.parse_args()
+    gib = 1 << 28  # FP16 complex elements per GiB
+    rows = [8, 10, 12] if args.quick else list(range(6, 15))
+    fours = [16, 20] if args.quick else list(range(15, 21))
+    results = {FP16: ({}, {}), SPLIT_FP32: ({}, {})}
+    for logn in rows:
+        n = 1 << logn
+        ch = tune(n, gib // n, FP16, reps=10)
+        results[FP16][0].update(ch)
+        print("FP16 2^%d:" % logn, {TILE_NAMES[t]: k for k, t in ch.items()}, flush=True)
+    for prec, per in ((FP16, gib), (SPLIT_FP32, gib // 2)):
+        for logn in fours:
+            n = 1 << logn
+            a, ch, ms = tune_split(n, per // n, prec, reps=10)
+            results[prec][0].update(ch)
+            results[prec][1][logn] = a
+            print("%s 2^%d: split 2^%d x 2^%d, %.4f ms" % ("FP16" if prec == FP16 else "split", logn, a,
+                                                            logn - a, ms), flush=True)
+    for prec, (ch, sp) in results.items():
+        path = save(ch, prec, args.out, splits=sp)
+    print("wrote", path)
+    torch.cuda.synchronize()
+
+
+if __name__ == "__main__":
+    main()

@@ -82,6 +82,21 @@ def small(peak_gbs):
         res[name] = {"ms_per_step": ms, "gflops": 2 * _f1d(n) * b / ms / 1e6,
                      "gbs": 2 * 2 * n * b * 4 / ms / 1e6}
     res["cold"]["hbm_frac"] = res["cold"]["gbs"] / peak_gbs
+    # the same 64 cold steps captured once in a CUDA graph and replayed
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        step_cold()  # warm the plan outside the capture
+    torch.cuda.current_stream().wait_stream(side)
+    state["i"] = 0
+    with torch.cuda.graph(graph):
+        for _ in range(64):
+            step_cold()
+    ms = _timed(graph.replay, 20) / 64
+    res["cold_graph"] = {"ms_per_step": ms, "gflops": 2 * _f1d(n) * b / ms / 1e6,
+                         "gbs": 2 * 2 * n * b * 4 / ms / 1e6, "launches_per_step": 2}
+    res["cold_graph"]["hbm_frac"] = res["cold_graph"]["gbs"] / peak_gbs
     res["rel_l2_forward"] = err_f
     fwd.exec(bufs[1], outs[1])
     fwd.exec(outs[1], bufs[1], direction=tc.INVERSE, scale=1.0 / n)

@@ -241,7 +241,11 @@ int tcfft_last_launch_count(void);
  * (precision, pass kind, log2 of the pass length) is process-wide state.
  * ------------------------------------------------------------------------ */
 typedef enum tcfftPassKind { TCFFT_PASS_ROW = 0, TCFFT_PASS_COL = 1, TCFFT_PASS_ROWT = 2 } tcfftPassKind;
-typedef enum tcfftTile { TCFFT_TILE_SMALL = 0, TCFFT_TILE_BIG = 1, TCFFT_TILE_MID = 2 } tcfftTile;
+typedef enum tcfftTile {
+  TCFFT_TILE_SMALL = 0,  /* 128 MMA rows per tile */
+  TCFFT_TILE_BIG = 1,    /* 1024 rows */
+  TCFFT_TILE_MID = 2     /* 512 rows, next tile prefetched, 3 CTAs/SM */
+} tcfftTile;
 /* tile = -1 restores the built-in choice. */
 tcfftStatus tcfft_tune_set(int precision, int pass_kind, int log2_len, int tile);
 tcfftStatus tcfft_tune_get(int precision, int pass_kind, int log2_len, int *tile);

@@ -18,7 +18,7 @@ PASS_ROW, PASS_COL, PASS_ROWT = 0, 1, 2
 
 def _variants(tc, kind, logl):
     out = []
-    for t in (0, 1, 2):
+    for t in range(3):  # small, big, mid (prefetching)
         g, c, s = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         if tc.lib().tcfft_pass_info(0, kind, logl, t, ctypes.byref(g), ctypes.byref(c), ctypes.byref(s)) == 0:
             out.append(t)
@@ -56,8 +56,10 @@ def test_four_step_tile_variants(tc, orc, n):
     ref = orc.fft1d(x)
     logn = n.bit_length() - 1
     a = min(logn // 2, 10)
+    tiles = sorted(set(_variants(tc, PASS_COL, a)) & set(_variants(tc, PASS_ROWT, logn - a)))
+    assert len(tiles) >= 2
     try:
-        for t in (1, 2):
+        for t in tiles:
             assert tc.lib().tcfft_tune_set(0, PASS_COL, a, t) == 0
             assert tc.lib().tcfft_tune_set(0, PASS_ROWT, logn - a, t) == 0
             plan = tc.plan_1d(n, batch)
@@ -91,3 +93,30 @@ def test_2d_col_tile_variants(tc, orc):
     finally:
         tc.lib().tcfft_tune_set(0, PASS_COL, 9, -1)
         tc.lib().tcfft_tune_set(0, PASS_ROW, 10, -1)
+
+
+@pytest.mark.parametrize("n,splits", [(1 << 16, (6, 7, 9, 10)), (1 << 20, (9, 11))])
+def test_four_step_splits(tc, orc, n, splits):
+    """Tuned column/row splits (tcfft_tune_split) give the same transform;
+    the fused one-launch form is only offered for the built-in split."""
+    batch = 3
+    rng = np.random.default_rng(9)
+    x = f16_round(uniform_complex(rng, (batch, n)))
+    ref = orc.fft1d(x)
+    logn = n.bit_length() - 1
+    try:
+        for a in splits:
+            assert tc.lib().tcfft_tune_split(0, logn, a) == 0
+            plan = tc.plan_1d(n, batch)
+            with pytest.raises(tc.TcfftError):
+                plan.set_fused(True)
+            d = to_dev_f16(x)
+            out = to_dev_f16(np.zeros_like(x))
+            plan.exec(d, out)
+            plan.check()
+            err = orc.rel_l2(from_dev_f16(out), ref)
+            assert err < REL_L2_FP16, (a, err)
+            plan.destroy()
+    finally:
+        tc.lib().tcfft_tune_split(0, logn, -1)
+    assert tc.lib().tcfft_tune_split(0, logn, 3) == tc.UNSUPPORTED  # 2^3-point column pass: no kernel
