@@ -7,6 +7,7 @@
 // FFT of length L <= 2^14 on tiles held in shared memory; sizes above 2^14
 // use the four-step split N = N1 * N2 (column pass with outer twiddle, then a
 // transposing row pass), so every transform is at most two HBM round trips.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -223,11 +224,50 @@ void free_plan(tcfftPlanImpl* p) {
 }
 
 // Launch one pass; grid = persistent CTAs (at most the co-resident count).
+// 3D tensor map over column-layout lines: x = line within its sequence
+// (lines adjacent in memory), y = element (stride elem_stride), z = sequence
+// (stride seq_stride); 4-byte elements, boxes of G lines x min(L, 256)
+// elements. False when the layout breaks a TMA rule (the caller keeps the
+// cp.async path then).
+bool encode_column_map(CUtensorMap* map, const void* base, long long lines_per_seq, long long nseq, int L,
+                       long long elem_stride, long long seq_stride, int G) {
+  if ((reinterpret_cast<uintptr_t>(base) & 15u) || (elem_stride * 4) % 16 || (seq_stride * 4) % 16 || (G * 4) % 16)
+    return false;
+  const cuuint64_t dims[3] = {static_cast<cuuint64_t>(lines_per_seq), static_cast<cuuint64_t>(L),
+                              static_cast<cuuint64_t>(nseq)};
+  const cuuint64_t strides[2] = {static_cast<cuuint64_t>(elem_stride * 4), static_cast<cuuint64_t>(seq_stride * 4)};
+  const cuuint32_t box[3] = {static_cast<cuuint32_t>(G), static_cast<cuuint32_t>(L < 256 ? L : 256), 1u};
+  const cuuint32_t estr[3] = {1u, 1u, 1u};
+  return cuTensorMapEncodeTiled(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, const_cast<void*>(base), dims, strides, box,
+                                estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Prefetching (mid-tile) kernels move column-layout tiles by TMA when every
+// tile lies inside one sequence.
 template <class IO>
-tcfftStatus launch_pass(int prec, int kind, int logL, int tile, int sign_idx, const IO& io, const PassCore& core,
+void attach_tensor_maps(IO& io, int kind, int tile, int logL, int G) {
+  if constexpr (TensorMapIo<IO>) {
+    io.in_tma = io.out_tma = false;
+    if (tile != kTileMid || kind == kPassRow) return;
+    const long long lps = 1ll << io.lps_log2;
+    if (lps % G != 0 || io.total_lines % lps != 0 || G % 4 != 0) return;
+    const long long nseq = io.total_lines / lps;
+    const int L = 1 << logL;
+    if (!IO::IN_VEC_L && io.in_line == 1)
+      io.in_tma = encode_column_map(&io.in_map, io.in, lps, nseq, L, io.in_elem, io.in_seq, G);
+    if (!IO::OUT_VEC_L && io.out_line == 1)
+      io.out_tma = encode_column_map(&io.out_map, io.out, lps, nseq, L, io.out_elem, io.out_seq, G);
+  }
+}
+
+template <class IO>
+tcfftStatus launch_pass(int prec, int kind, int logL, int tile, int sign_idx, const IO& io_in, const PassCore& core,
                         cudaStream_t stream) {
   const PassKernel& pk = g_tab[prec][kind][logL][tile][sign_idx];
   if (!pk.fn) return TCFFT_UNSUPPORTED;
+  IO io = io_in;
+  attach_tensor_maps(io, kind, tile, logL, pk.G);
   const long long ntiles = (io.total_lines + pk.G - 1) / pk.G;
   long long grid = static_cast<long long>(g_num_sms) * g_occ[prec][kind][logL][tile][sign_idx];
   if (grid < 1) grid = 1;

@@ -168,6 +168,16 @@ struct IoLines {
   __device__ __forceinline__ E* tile_dst(long long) const { return out; }
 };
 
+// The batch kernel moves its tiles itself (no tensor maps): clear the flags
+// of IO policies that have them.
+template <class IO>
+__device__ __forceinline__ void clear_tensor_flags(IO& io) {
+  if constexpr (TensorMapIo<IO>) {
+    io.in_tma = false;
+    io.out_tma = false;
+  }
+}
+
 template <bool SPLIT>
 struct BatchPrec;
 
@@ -224,6 +234,7 @@ __device__ __noinline__ bool batch_p1_item(typename BatchPrec<SPLIT>::State& st,
   const BatchXform xf = a.xforms[it.obj];
   const long long n = 1ll << xf.logn, n2 = 1ll << xf.log_n2;
   typename P::template Io<false, false, false> io;
+  clear_tensor_flags(io);
   io.in = static_cast<const E*>(a.in) + xf.in_off;
   io.out = static_cast<E*>(a.ws) + xf.ws_off;
   io.total_lines = n2;
@@ -246,6 +257,7 @@ __device__ __noinline__ bool batch_p2_item(typename BatchPrec<SPLIT>::State& st,
   const BatchXform xf = a.xforms[it.obj];
   const long long n = 1ll << xf.logn, n1 = 1ll << xf.log_n1, n2 = 1ll << xf.log_n2;
   typename P::template Io<true, false, true> io;
+  clear_tensor_flags(io);
   io.in = static_cast<const E*>(a.ws) + xf.ws_off;
   io.out = static_cast<E*>(a.out) + xf.out_off;
   io.total_lines = n1;

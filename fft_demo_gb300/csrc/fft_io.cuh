@@ -12,6 +12,7 @@
 //   void decode_l(raw, line, l0, v[4]) / decode_g(...)   (to FP32)
 //   void store_row16(line, j, J, v[16])   (outputs l = j + c*J, c = 0..15)
 #pragma once
+#include <cuda.h>
 #include <cuda_fp16.h>
 #include <cstdint>
 
@@ -89,6 +90,13 @@ struct IoHalf {
   // tile of lines moves as one bulk copy. Set by the host.
   bool in_contig, out_contig;
   long long contig_len;  // L
+  // Column-layout tiles (lines adjacent in memory, in_line / out_line == 1)
+  // moved by TMA through 3D tensor maps: x = line within its sequence,
+  // y = element of the line, z = sequence; 4-byte elements. Set by the host
+  // for the prefetching kernels only (the kernel parameter is
+  // __grid_constant__, so the maps stay in parameter space).
+  bool in_tma, out_tma;
+  CUtensorMap in_map, out_map;
 
   __device__ __forceinline__ const half2* tile_src(long long line0) const { return in + line0 * contig_len; }
   __device__ __forceinline__ half2* tile_dst(long long line0) const { return out + line0 * contig_len; }
@@ -126,6 +134,24 @@ struct IoHalf {
   }
   __device__ __forceinline__ void decode_g(const Raw& r, long long, int, float2 (&v)[4]) const {
     unpack_h2x4(r, v);
+  }
+  // The outer twiddle and scale store_row16 applies, in place (for outputs
+  // that go out through a staged tensor store instead).
+  __device__ __forceinline__ void prepare_row16(long long line, int j, int J, float2 (&v)[16]) const {
+    if (otw.hi) {
+      const long long li = line & ((1ll << lps_log2) - 1);
+      float2 w = otw(li, j);
+      const float2 step = otw(li, J);
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        v[c] = cmulf(v[c], w);
+        w = cmulf(w, step);
+      }
+    }
+    if (scale != 1.0f) {
+#pragma unroll
+      for (int c = 0; c < 16; ++c) v[c] = make_float2(v[c].x * scale, v[c].y * scale);
+    }
   }
   // Outputs l = j + c*J (c = 0..15) of one line. The outer twiddle
   // W_N^{li*l} is formed as W_N^{li*j} * (W_N^{li*J})^c (FP32 recurrence).

@@ -67,6 +67,15 @@ struct PassCore {
   int* err;
 };
 
+// IO policies that can move column-layout tiles by TMA tensor maps.
+template <class IO>
+concept TensorMapIo = requires(const IO& io) {
+  io.in_tma;
+  io.out_tma;
+  io.in_map;
+  io.out_map;
+};
+
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
@@ -214,6 +223,7 @@ __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const f
         float2 v[16];
 #pragma unroll
         for (int c = 0; c < 16; ++c) v[c] = make_float2(__uint_as_float(d[c]), __uint_as_float(d[16 + c]));
+        bool staged = false;
         if (stage_out) {
           // natural-order half2 copy of the tile for the bulk store
           uint32_t* row = reinterpret_cast<uint32_t*>(re) + static_cast<uint32_t>(g) * L + j;
@@ -222,9 +232,23 @@ __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const f
             __half2 h = __floats2half2_rn(v[c].x * io.scale, v[c].y * io.scale);
             row[c * J] = *reinterpret_cast<uint32_t*>(&h);
           }
-        } else {
-          io.store_row16(line, j, J, v);
+          staged = true;
         }
+        if constexpr (TensorMapIo<IO> && LINE_MINOR) {
+          if (io.out_tma) {
+            // column-layout copy of the tile (element (g, l) at l * G + g)
+            // for the tensor store the kernel issues after the stages
+            io.prepare_row16(line, j, J, v);
+            uint32_t* col = reinterpret_cast<uint32_t*>(re) + g;
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+              __half2 h = __floats2half2_rn(v[c].x, v[c].y);
+              col[(j + c * J) * G] = *reinterpret_cast<uint32_t*>(&h);
+            }
+            staged = true;
+          }
+        }
+        if (!staged) io.store_row16(line, j, J, v);
       }
     } else {
       // output c goes to l' = (j / Ns) * 16Ns + c*Ns + (j % Ns); all 16 land in
@@ -701,6 +725,22 @@ __device__ __forceinline__ void prefetch_tile(PassState& st, const IO& io, long 
       bulk_g2s(raw, io.tile_src(line0), bytes, st.tma_bar);
     }
   } else if constexpr (!IO::IN_VEC_L) {
+    if constexpr (TensorMapIo<IO>) {
+      if (io.in_tma) {
+        // one [L x G] box as L / 256 tensor loads (the host only sets the
+        // map when tiles never straddle a sequence)
+        if (threadIdx.x == 0) {
+          constexpr int BY = L < 256 ? L : 256;
+          mbar_arrive_expect_tx(st.tma_bar, static_cast<uint32_t>(G) * L * 4u);
+          const int seq = static_cast<int>(line0 >> io.lps_log2);
+          const int x0 = static_cast<int>(line0 & ((1ll << io.lps_log2) - 1));
+#pragma unroll
+          for (int r0 = 0; r0 < L; r0 += BY)
+            tma_load_3d(raw + static_cast<uint32_t>(r0) * G * 4u, &io.in_map, x0, r0, seq, st.tma_bar);
+        }
+        return;
+      }
+    }
     constexpr int GQ = G / 4;
     constexpr int CH = L * GQ;
 #pragma unroll 4
@@ -725,10 +765,22 @@ __device__ __forceinline__ void prefetch_tile(PassState& st, const IO& io, long 
   }
 }
 
+// Whether a tile's input / output moves by tensor map.
+template <class IO>
+__device__ __forceinline__ bool tensor_in(const IO& io) {
+  if constexpr (TensorMapIo<IO>) return !IO::IN_VEC_L && io.in_tma;
+  return false;
+}
+template <class IO>
+__device__ __forceinline__ bool tensor_out(const IO& io) {
+  if constexpr (TensorMapIo<IO>) return io.out_tma;
+  return false;
+}
+
 // Wait for the prefetched tile (whole CTA). False if the bounded wait gave up.
 template <class IO>
 __device__ __forceinline__ bool wait_prefetch(PassState& st, const IO& io, const PassCore& core) {
-  if (IO::IN_VEC_L && io.in_contig) {
+  if ((IO::IN_VEC_L && io.in_contig) || tensor_in(io)) {
     const bool ok = mbar_wait_bounded(st.tma_bar, st.tma_phase & 1u);
     st.tma_phase++;
     if (!ok && (threadIdx.x & 31) == 0) atomicOr(core.err, kErrMmaTimeout);
@@ -851,7 +903,8 @@ __device__ __forceinline__ void permute_raw(const uint8_t* raw, uint8_t* re, uin
 }
 
 template <int L, int G, bool LINE_MINOR, int SIGN, class IO, int MINB = 3>
-__global__ void __launch_bounds__(kPassThreads, MINB) fft_pass_f16_pf(const IO io, const PassCore core) {
+__global__ void __launch_bounds__(kPassThreads, MINB) fft_pass_f16_pf(const __grid_constant__ IO io,
+                                                                      const PassCore core) {
   using Tl = Tile<L, G, LINE_MINOR>;
   constexpr uint32_t TMEM_COLS = pass_tmem_cols<L, G>();
   static_assert(TMEM_COLS >= 32 && (TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM columns");
@@ -862,7 +915,8 @@ __global__ void __launch_bounds__(kPassThreads, MINB) fft_pass_f16_pf(const IO i
   uint8_t* im = re + Tl::PLANE;
   uint8_t* raw = re + 2 * Tl::PLANE;
   const bool stage_out = IO::OUT_VEC_L && io.out_contig && !LINE_MINOR;
-  const bool tma_in = IO::IN_VEC_L && io.in_contig;
+  const bool tma_in = (IO::IN_VEC_L && io.in_contig) || tensor_in(io);
+  const bool tensor_store = LINE_MINOR && tensor_out(io);
   const long long ntiles = (io.total_lines + G - 1) / G;
   long long tile = blockIdx.x;
   bool pending = false;
@@ -879,7 +933,7 @@ __global__ void __launch_bounds__(kPassThreads, MINB) fft_pass_f16_pf(const IO i
       break;
     }
     pending = false;
-    if (stage_out && threadIdx.x == 0) bulk_wait_read_all();  // previous store has read the planes
+    if ((stage_out || tensor_store) && threadIdx.x == 0) bulk_wait_read_all();  // previous store has read the planes
     __syncthreads();
     permute_raw<L, G, LINE_MINOR, SIGN, IO>(raw, re, im, core, nval);
     fence_proxy_async_smem();
@@ -893,6 +947,16 @@ __global__ void __launch_bounds__(kPassThreads, MINB) fft_pass_f16_pf(const IO i
     if (stage_out && threadIdx.x == 0) {
       bulk_s2g(io.tile_dst(line0), re, static_cast<uint32_t>(nval) * L * 4u);
       bulk_commit();
+    }
+    if constexpr (TensorMapIo<IO> && LINE_MINOR) {
+      if (tensor_store && threadIdx.x == 0) {
+        constexpr int BY = L < 256 ? L : 256;
+        const int seq = static_cast<int>(line0 >> io.lps_log2);
+        const int x0 = static_cast<int>(line0 & ((1ll << io.lps_log2) - 1));
+#pragma unroll
+        for (int r0 = 0; r0 < L; r0 += BY) tma_store_3d(&io.out_map, re + static_cast<uint32_t>(r0) * G * 4u, x0, r0, seq);
+        bulk_commit();
+      }
     }
   }
   // an early exit may leave a prefetch in flight: let it land before the CTA ends
