@@ -103,15 +103,68 @@ __device__ __forceinline__ void split_stage_epilogue(const SplitPlanes& P, const
       const int e0 = rp * b * (L / (256 * Ns));
       const int de = rp * (L / 256);
       const uint32_t krow = (static_cast<uint32_t>(rp) >> 3) * Tl::KSTRIDE + (rp & 7) * 128u;
+      constexpr uint32_t CSTEP = LINE_MINOR ? static_cast<uint32_t>(Ns * G) : static_cast<uint32_t>(Ns);
+      if constexpr (Ns == 1 && !LINE_MINOR) {
+        // 16 outputs -> 16 consecutive columns: per plane two 16-byte stores
+        uint32_t prh[8], pih[8], prl[8], pil[8];
 #pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        const float2 w = __ldg(tw + e0 + c * de);
-        float2 x = cmulf(v[c], w);
-        x.x *= 0.0625f;  // 2^-4 per stage
-        x.y *= 0.0625f;
-        const uint32_t mp = static_cast<uint32_t>(Tl::pos(g, jp0 + c * Ns));
-        const uint32_t off = krow + (mp >> 6) * 1024u + ((((mp & 63u) >> 3) ^ (rp & 7)) << 4) + (mp & 7u) * 2u;
-        st_pair_split(P, off, x);
+        for (int c = 0; c < 16; c += 2) {
+          float2 x0 = cmulf(v[c], __ldg(tw + e0 + c * de));
+          float2 x1 = cmulf(v[c + 1], __ldg(tw + e0 + (c + 1) * de));
+          x0 = make_float2(x0.x * 0.0625f, x0.y * 0.0625f);  // 2^-4 per stage
+          x1 = make_float2(x1.x * 0.0625f, x1.y * 0.0625f);
+          const __half2 hr = __floats2half2_rn(x0.x, x1.x), hi = __floats2half2_rn(x0.y, x1.y);
+          const float2 fr = __half22float2(hr), fi = __half22float2(hi);
+          const __half2 lr = __floats2half2_rn((x0.x - fr.x) * 2048.0f, (x1.x - fr.y) * 2048.0f);
+          const __half2 li = __floats2half2_rn((x0.y - fi.x) * 2048.0f, (x1.y - fi.y) * 2048.0f);
+          prh[c / 2] = *reinterpret_cast<const uint32_t*>(&hr);
+          pih[c / 2] = *reinterpret_cast<const uint32_t*>(&hi);
+          prl[c / 2] = *reinterpret_cast<const uint32_t*>(&lr);
+          pil[c / 2] = *reinterpret_cast<const uint32_t*>(&li);
+        }
+        const uint32_t mp = static_cast<uint32_t>(Tl::pos(g, jp0));  // multiple of 16
+        // lanes with bit 2 set store the upper half first (bank spread)
+        const bool sw = (lane >> 2) & 1;
+        const uint32_t m0 = mp + (sw ? 8u : 0u), m1 = mp + (sw ? 0u : 8u);
+        const uint32_t off0 = krow + (m0 >> 6) * 1024u + ((((m0 & 63u) >> 3) ^ (rp & 7)) << 4);
+        const uint32_t off1 = krow + (m1 >> 6) * 1024u + ((((m1 & 63u) >> 3) ^ (rp & 7)) << 4);
+        auto put = [&](uint8_t* plane, const uint32_t (&p)[8]) {
+          const uint4 lo = make_uint4(p[0], p[1], p[2], p[3]), hi4 = make_uint4(p[4], p[5], p[6], p[7]);
+          *reinterpret_cast<uint4*>(plane + off0) = sw ? hi4 : lo;
+          *reinterpret_cast<uint4*>(plane + off1) = sw ? lo : hi4;
+        };
+        put(P.rh, prh);
+        put(P.ih, pih);
+        put(P.rl, prl);
+        put(P.il, pil);
+      } else if constexpr (CSTEP >= 8 && CSTEP < 64 && (CSTEP & (CSTEP - 1)) == 0) {
+        // offsets repeat with period 64 / CSTEP, one 1 KiB atom further per period
+        constexpr int PER = static_cast<int>(64u / CSTEP);
+        const uint32_t mp0 = static_cast<uint32_t>(Tl::pos(g, jp0));
+        uint32_t offs[PER];
+#pragma unroll
+        for (int k = 0; k < PER; ++k) {
+          const uint32_t mp = mp0 + static_cast<uint32_t>(k) * CSTEP;
+          offs[k] = krow + (mp >> 6) * 1024u + ((((mp & 63u) >> 3) ^ (rp & 7)) << 4) + (mp & 7u) * 2u;
+        }
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+          float2 x = cmulf(v[c], __ldg(tw + e0 + c * de));
+          x.x *= 0.0625f;
+          x.y *= 0.0625f;
+          st_pair_split(P, offs[c % PER] + static_cast<uint32_t>(c / PER) * 1024u, x);
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+          const float2 w = __ldg(tw + e0 + c * de);
+          float2 x = cmulf(v[c], w);
+          x.x *= 0.0625f;  // 2^-4 per stage
+          x.y *= 0.0625f;
+          const uint32_t mp = static_cast<uint32_t>(Tl::pos(g, jp0 + c * Ns));
+          const uint32_t off = krow + (mp >> 6) * 1024u + ((((mp & 63u) >> 3) ^ (rp & 7)) << 4) + (mp & 7u) * 2u;
+          st_pair_split(P, off, x);
+        }
       }
     }
   }
@@ -198,111 +251,87 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
     if (tid == 0) *st.smax = 0;
     __syncthreads();
 
-    // ---- pass A: largest magnitude in the tile (data stays in L1/L2) ----
-    float lmax = 0.f;
-    if constexpr (IO::IN_VEC_L) {
-      constexpr int ITEMS = G * (L / 4);
-#pragma unroll 1
-      for (int base = tid; base < ITEMS; base += kPassThreads * 8) {
-        typename IO::Raw raw[8];
+    // ---- the tile is read once: every thread's share fits one batch of
+    // loads (4 * Mt / T items of T x 4 elements, Mt <= 512), so the loaded
+    // values give the tile's largest magnitude before they are scaled,
+    // put through the radix-T stage and split ----
+    float in_scale = 1.0f, out_scale = 1.0f;
+    auto scales_from = [&](float lmax) {
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int it = base + u * kPassThreads;
-          raw[u] = io.fetch_l(line0 + it / (L / 4), (it % (L / 4)) * 4, it < ITEMS);
-        }
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          float2 v[4];
-          io.decode_l(raw[u], 0, 0, v);
-          lmax = fmaxf(lmax, max_abs4(v));
-        }
+      for (int o = 16; o > 0; o >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+      if (lane == 0) atomicMax(st.smax, __float_as_int(lmax));
+      __syncthreads();
+      const float tmax = __int_as_float(*st.smax) * static_cast<float>(T);
+      // sigma: largest value after the radix-T stage maps to <= 2^14
+      int sigma = 0;
+      if (tmax > 0.f && isfinite(tmax)) {
+        int ex;
+        frexpf(tmax, &ex);  // tmax = f * 2^ex, f in [0.5, 1)
+        sigma = 14 - ex;
       }
-    } else {
-      constexpr int GQ = G / 4;
-      constexpr int ITEMS = GQ * L;
-#pragma unroll 1
-      for (int base = tid; base < ITEMS; base += kPassThreads * 8) {
-        typename IO::Raw raw[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int it = base + u * kPassThreads;
-          raw[u] = io.fetch_g(line0 + (it % GQ) * 4, it / GQ, it < ITEMS);
-        }
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          float2 v[4];
-          io.decode_g(raw[u], 0, 0, v);
-          lmax = fmaxf(lmax, max_abs4(v));
-        }
-      }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-    if (lane == 0) atomicMax(st.smax, __float_as_int(lmax));
-    __syncthreads();
-    const float tmax = __int_as_float(*st.smax) * static_cast<float>(T);
-    // sigma: largest value after the radix-T stage maps to <= 2^14
-    int sigma = 0;
-    if (tmax > 0.f && isfinite(tmax)) {
-      int ex;
-      frexpf(tmax, &ex);  // tmax = f * 2^ex, f in [0.5, 1)
-      sigma = 14 - ex;
-    }
-    const float in_scale = ldexpf(1.0f, sigma);
-    const float out_scale = ldexpf(1.0f, -(sigma - 4 * (S - 1)));
-
-    // ---- pass B: load, scale, radix-T stage, twiddle, split ----
+      in_scale = ldexpf(1.0f, sigma);
+      out_scale = ldexpf(1.0f, -(sigma - 4 * (S - 1)));
+    };
     if constexpr (IO::IN_VEC_L) {
       constexpr int QPL = (L / T) / 4;
       constexpr int ITEMS = G * QPL;
-#pragma unroll 1
-      for (int base = tid; base < ITEMS; base += kPassThreads * U) {
-        typename IO::Raw raw[U][T];
+      static_assert(ITEMS <= kPassThreads * U, "one load batch per tile");
+      typename IO::Raw raw[U][T];
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int it = base + u * kPassThreads;
+      for (int u = 0; u < U; ++u) {
+        const int it = tid + u * kPassThreads;
 #pragma unroll
-          for (int r = 0; r < T; ++r)
-            raw[u][r] = io.fetch_l(line0 + it / QPL, (it % QPL) * 4 + r * (L / T), it < ITEMS);
+        for (int r = 0; r < T; ++r)
+          raw[u][r] = io.fetch_l(line0 + it / QPL, (it % QPL) * 4 + r * (L / T), it < ITEMS);
+      }
+      float2 v[U][T][4];
+      float lmax = 0.f;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int it = tid + u * kPassThreads;
+        const int g = it / QPL;
+        const int j0 = (it % QPL) * 4;
+#pragma unroll
+        for (int r = 0; r < T; ++r) {
+          io.decode_l(raw[u][r], line0 + g, j0 + r * (L / T), v[u][r]);
+          lmax = fmaxf(lmax, max_abs4(v[u][r]));
         }
+      }
+      scales_from(lmax);
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int it = base + u * kPassThreads;
-          if (ITEMS % (kPassThreads * U) != 0 && it >= ITEMS) continue;
-          const int g = it / QPL;
-          const int j0 = (it % QPL) * 4;
-          float2 v[T][4];
+      for (int u = 0; u < U; ++u) {
+        const int it = tid + u * kPassThreads;
+        if (ITEMS % (kPassThreads * U) != 0 && it >= ITEMS) continue;
+        const int g = it / QPL;
+        const int j0 = (it % QPL) * 4;
 #pragma unroll
-          for (int r = 0; r < T; ++r) {
-            io.decode_l(raw[u][r], line0 + g, j0 + r * (L / T), v[r]);
+        for (int r = 0; r < T; ++r)
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              v[r][q].x *= in_scale;
-              v[r][q].y *= in_scale;
-            }
+          for (int q = 0; q < 4; ++q) {
+            v[u][r][q].x *= in_scale;
+            v[u][r][q].y *= in_scale;
           }
-          if constexpr (T == 1) {
-            if constexpr (!LINE_MINOR && J >= 4) {
-              st_quad_split(P, Tl::off(g, j0), v[0]);
-            } else {
-#pragma unroll
-              for (int q = 0; q < 4; ++q) st_pair_split(P, Tl::off(g, j0 + q), v[0][q]);
-            }
+        if constexpr (T == 1) {
+          if constexpr (!LINE_MINOR && J >= 4) {
+            st_quad_split(P, Tl::off(g, j0), v[u][0]);
           } else {
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              float2 t[T];
+            for (int q = 0; q < 4; ++q) st_pair_split(P, Tl::off(g, j0 + q), v[u][0][q]);
+          }
+        } else {
 #pragma unroll
-              for (int r = 0; r < T; ++r) t[r] = v[r][q];
-              small_dft<T, SIGN>(t);
-              const int j = j0 + q;
+          for (int q = 0; q < 4; ++q) {
+            float2 t[T];
 #pragma unroll
-              for (int c = 0; c < T; ++c) {
-                const int lp = j * T + c;
-                const int rp = lp / J, jp = lp % J;
-                const float2 w = __ldg(core.tw + rp * (jp % T) * (L / (16 * T)));
-                st_pair_split(P, Tl::off(g, lp), cmulf(t[c], w));
-              }
+            for (int r = 0; r < T; ++r) t[r] = v[u][r][q];
+            small_dft<T, SIGN>(t);
+            const int j = j0 + q;
+#pragma unroll
+            for (int c = 0; c < T; ++c) {
+              const int lp = j * T + c;
+              const int rp = lp / J, jp = lp % J;
+              const float2 w = __ldg(core.tw + rp * (jp % T) * (L / (16 * T)));
+              st_pair_split(P, Tl::off(g, lp), cmulf(t[c], w));
             }
           }
         }
@@ -310,56 +339,65 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
     } else {
       constexpr int GQ = G / 4;
       constexpr int ITEMS = GQ * (L / T);
-#pragma unroll 1
-      for (int base = tid; base < ITEMS; base += kPassThreads * U) {
-        typename IO::Raw raw[U][T];
+      static_assert(ITEMS <= kPassThreads * U, "one load batch per tile");
+      typename IO::Raw raw[U][T];
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int it = base + u * kPassThreads;
+      for (int u = 0; u < U; ++u) {
+        const int it = tid + u * kPassThreads;
 #pragma unroll
-          for (int r = 0; r < T; ++r) raw[u][r] = io.fetch_g(line0 + (it % GQ) * 4, it / GQ + r * (L / T), it < ITEMS);
+        for (int r = 0; r < T; ++r) raw[u][r] = io.fetch_g(line0 + (it % GQ) * 4, it / GQ + r * (L / T), it < ITEMS);
+      }
+      float2 v[U][T][4];
+      float lmax = 0.f;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int it = tid + u * kPassThreads;
+        const int j = it / GQ;
+        const int g0 = (it % GQ) * 4;
+#pragma unroll
+        for (int r = 0; r < T; ++r) {
+          io.decode_g(raw[u][r], line0 + g0, j + r * (L / T), v[u][r]);
+          lmax = fmaxf(lmax, max_abs4(v[u][r]));
         }
+      }
+      scales_from(lmax);
 #pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int it = base + u * kPassThreads;
-          if (ITEMS % (kPassThreads * U) != 0 && it >= ITEMS) continue;
-          const int j = it / GQ;
-          const int g0 = (it % GQ) * 4;
-          float2 v[T][4];
+      for (int u = 0; u < U; ++u) {
+        const int it = tid + u * kPassThreads;
+        if (ITEMS % (kPassThreads * U) != 0 && it >= ITEMS) continue;
+        const int j = it / GQ;
+        const int g0 = (it % GQ) * 4;
 #pragma unroll
-          for (int r = 0; r < T; ++r) {
-            io.decode_g(raw[u][r], line0 + g0, j + r * (L / T), v[r]);
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              v[r][q].x *= in_scale;
-              v[r][q].y *= in_scale;
-            }
-          }
+        for (int r = 0; r < T; ++r)
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
-            float2 t[T];
-#pragma unroll
-            for (int r = 0; r < T; ++r) t[r] = v[r][q];
-            small_dft<T, SIGN>(t);
-#pragma unroll
-            for (int r = 0; r < T; ++r) v[r][q] = t[r];
+            v[u][r][q].x *= in_scale;
+            v[u][r][q].y *= in_scale;
           }
 #pragma unroll
-          for (int c = 0; c < T; ++c) {
-            const int lp = j * T + c;
-            float2 x[4] = {v[c][0], v[c][1], v[c][2], v[c][3]};
-            if constexpr (T > 1) {
-              const int rp = lp / J, jp = lp % J;
-              const float2 w = __ldg(core.tw + rp * (jp % T) * (L / (16 * T)));
+        for (int q = 0; q < 4; ++q) {
+          float2 t[T];
 #pragma unroll
-              for (int q = 0; q < 4; ++q) x[q] = cmulf(x[q], w);
-            }
-            if constexpr (LINE_MINOR) {
-              st_quad_split(P, Tl::off(g0, lp), x);
-            } else {
+          for (int r = 0; r < T; ++r) t[r] = v[u][r][q];
+          small_dft<T, SIGN>(t);
 #pragma unroll
-              for (int q = 0; q < 4; ++q) st_pair_split(P, Tl::off(g0 + q, lp), x[q]);
-            }
+          for (int r = 0; r < T; ++r) v[u][r][q] = t[r];
+        }
+#pragma unroll
+        for (int c = 0; c < T; ++c) {
+          const int lp = j * T + c;
+          float2 x[4] = {v[u][c][0], v[u][c][1], v[u][c][2], v[u][c][3]};
+          if constexpr (T > 1) {
+            const int rp = lp / J, jp = lp % J;
+            const float2 w = __ldg(core.tw + rp * (jp % T) * (L / (16 * T)));
+#pragma unroll
+            for (int q = 0; q < 4; ++q) x[q] = cmulf(x[q], w);
+          }
+          if constexpr (LINE_MINOR) {
+            st_quad_split(P, Tl::off(g0, lp), x);
+          } else {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) st_pair_split(P, Tl::off(g0 + q, lp), x[q]);
           }
         }
       }
