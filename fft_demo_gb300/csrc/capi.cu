@@ -8,6 +8,7 @@
 // use the four-step split N = N1 * N2 (column pass with outer twiddle, then a
 // transposing row pass), so every transform is at most two HBM round trips.
 #include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -238,9 +239,21 @@ bool encode_column_map(CUtensorMap* map, const void* base, long long lines_per_s
   const cuuint64_t strides[2] = {static_cast<cuuint64_t>(elem_stride * 4), static_cast<cuuint64_t>(seq_stride * 4)};
   const cuuint32_t box[3] = {static_cast<cuuint32_t>(G), static_cast<cuuint32_t>(L < 256 ? L : 256), 1u};
   const cuuint32_t estr[3] = {1u, 1u, 1u};
-  return cuTensorMapEncodeTiled(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, const_cast<void*>(base), dims, strides, box,
-                                estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+  // the driver's encoder, found through the runtime (the library does not
+  // link the driver library itself)
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      fn = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  if (!encode) return false;
+  return encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, const_cast<void*>(base), dims, strides, box, estr,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 // Prefetching (mid-tile) kernels move column-layout tiles by TMA when every
