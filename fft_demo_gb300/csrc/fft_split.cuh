@@ -3,17 +3,17 @@
 //
 // Every value v held in shared memory is stored as two FP16 numbers with a
 // per-tile power-of-two scale 2^sigma:
-//     v * 2^sigma = hi + lo * 2^-11,  hi = fp16(v * 2^sigma),
-//                                     lo = fp16((v * 2^sigma - hi) * 2^11)
-// and so is the DFT matrix B = B_hi + B_lo * 2^-11. Each radix-16 stage forms
-//     D_main = A_hi * B_hi                      (TMEM columns  0..31)
-//     D_corr = A_hi * B_lo + A_lo * B_hi        (TMEM columns 32..63)
-// and the epilogue takes A*B = D_main + 2^-11 * D_corr in FP32 (the dropped
-// A_lo * B_lo term is 2^-22 relative). sigma is chosen per tile from the
-// input's largest magnitude (largest value -> <= 2^14 after the radix-T
-// stage); each radix-16 stage scales its output by 2^-4 (its largest possible
-// growth is 16), so no FP16 operand overflows and typical values stay far
-// above FP16's subnormal range.
+//     v * 2^sigma = hi + lo,  hi = fp16(v * 2^sigma),  lo = fp16(v * 2^sigma - hi)
+// and so is the DFT matrix B = B_hi + B_lo. Each radix-16 stage accumulates
+//     D = A_hi * B_hi + A_hi * B_lo + A_lo * B_hi
+// in one FP32 TMEM accumulator (six K = 16 MMAs per 128 rows; the dropped
+// A_lo * B_lo term is ~2^-22 relative, and the correction products, ~2^-11
+// of the main one, sit far above FP32's resolution of the sum). sigma is
+// chosen per tile from the input's largest magnitude (largest value ->
+// <= 2^14 after the radix-T stage), so lo stays in FP16's normal range for
+// every value within 2^17 of the tile's maximum; each radix-16 stage scales
+// its output by 2^-4 (its largest possible growth is 16), so no FP16
+// operand overflows.
 #pragma once
 #include "fft_io.cuh"
 #include "fft_tile.cuh"
@@ -26,7 +26,7 @@ struct SplitPlanes {
 
 __device__ __forceinline__ void split_f(float v, __half& hi, __half& lo) {
   hi = __float2half_rn(v);
-  lo = __float2half_rn((v - __half2float(hi)) * 2048.0f);
+  lo = __float2half_rn(v - __half2float(hi));
 }
 
 __device__ __forceinline__ void st_pair_split(const SplitPlanes& P, uint32_t off, float2 v) {
@@ -72,19 +72,16 @@ __device__ __forceinline__ void split_stage_epilogue(const SplitPlanes& P, const
   constexpr bool LAST = (s == Sh::S - 1);
 #pragma unroll 1
   for (int grp = warp >> 2; grp < NG; grp += kPassThreads / 128) {
-    const uint32_t taddr = tbase + (static_cast<uint32_t>(32 * (warp & 3)) << 16) + grp * 64u;
-    uint32_t dm[32], dc[32];
-    tmem_ld_x32(taddr, dm);
-    tmem_ld_x32(taddr + 32u, dc);
+    const uint32_t taddr = tbase + (static_cast<uint32_t>(32 * (warp & 3)) << 16) + grp * 32u;
+    uint32_t d[32];
+    tmem_ld_x32(taddr, d);
     tmem_ld_wait();
     const int m = grp * 128 + 32 * (warp & 3) + lane;
     int g, j;
     Tl::unpos(m, g, j);
     float2 v[16];
 #pragma unroll
-    for (int c = 0; c < 16; ++c)
-      v[c] = make_float2(fmaf(__uint_as_float(dc[c]), 1.0f / 2048.0f, __uint_as_float(dm[c])),
-                         fmaf(__uint_as_float(dc[16 + c]), 1.0f / 2048.0f, __uint_as_float(dm[16 + c])));
+    for (int c = 0; c < 16; ++c) v[c] = make_float2(__uint_as_float(d[c]), __uint_as_float(d[16 + c]));
     if constexpr (LAST) {
       const long long line = line0 + g;
       if (line < io.total_lines) {
@@ -115,8 +112,8 @@ __device__ __forceinline__ void split_stage_epilogue(const SplitPlanes& P, const
           x1 = make_float2(x1.x * 0.0625f, x1.y * 0.0625f);
           const __half2 hr = __floats2half2_rn(x0.x, x1.x), hi = __floats2half2_rn(x0.y, x1.y);
           const float2 fr = __half22float2(hr), fi = __half22float2(hi);
-          const __half2 lr = __floats2half2_rn((x0.x - fr.x) * 2048.0f, (x1.x - fr.y) * 2048.0f);
-          const __half2 li = __floats2half2_rn((x0.y - fi.x) * 2048.0f, (x1.y - fi.y) * 2048.0f);
+          const __half2 lr = __floats2half2_rn(x0.x - fr.x, x1.x - fr.y);
+          const __half2 li = __floats2half2_rn(x0.y - fi.x, x1.y - fi.y);
           prh[c / 2] = *reinterpret_cast<const uint32_t*>(&hr);
           pih[c / 2] = *reinterpret_cast<const uint32_t*>(&hi);
           prl[c / 2] = *reinterpret_cast<const uint32_t*>(&lr);
@@ -221,12 +218,12 @@ __device__ __forceinline__ void split_teardown(SplitState& st) {
 
 template <int L, int G>
 __host__ __device__ constexpr uint32_t split_tmem_cols() {
-  return static_cast<uint32_t>(G * L / 16 / 128 * 64);
+  return static_cast<uint32_t>(G * L / 16 / 128 * 32);
 }
 
 // One split-precision tile: G lines of length L starting at line0. Same
 // geometry rules as pass_tile, with G * L / 16 in {128, 256, 512} (4 planes
-// + 64 TMEM columns per 128 rows). False if a bounded wait gave up.
+// + 32 TMEM columns per 128 rows). False if a bounded wait gave up.
 template <int L, int G, bool LINE_MINOR, int SIGN, class IO>
 __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const PassCore& core, long long line0) {
   using Sh = LineShape<L>;
@@ -423,13 +420,13 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
           const uint64_t a_ih = make_sdesc(aih + o, 1024u, KSTRIDE, kLayoutSw128);
           const uint64_t a_rl = make_sdesc(arl + o, 1024u, KSTRIDE, kLayoutSw128);
           const uint64_t a_il = make_sdesc(ail + o, 1024u, KSTRIDE, kLayoutSw128);
-          const uint32_t dmain = st.tbase + grp * 64u, dcorr = dmain + 32u;
-          umma_f16(dmain, a_rh, bh0, IDESC, 0u);
-          umma_f16(dmain, a_ih, bh1, IDESC, 1u);
-          umma_f16(dcorr, a_rh, bl0, IDESC, 0u);
-          umma_f16(dcorr, a_ih, bl1, IDESC, 1u);
-          umma_f16(dcorr, a_rl, bh0, IDESC, 1u);
-          umma_f16(dcorr, a_il, bh1, IDESC, 1u);
+          const uint32_t dacc = st.tbase + grp * 32u;
+          umma_f16(dacc, a_rh, bh0, IDESC, 0u);
+          umma_f16(dacc, a_ih, bh1, IDESC, 1u);
+          umma_f16(dacc, a_rh, bl0, IDESC, 1u);
+          umma_f16(dacc, a_ih, bl1, IDESC, 1u);
+          umma_f16(dacc, a_rl, bh0, IDESC, 1u);
+          umma_f16(dacc, a_il, bh1, IDESC, 1u);
         }
         umma_commit(st.mbar);
       }

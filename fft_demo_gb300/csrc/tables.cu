@@ -2,8 +2,9 @@
 //
 // Every table entry is computed in double precision (sincospi of an exactly
 // reduced rational angle) and rounded once: to FP32 for twiddles, to an FP16
-// (hi, lo) pair for the 16-point DFT matrix (lo carries the residual scaled by
-// 2^11 so it stays in FP16's normal range).
+// (hi, lo) pair for the 16-point DFT matrix (lo = the residual B - hi; at most
+// 2^-12, it keeps at least 8 significant bits even where it is subnormal,
+// about 6e-8 absolute).
 //
 // The reference computes its 16x16 DFT matrix on the host in FP32 and rounds
 // it to FP16 (tcfft_half.cu:1332-1339) and its twiddles per thread with
@@ -36,7 +37,7 @@ __global__ void gen_twiddle_kernel(float2* __restrict__ tw, long long count, int
 // 16-point DFT F[c][r] = exp(sign * 2 pi i c r / 16):
 //   B[r][c]       =  Re F[c][r]     B[r][16+c]    = Im F[c][r]
 //   B[16+r][c]    = -Im F[c][r]     B[16+r][16+c] = Re F[c][r]
-// part 0 = FP16 hi, part 1 = FP16 lo residual * 2^11.
+// part 0 = FP16 hi, part 1 = FP16 lo residual (B - hi, at its own scale).
 __global__ void gen_dft16_bmat_kernel(uint16_t* __restrict__ img, int sign, int part) {
   const int idx = threadIdx.x;  // 0..1023 = n * 32 + k
   if (idx >= 1024) return;
@@ -53,7 +54,7 @@ __global__ void gen_dft16_bmat_kernel(uint16_t* __restrict__ img, int sign, int 
     v = (n < 16) ? -fi : fr;
   const __half hi = __double2half(v);
   __half outv = hi;
-  if (part == 1) outv = __double2half((v - static_cast<double>(__half2float(hi))) * 2048.0);
+  if (part == 1) outv = __double2half(v - static_cast<double>(__half2float(hi)));
   const uint32_t off = kmajor_none_offset(static_cast<uint32_t>(n), static_cast<uint32_t>(k), 128u, 512u);
   img[off / 2] = __half_as_ushort(outv);
 }
