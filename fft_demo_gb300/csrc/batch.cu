@@ -56,7 +56,7 @@ void init_batch_registry() {
       const int regs_per_warp = ((fa.numRegs * 32 + 255) / 256) * 256;
       int occ = 65536 / (regs_per_warp * (kPassThreads / 32));
       const int by_smem = (228 * 1024) / (k.smem + static_cast<int>(fa.sharedSizeBytes) + 1024);
-      const int tmem_cols = kBatchMt / 4;
+      const int tmem_cols = pr == 0 ? kBatchMt / 4 : kBatchMt / 2;
       occ = std::min({occ, by_smem, 2048 / kPassThreads, 512 / tmem_cols});
       g_bk_ctas[pr][sg] = sms * (occ < 1 ? 1 : occ);
     }

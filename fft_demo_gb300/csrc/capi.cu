@@ -101,9 +101,9 @@ void init_registry() {
           int own = by_regs < by_smem ? by_regs : by_smem;
           own = own < by_threads ? own : by_threads;
           if (own > occ) occ = own;
-          // TMEM: 512 columns per SM; a CTA holds Mt/4 columns (one FP32
-          // accumulator of 32 columns per 128 rows, both precisions).
-          const int tmem_limit = 512 / (pk.Mt / 4);
+          // TMEM: 512 columns per SM; a CTA holds Mt/4 (FP16) or Mt/2 (split)
+          // columns.
+          const int tmem_limit = 512 / (pk.Mt / (pr == kPrecF16 ? 4 : 2));
           g_occ[pr][k][l][t][s] = occ < tmem_limit ? occ : tmem_limit;
         }
   for (int l = kFusedMinLog; l <= kFusedMaxLog && e == cudaSuccess; ++l)

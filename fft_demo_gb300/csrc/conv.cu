@@ -70,7 +70,7 @@ void conv_init() {
         int occ = 65536 / (regs_per_warp * (kPassThreads / 32));
         const int by_smem = (228 * 1024) / (ck.smem + 1024);
         if (by_smem < occ) occ = by_smem;
-        const int tmem = 512 / (ck.Mt / 4);
+        const int tmem = 512 / (ck.Mt / (pr == 0 ? 4 : 2));
         if (tmem < occ) occ = tmem;
         g_cocc[pr][k][l] = occ < 1 ? 1 : occ;
       }

@@ -22,8 +22,8 @@
 // every CTA of the grid is resident at once.
 //
 // All tiles hold 512 rows of the 16-column MMA layout (Mt = 512), FP16 or
-// split precision, so one TMEM allocation (128 columns) and one
-// shared-memory carve-out serve every item kind and size.
+// split precision, so one TMEM allocation (128 columns FP16, 256 split) and
+// one shared-memory carve-out serve every item kind and size.
 #pragma once
 #include "fft_fused.cuh"
 #include "fft_io.cuh"
@@ -200,7 +200,7 @@ template <>
 struct BatchPrec<true> {
   using E = float2;
   using State = SplitState;
-  static constexpr uint32_t kTmemCols = kBatchMt / 4;
+  static constexpr uint32_t kTmemCols = kBatchMt / 2;
   template <bool IN_L, bool OUT_L, bool COH>
   using Io = IoFloat<IN_L, OUT_L, COH>;
   template <int L, bool LM, int SIGN, class IO>

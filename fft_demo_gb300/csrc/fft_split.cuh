@@ -4,11 +4,12 @@
 // Every value v held in shared memory is stored as two FP16 numbers with a
 // per-tile power-of-two scale 2^sigma:
 //     v * 2^sigma = hi + lo,  hi = fp16(v * 2^sigma),  lo = fp16(v * 2^sigma - hi)
-// and so is the DFT matrix B = B_hi + B_lo. Each radix-16 stage accumulates
-//     D = A_hi * B_hi + A_hi * B_lo + A_lo * B_hi
-// in one FP32 TMEM accumulator (six K = 16 MMAs per 128 rows; the dropped
-// A_lo * B_lo term is ~2^-22 relative, and the correction products, ~2^-11
-// of the main one, sit far above FP32's resolution of the sum). sigma is
+// and so is the DFT matrix B = B_hi + B_lo. Each radix-16 stage runs, per
+// plane (real, imaginary), two K = 16 MMAs with N = 64 against [B_hi | B_lo]:
+//     D[:, 0:32]  += A_hi * B_hi + A_lo * B_hi
+//     D[:, 32:64] += A_hi * B_lo + A_lo * B_lo
+// (four MMAs per 128 rows) and the epilogue adds the two halves in FP32: the
+// full product (A_hi + A_lo)(B_hi + B_lo). sigma is
 // chosen per tile from the input's largest magnitude (largest value ->
 // <= 2^14 after the radix-T stage), so lo stays in FP16's normal range for
 // every value within 2^17 of the tile's maximum; each radix-16 stage scales
@@ -72,16 +73,19 @@ __device__ __forceinline__ void split_stage_epilogue(const SplitPlanes& P, const
   constexpr bool LAST = (s == Sh::S - 1);
 #pragma unroll 1
   for (int grp = warp >> 2; grp < NG; grp += kPassThreads / 128) {
-    const uint32_t taddr = tbase + (static_cast<uint32_t>(32 * (warp & 3)) << 16) + grp * 32u;
-    uint32_t d[32];
+    const uint32_t taddr = tbase + (static_cast<uint32_t>(32 * (warp & 3)) << 16) + grp * 64u;
+    uint32_t d[32], e[32];
     tmem_ld_x32(taddr, d);
+    tmem_ld_x32(taddr + 32u, e);
     tmem_ld_wait();
     const int m = grp * 128 + 32 * (warp & 3) + lane;
     int g, j;
     Tl::unpos(m, g, j);
     float2 v[16];
 #pragma unroll
-    for (int c = 0; c < 16; ++c) v[c] = make_float2(__uint_as_float(d[c]), __uint_as_float(d[16 + c]));
+    for (int c = 0; c < 16; ++c)
+      v[c] = make_float2(__uint_as_float(d[c]) + __uint_as_float(e[c]),
+                         __uint_as_float(d[16 + c]) + __uint_as_float(e[16 + c]));
     if constexpr (LAST) {
       const long long line = line0 + g;
       if (line < io.total_lines) {
@@ -218,12 +222,12 @@ __device__ __forceinline__ void split_teardown(SplitState& st) {
 
 template <int L, int G>
 __host__ __device__ constexpr uint32_t split_tmem_cols() {
-  return static_cast<uint32_t>(G * L / 16 / 128 * 32);
+  return static_cast<uint32_t>(G * L / 16 / 128 * 64);
 }
 
 // One split-precision tile: G lines of length L starting at line0. Same
 // geometry rules as pass_tile, with G * L / 16 in {128, 256, 512} (4 planes
-// + 32 TMEM columns per 128 rows). False if a bounded wait gave up.
+// + 64 TMEM columns per 128 rows). False if a bounded wait gave up.
 template <int L, int G, bool LINE_MINOR, int SIGN, class IO>
 __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const PassCore& core, long long line0) {
   using Sh = LineShape<L>;
@@ -237,7 +241,9 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
   constexpr uint32_t KSTRIDE = Tl::KSTRIDE;
   static_assert(Mt % 128 == 0 && Mt <= 512, "tile size");
   static_assert(G % 4 == 0 || IO::IN_VEC_L, "line-vectorised loads need G % 4 == 0");
-  constexpr uint32_t IDESC = make_idesc_f16_f32(128, 32, true, false);
+  // N = 64: B_hi (2 KiB) and B_lo (the next 2 KiB) side by side form one
+  // K-major operand (SBO 512 B), so D = [A * B_hi | A * B_lo]
+  constexpr uint32_t IDESC = make_idesc_f16_f32(128, 64, true, false);
   constexpr int U = T >= 8 ? 1 : 8 / T;
   uint8_t* pl = st.smem + kSplitPlaneOffset;
   SplitPlanes P{pl, pl + PLANE, pl + 2 * PLANE, pl + 3 * PLANE};
@@ -411,8 +417,6 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
         const uint32_t arh = smem_u32(P.rh), aih = smem_u32(P.ih), arl = smem_u32(P.rl), ail = smem_u32(P.il);
         const uint64_t bh0 = make_sdesc(smem_u32(st.bhi), 128u, 512u, kLayoutNone);
         const uint64_t bh1 = make_sdesc(smem_u32(st.bhi) + 256u, 128u, 512u, kLayoutNone);
-        const uint64_t bl0 = make_sdesc(smem_u32(st.blo), 128u, 512u, kLayoutNone);
-        const uint64_t bl1 = make_sdesc(smem_u32(st.blo) + 256u, 128u, 512u, kLayoutNone);
 #pragma unroll
         for (int grp = 0; grp < NG; ++grp) {
           const uint32_t o = grp * 2048u;
@@ -420,11 +424,9 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
           const uint64_t a_ih = make_sdesc(aih + o, 1024u, KSTRIDE, kLayoutSw128);
           const uint64_t a_rl = make_sdesc(arl + o, 1024u, KSTRIDE, kLayoutSw128);
           const uint64_t a_il = make_sdesc(ail + o, 1024u, KSTRIDE, kLayoutSw128);
-          const uint32_t dacc = st.tbase + grp * 32u;
+          const uint32_t dacc = st.tbase + grp * 64u;
           umma_f16(dacc, a_rh, bh0, IDESC, 0u);
           umma_f16(dacc, a_ih, bh1, IDESC, 1u);
-          umma_f16(dacc, a_rh, bl0, IDESC, 1u);
-          umma_f16(dacc, a_ih, bl1, IDESC, 1u);
           umma_f16(dacc, a_rl, bh0, IDESC, 1u);
           umma_f16(dacc, a_il, bh1, IDESC, 1u);
         }
