@@ -259,7 +259,7 @@ def main():
                     help="profiling case N,BATCH[,REPS[,PREC]]: REPS forward transforms of one size, no timing "
                          "(PREC fp16 or split); the target of the ncu captures kept under profiles/")
     ap.add_argument("--workload", default="large-1d",
-                    choices=["large-1d", "small", "2d-conv", "uneven", "serving"],
+                    choices=["large-1d", "large-1d-split", "small", "2d-conv", "uneven", "serving"],
                     help="large-1d: the headline run (default); the others print one JSON line each "
                          "(fft_demo_gb300/workloads.py)")
     args = ap.parse_args()

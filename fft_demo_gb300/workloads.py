@@ -13,6 +13,10 @@
              (one launch chain per transform, one convolution plan per
              convolution), with and without CUDA-graph replay
   serving  : fft_demo_gb300/serve.py at 20k requests/s
+  large-1d-split : split precision (FP32 storage, 8 B per element) forward
+             C2C of N = 4096, 65536, 2^20 over 1 GiB each (batch 32768,
+             2048, 128), against plain FP16 over the same 2^27 elements;
+             reports the element-rate ratio split / FP16 and rel-L2 vs FP64
 
 Each returns a dict for bench.py's JSON line. Inputs are seeded synthetic
 data of the stated shapes (no dataset is involved). Device time is taken
@@ -223,4 +227,36 @@ def serving(peak_gbs, rate=20000.0, seconds=1.0):
             % (rate, seconds), **out}
 
 
-WORKLOADS = {"small": small, "2d-conv": two_d_conv, "uneven": uneven, "serving": serving}
+def large_1d_split(peak_gbs, seed=1):
+    import torch
+    import pyoracle as orc
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    res = {}
+    for n, b in ((4096, 32768), (65536, 2048), (1 << 20, 128)):
+        row = {}
+        for prec, name, dt in ((tc.SPLIT_FP32, "split", torch.float32), (tc.FP16, "fp16", torch.float16)):
+            x = (torch.rand((b, n, 2), device="cuda", generator=g) * 2 - 1).to(dt)
+            y = torch.empty_like(x)
+            plan = tc.plan_1d(n, b, prec)
+            ms = _timed(lambda: plan.exec(x, y), 10)
+            plan.check()
+            eb = x.element_size() * 2
+            row[name] = {"ms": ms, "gflops": _f1d(n) * b / ms / 1e6,
+                         "gbs": 2 * n * b * eb / ms / 1e6, "hbm_frac": 2 * n * b * eb / ms / 1e6 / peak_gbs,
+                         "launches": tc.last_launch_count()}
+            if name == "split":
+                xs = x[:2].double().cpu().numpy()
+                ys = y[:2].double().cpu().numpy()
+                row[name]["rel_l2_vs_fp64"] = orc.rel_l2(ys[..., 0] + 1j * ys[..., 1],
+                                                         orc.fft1d(xs[..., 0] + 1j * xs[..., 1]))
+            plan.destroy()
+            del x, y
+            torch.cuda.empty_cache()
+        row["split_over_fp16_element_rate"] = row["fp16"]["ms"] / row["split"]["ms"]
+        res[str(n)] = row
+    return {"workload": "large-1d-split: N=4096/65536/2^20, 1 GiB FP32 each (batch 32768/2048/128), "
+                        "FP16 over the same element counts", **res}
+
+
+WORKLOADS = {"small": small, "large-1d-split": large_1d_split, "2d-conv": two_d_conv, "uneven": uneven, "serving": serving}
