@@ -33,3 +33,8 @@ def f16_round(z):
     """The input exactly as the FP16 kernel sees it."""
     return (z.real.astype(np.float16).astype(np.float64)
             + 1j * z.imag.astype(np.float16).astype(np.float64))
+
+
+def f32_round(z):
+    """z with real and imaginary parts rounded to FP32 (complex128 result)."""
+    return z.real.astype(np.float32).astype(np.float64) + 1j * z.imag.astype(np.float32).astype(np.float64)

@@ -8,15 +8,11 @@ import numpy as np
 import pytest
 
 from conftest import uniform_complex
-from gpu_util import from_dev_f32, to_dev_f32
+from gpu_util import f32_round, from_dev_f32, to_dev_f32
 
 pytestmark = pytest.mark.gpu
 
 REL_L2_SPLIT = 1e-5
-
-
-def f32_round(z):
-    return z.real.astype(np.float32).astype(np.float64) + 1j * z.imag.astype(np.float32).astype(np.float64)
 
 
 def _case(tc, orc, n, batch, seed, direction=-1, scale=1.0, amp=1.0):
