@@ -73,14 +73,41 @@ __device__ __forceinline__ void split_stage_epilogue(const SplitPlanes& P, const
   constexpr bool LAST = (s == Sh::S - 1);
 #pragma unroll 1
   for (int grp = warp >> 2; grp < NG; grp += kPassThreads / 128) {
+    const int m = grp * 128 + 32 * (warp & 3) + lane;
+    int g, j;
+    Tl::unpos(m, g, j);
+    // Twiddles of the next stage, W_L^(e0 + c*de) for outputs c = 0..15 (see
+    // below for e0, de). Line-minor tiles: the G lanes of a line group share
+    // the address, so each output's exact table value is one broadcast load.
+    // Line-major tiles (32 distinct addresses per load): exact table values
+    // at c = 0, 4, 8, 12 and the step W_L^de, read before the TMEM load so
+    // their latency overlaps it; the three values between two exact ones
+    // follow by multiplying with the step (at most three FP32 products from
+    // an exact value).
+    int e0_ = 0, de_ = 0;
+    float2 wq[4] = {}, wstep = make_float2(1.f, 0.f);
+    if constexpr (!LAST) {
+      const int rp_ = ((j / Ns) * 16 * Ns + j % Ns) / J;
+      e0_ = rp_ * (j % Ns) * (L / (256 * Ns));
+      de_ = rp_ * (L / 256);
+      if constexpr (!LINE_MINOR) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) wq[q] = __ldg(tw + e0_ + 4 * q * de_);
+        wstep = __ldg(tw + de_);
+      }
+    }
+    auto twiddle = [&](int c, float2& w) {
+      if constexpr (LINE_MINOR)
+        w = __ldg(tw + e0_ + c * de_);
+      else
+        w = (c & 3) == 0 ? wq[c >> 2] : cmulf(w, wstep);
+      return w;
+    };
     const uint32_t taddr = tbase + (static_cast<uint32_t>(32 * (warp & 3)) << 16) + grp * 64u;
     uint32_t d[32], e[32];
     tmem_ld_x32(taddr, d);
     tmem_ld_x32(taddr + 32u, e);
     tmem_ld_wait();
-    const int m = grp * 128 + 32 * (warp & 3) + lane;
-    int g, j;
-    Tl::unpos(m, g, j);
     float2 v[16];
 #pragma unroll
     for (int c = 0; c < 16; ++c)
@@ -101,17 +128,18 @@ __device__ __forceinline__ void split_stage_epilogue(const SplitPlanes& P, const
       const int lp0 = a * 16 * Ns + b;
       const int rp = lp0 / J;
       const int jp0 = lp0 % J;
-      const int e0 = rp * b * (L / (256 * Ns));
-      const int de = rp * (L / 256);
+      // next stage's twiddle exponents (read above): e0 = rp b L / (256 Ns),
+      // de = rp L / 256
       const uint32_t krow = (static_cast<uint32_t>(rp) >> 3) * Tl::KSTRIDE + (rp & 7) * 128u;
       constexpr uint32_t CSTEP = LINE_MINOR ? static_cast<uint32_t>(Ns * G) : static_cast<uint32_t>(Ns);
       if constexpr (Ns == 1 && !LINE_MINOR) {
         // 16 outputs -> 16 consecutive columns: per plane two 16-byte stores
         uint32_t prh[8], pih[8], prl[8], pil[8];
+        float2 w;
 #pragma unroll
         for (int c = 0; c < 16; c += 2) {
-          float2 x0 = cmulf(v[c], __ldg(tw + e0 + c * de));
-          float2 x1 = cmulf(v[c + 1], __ldg(tw + e0 + (c + 1) * de));
+          float2 x0 = cmulf(v[c], twiddle(c, w));
+          float2 x1 = cmulf(v[c + 1], twiddle(c + 1, w));
           x0 = make_float2(x0.x * 0.0625f, x0.y * 0.0625f);  // 2^-4 per stage
           x1 = make_float2(x1.x * 0.0625f, x1.y * 0.0625f);
           const __half2 hr = __floats2half2_rn(x0.x, x1.x), hi = __floats2half2_rn(x0.y, x1.y);
@@ -148,18 +176,19 @@ __device__ __forceinline__ void split_stage_epilogue(const SplitPlanes& P, const
           const uint32_t mp = mp0 + static_cast<uint32_t>(k) * CSTEP;
           offs[k] = krow + (mp >> 6) * 1024u + ((((mp & 63u) >> 3) ^ (rp & 7)) << 4) + (mp & 7u) * 2u;
         }
+        float2 w;
 #pragma unroll
         for (int c = 0; c < 16; ++c) {
-          float2 x = cmulf(v[c], __ldg(tw + e0 + c * de));
+          float2 x = cmulf(v[c], twiddle(c, w));
           x.x *= 0.0625f;
           x.y *= 0.0625f;
           st_pair_split(P, offs[c % PER] + static_cast<uint32_t>(c / PER) * 1024u, x);
         }
       } else {
+        float2 w;
 #pragma unroll
         for (int c = 0; c < 16; ++c) {
-          const float2 w = __ldg(tw + e0 + c * de);
-          float2 x = cmulf(v[c], w);
+          float2 x = cmulf(v[c], twiddle(c, w));
           x.x *= 0.0625f;  // 2^-4 per stage
           x.y *= 0.0625f;
           const uint32_t mp = static_cast<uint32_t>(Tl::pos(g, jp0 + c * Ns));

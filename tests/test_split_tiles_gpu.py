@@ -1,8 +1,8 @@
 """Every split-precision tile variant gives the transform within the split
 bound (GPU).
 
-tcfft_tune_set forces a variant (small 128-row tiles, big 512-row tiles at 2
-CTAs per SM, mid 256-row tiles at 3 CTAs per SM); results are compared with
+tcfft_tune_set forces a variant (small 128-row tiles, big 512-row tiles);
+results are compared with
 the FP64 oracle at REL_L2_SPLIT. Batches are ragged (not a multiple of the
 tile's lines) so the last tile is partly empty."""
 import ctypes
@@ -58,17 +58,18 @@ def test_split_row_tile_variants(tc, orc, n):
     assert seen
 
 
-def test_split_row_mid_inverse(tc, orc):
+def test_split_row_inverse_variants(tc, orc):
     n, batch = 4096, 9
     rng = np.random.default_rng(5)
     x = f32_round(uniform_complex(rng, (batch, n)))
+    ref = orc.fft1d(x, +1)
     try:
-        assert tc.lib().tcfft_tune_set(SPLIT, PASS_ROW, 12, 2) == 0
-        y = _run(tc, x, n, batch, direction=tc.INVERSE)
+        for t in _variants(tc, PASS_ROW, 12):
+            assert tc.lib().tcfft_tune_set(SPLIT, PASS_ROW, 12, t) == 0
+            err = orc.rel_l2(_run(tc, x, n, batch, direction=tc.INVERSE), ref)
+            assert err < REL_L2_SPLIT, (t, err)
     finally:
         tc.lib().tcfft_tune_set(SPLIT, PASS_ROW, 12, -1)
-    err = orc.rel_l2(y, orc.fft1d(x, +1))
-    assert err < REL_L2_SPLIT, err
 
 
 @pytest.mark.parametrize("n,log_n1", [(1 << 16, 9), (1 << 16, 8), (1 << 20, 9), (1 << 20, 10)])
