@@ -61,16 +61,25 @@ __device__ __forceinline__ float max_abs4(const float2 (&v)[4]) {
   return m;
 }
 
+// Each warp waits for its own group's MMAs (mbar[grp], committed per group)
+// before reading that group's accumulator, so TMEM reads (and, in the last
+// stage, the global stores) overlap the MMAs of later groups. Stores into
+// the planes wait for every group (mbar[NG - 1]): the planes are rewritten in
+// place, and a later group's MMAs may still be reading them. Returns false if
+// a bounded wait gave up (the group is then skipped).
 template <int L, int G, bool LINE_MINOR, int s, class IO>
-__device__ __forceinline__ void split_stage_epilogue(const SplitPlanes& P, const float2* __restrict__ tw,
+__device__ __forceinline__ bool split_stage_epilogue(const SplitPlanes& P, const float2* __restrict__ tw,
                                                      uint32_t tbase, int warp, int lane, const IO& io,
-                                                     long long line0, float out_scale) {
+                                                     long long line0, float out_scale, uint64_t* mbar,
+                                                     uint32_t parity) {
   using Sh = LineShape<L>;
   using Tl = Tile<L, G, LINE_MINOR>;
   constexpr int J = Sh::J;
   constexpr int NG = Tl::Mt / 128;
   constexpr int Ns = Sh::T << (4 * s);
   constexpr bool LAST = (s == Sh::S - 1);
+  bool ok = true;
+  bool planes_free = LAST;
 #pragma unroll 1
   for (int grp = warp >> 2; grp < NG; grp += kPassThreads / 128) {
     const int m = grp * 128 + 32 * (warp & 3) + lane;
@@ -103,6 +112,11 @@ __device__ __forceinline__ void split_stage_epilogue(const SplitPlanes& P, const
         w = (c & 3) == 0 ? wq[c >> 2] : cmulf(w, wstep);
       return w;
     };
+    if (!mbar_wait_bounded(mbar + grp, parity)) {
+      ok = false;
+      continue;
+    }
+    tc_fence_after_sync();
     const uint32_t taddr = tbase + (static_cast<uint32_t>(32 * (warp & 3)) << 16) + grp * 64u;
     uint32_t d[32], e[32];
     tmem_ld_x32(taddr, d);
@@ -124,6 +138,13 @@ __device__ __forceinline__ void split_stage_epilogue(const SplitPlanes& P, const
         io.store_row16(line, j, J, v);
       }
     } else {
+      if (!planes_free) {
+        if (!mbar_wait_bounded(mbar + (NG - 1), parity)) {
+          ok = false;
+          continue;
+        }
+        planes_free = true;
+      }
       const int a = j / Ns, b = j % Ns;
       const int lp0 = a * 16 * Ns + b;
       const int rp = lp0 / J;
@@ -198,12 +219,13 @@ __device__ __forceinline__ void split_stage_epilogue(const SplitPlanes& P, const
       }
     }
   }
+  return ok;
 }
 
 // ---------------------------------------------------------------------------
 // Split-precision tile machinery. Shared-memory layout:
 //   [0, 4096)      B matrix images (hi, lo)
-//   [4096, 4160)   mbarrier, TMEM slot, tile maximum
+//   [4096, 4160)   mbarriers (one per 128-row group), TMEM slot, tile maximum
 //   [5120, ...)    four planes (re hi, im hi, re lo, im lo), 1024-aligned
 // ---------------------------------------------------------------------------
 constexpr uint32_t kSplitPlaneOffset = 5120;
@@ -212,12 +234,14 @@ struct SplitState {
   uint8_t* smem;
   uint8_t* bhi;
   uint8_t* blo;
-  uint64_t* mbar;
+  uint64_t* mbar;  // kSplitMaxGroups mbarriers: MMA completion per 128-row group
   uint32_t* tslot;
   int* smax;
   uint32_t tbase;
   uint32_t phase;
 };
+
+constexpr int kSplitMaxGroups = 4;  // Mt <= 512
 
 template <uint32_t TMEM_COLS>
 __device__ __forceinline__ void split_setup(SplitState& st, const uint32_t* __restrict__ bmat_g) {
@@ -225,11 +249,12 @@ __device__ __forceinline__ void split_setup(SplitState& st, const uint32_t* __re
   st.bhi = st.smem;
   st.blo = st.smem + 2048;
   st.mbar = reinterpret_cast<uint64_t*>(st.smem + 4096);
-  st.tslot = reinterpret_cast<uint32_t*>(st.smem + 4112);
-  st.smax = reinterpret_cast<int*>(st.smem + 4128);
+  st.tslot = reinterpret_cast<uint32_t*>(st.smem + 4096 + 8 * kSplitMaxGroups);
+  st.smax = reinterpret_cast<int*>(st.smem + 4096 + 8 * kSplitMaxGroups + 8);
   const int tid = threadIdx.x;
   for (int i = tid; i < 1024; i += kPassThreads) reinterpret_cast<uint32_t*>(st.bhi)[i] = __ldg(bmat_g + i);
-  if (tid == 0) mbar_init(st.mbar, 1);
+  if (tid == 0)
+    for (int k = 0; k < kSplitMaxGroups; ++k) mbar_init(st.mbar + k, 1);
   if ((tid >> 5) == 0) {
     tmem_alloc(st.tslot, TMEM_COLS);
     tmem_relinquish();
@@ -268,7 +293,7 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
   constexpr int NG = Mt / 128;
   constexpr uint32_t PLANE = Tl::PLANE;
   constexpr uint32_t KSTRIDE = Tl::KSTRIDE;
-  static_assert(Mt % 128 == 0 && Mt <= 512, "tile size");
+  static_assert(Mt % 128 == 0 && Mt / 128 <= kSplitMaxGroups, "tile size");
   static_assert(G % 4 == 0 || IO::IN_VEC_L, "line-vectorised loads need G % 4 == 0");
   // N = 64: B_hi (2 KiB) and B_lo (the next 2 KiB) side by side form one
   // K-major operand (SBO 512 B), so D = [A * B_hi | A * B_lo]
@@ -458,21 +483,16 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
           umma_f16(dacc, a_ih, bh1, IDESC, 1u);
           umma_f16(dacc, a_rl, bh0, IDESC, 1u);
           umma_f16(dacc, a_il, bh1, IDESC, 1u);
+          umma_commit(st.mbar + grp);  // this group and every earlier one
         }
-        umma_commit(st.mbar);
       }
-      bool to = !mbar_wait_bounded(st.mbar, st.phase & 1u);
+      const bool to = !split_stage_epilogue<L, G, LINE_MINOR, s, IO>(P, core.tw, st.tbase, warp, lane, io, line0,
+                                                                     out_scale, st.mbar, st.phase & 1u);
       if (to && lane == 0) atomicOr(core.err, kErrMmaTimeout);
       st.phase++;
-      if (__syncthreads_or(to)) {
-        timed_out = true;
-        return;
-      }
-      tc_fence_after_sync();
-      split_stage_epilogue<L, G, LINE_MINOR, s, IO>(P, core.tw, st.tbase, warp, lane, io, line0, out_scale);
       fence_proxy_async_smem();
       tc_fence_before_sync();
-      __syncthreads();
+      if (__syncthreads_or(to)) timed_out = true;
     };
     [&]<int... Is>(std::integer_sequence<int, Is...>) {
       (run_stage(std::integral_constant<int, Is>{}), ...);
