@@ -282,8 +282,15 @@ __host__ __device__ constexpr uint32_t split_tmem_cols() {
 // One split-precision tile: G lines of length L starting at line0. Same
 // geometry rules as pass_tile, with G * L / 16 in {128, 256, 512} (4 planes
 // + 64 TMEM columns per 128 rows). False if a bounded wait gave up.
+// IO types that can hint the next tile's input into L2.
+template <class IO>
+concept L2PrefetchIo = requires(const IO& io) { io.prefetch_tile_l2(0ll, 0, 0); };
+
+// next_line0 >= 0: the tile this CTA processes next, whose input is
+// prefetched into L2 while this one runs.
 template <int L, int G, bool LINE_MINOR, int SIGN, class IO>
-__device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const PassCore& core, long long line0) {
+__device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const PassCore& core, long long line0,
+                                           long long next_line0 = -1) {
   using Sh = LineShape<L>;
   using Tl = Tile<L, G, LINE_MINOR>;
   constexpr int T = Sh::T;
@@ -305,6 +312,9 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
   const int warp = tid >> 5;
   const int lane = tid & 31;
   bool timed_out = false;
+  if constexpr (L2PrefetchIo<IO>) {
+    if (next_line0 >= 0) io.prefetch_tile_l2(next_line0, G, L);
+  }
     if (tid == 0) *st.smax = 0;
     __syncthreads();
 
@@ -510,8 +520,10 @@ __global__ void __launch_bounds__(kPassThreads, 2) fft_pass_split(const IO io, c
   SplitState st;
   split_setup<TMEM_COLS>(st, core.bmat);
   const long long ntiles = (io.total_lines + G - 1) / G;
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
-    if (!split_tile<L, G, LINE_MINOR, SIGN, IO>(st, io, core, tile * G)) break;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long long next = tile + gridDim.x < ntiles ? (tile + gridDim.x) * G : -1;
+    if (!split_tile<L, G, LINE_MINOR, SIGN, IO>(st, io, core, tile * G, next)) break;
+  }
   split_teardown<TMEM_COLS>(st);
 }
 
@@ -547,6 +559,30 @@ struct IoFloat {
   }
   __device__ __forceinline__ long long out_base(long long line) const {
     return (line >> lps_log2) * out_seq + (line & ((1ll << lps_log2) - 1)) * out_line;
+  }
+  // L2 prefetch of the input of lines [line0, line0 + g) of length l:
+  // contiguous lines (IN_L) one range per line; column layout (adjacent
+  // lines adjacent in memory, in_line == 1) one range of g elements per line
+  // element. Called by every thread of the CTA; lines past the end are left
+  // out.
+  __device__ __forceinline__ void prefetch_tile_l2(long long line0, int g, int l) const {
+    const int tid = threadIdx.x;
+    if constexpr (IN_L) {
+      for (int k = tid; k < g; k += blockDim.x) {
+        const long long line = line0 + k;
+        if (line < total_lines) prefetch_l2_bulk(in + in_base(line), static_cast<uint32_t>(l) * 8u);
+      }
+    } else {
+      if (in_line != 1) return;
+      const long long rem = total_lines - line0;
+      const int lines = rem < g ? static_cast<int>(rem) : g;
+      if (lines <= 0 || (lines & 1)) return;  // ranges of whole 16-byte units
+      // the lines must lie in one sequence (adjacent in memory)
+      if ((line0 >> lps_log2) != ((line0 + lines - 1) >> lps_log2)) return;
+      const float2* base = in + in_base(line0);
+      for (int e = tid; e < l; e += blockDim.x)
+        prefetch_l2_bulk(base + static_cast<long long>(e) * in_elem, static_cast<uint32_t>(lines) * 8u);
+    }
   }
   __device__ __forceinline__ Raw fetch_l(long long line, int l0, bool ok) const {
     Raw r{make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};

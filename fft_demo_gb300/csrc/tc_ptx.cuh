@@ -245,6 +245,11 @@ __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc, uin
                "r"(src_bytes)
                : "memory");
 }
+// Bulk prefetch of [gsrc, gsrc + bytes) into L2 (a hint: no data moves to
+// the SM). gsrc 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void prefetch_l2_bulk(const void* gsrc, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(gsrc), "r"(bytes) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
