@@ -608,15 +608,29 @@ struct IoFloat {
   }
   __device__ __forceinline__ void decode_l(const Raw& r, long long, int, float2 (&v)[4]) const { unpack(r, v); }
   __device__ __forceinline__ void decode_g(const Raw& r, long long, int, float2 (&v)[4]) const { unpack(r, v); }
-  // Outer twiddle taken exactly from the tables per element (FP32 accuracy).
+  // Outputs l = j + c*J (c = 0..15) of one line. The outer twiddle
+  // W_N^{li*l} is exact (two-level table) at c = 0, 4, 8, 12; in between it
+  // follows from the exact step W_N^{li*J} (at most three FP32 products from
+  // an exact value), so a row costs 5 table pairs instead of 16.
   __device__ __forceinline__ void store_row16(long long line, int j, int J, float2 (&v)[16]) const {
     float2* p = out + out_base(line);
     const long long li = line & ((1ll << lps_log2) - 1);
+    if (otw.hi) {
+      float2 wq[4];
 #pragma unroll
-    for (int c = 0; c < 16; ++c) {
-      float2 x = v[c];
-      if (otw.hi) x = cmulf(x, otw(li, j + c * J));
-      p[static_cast<long long>(j + c * J) * out_elem] = make_float2(x.x * scale, x.y * scale);
+      for (int q = 0; q < 4; ++q) wq[q] = otw(li, j + 4 * q * J);
+      const float2 step = otw(li, J);
+      float2 w = wq[0];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        w = (c & 3) == 0 ? wq[c >> 2] : cmulf(w, step);
+        const float2 x = cmulf(v[c], w);
+        p[static_cast<long long>(j + c * J) * out_elem] = make_float2(x.x * scale, x.y * scale);
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < 16; ++c)
+        p[static_cast<long long>(j + c * J) * out_elem] = make_float2(v[c].x * scale, v[c].y * scale);
     }
   }
 };
