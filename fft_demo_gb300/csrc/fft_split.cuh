@@ -86,13 +86,13 @@ __device__ __forceinline__ bool split_stage_epilogue(const SplitPlanes& P, const
     int g, j;
     Tl::unpos(m, g, j);
     // Twiddles of the next stage, W_L^(e0 + c*de) for outputs c = 0..15 (see
-    // below for e0, de). Line-minor tiles: the G lanes of a line group share
-    // the address, so each output's exact table value is one broadcast load.
-    // Line-major tiles (32 distinct addresses per load): exact table values
-    // at c = 0, 4, 8, 12 and the step W_L^de, read before the TMEM load so
-    // their latency overlaps it; the three values between two exact ones
-    // follow by multiplying with the step (at most three FP32 products from
-    // an exact value).
+    // below for e0, de), each times the stage's 2^-4 (exact). Line-minor
+    // tiles: the G lanes of a line group share the address, so each output's
+    // exact table value is one broadcast load. Line-major tiles (32 distinct
+    // addresses per load): exact table values at c = 0, 4, 8, 12 and the
+    // step W_L^de, read before the TMEM load so their latency overlaps it;
+    // the three values between two exact ones follow by multiplying with the
+    // step (at most three FP32 products from an exact value).
     int e0_ = 0, de_ = 0;
     float2 wq[4] = {}, wstep = make_float2(1.f, 0.f);
     if constexpr (!LAST) {
@@ -101,15 +101,20 @@ __device__ __forceinline__ bool split_stage_epilogue(const SplitPlanes& P, const
       de_ = rp_ * (L / 256);
       if constexpr (!LINE_MINOR) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) wq[q] = __ldg(tw + e0_ + 4 * q * de_);
+        for (int q = 0; q < 4; ++q) {
+          const float2 t = __ldg(tw + e0_ + 4 * q * de_);
+          wq[q] = make_float2(t.x * 0.0625f, t.y * 0.0625f);
+        }
         wstep = __ldg(tw + de_);
       }
     }
     auto twiddle = [&](int c, float2& w) {
-      if constexpr (LINE_MINOR)
-        w = __ldg(tw + e0_ + c * de_);
-      else
+      if constexpr (LINE_MINOR) {
+        const float2 t = __ldg(tw + e0_ + c * de_);
+        w = make_float2(t.x * 0.0625f, t.y * 0.0625f);
+      } else {
         w = (c & 3) == 0 ? wq[c >> 2] : cmulf(w, wstep);
+      }
       return w;
     };
     if (!mbar_wait_bounded(mbar + grp, parity)) {
@@ -161,8 +166,6 @@ __device__ __forceinline__ bool split_stage_epilogue(const SplitPlanes& P, const
         for (int c = 0; c < 16; c += 2) {
           float2 x0 = cmulf(v[c], twiddle(c, w));
           float2 x1 = cmulf(v[c + 1], twiddle(c + 1, w));
-          x0 = make_float2(x0.x * 0.0625f, x0.y * 0.0625f);  // 2^-4 per stage
-          x1 = make_float2(x1.x * 0.0625f, x1.y * 0.0625f);
           const __half2 hr = __floats2half2_rn(x0.x, x1.x), hi = __floats2half2_rn(x0.y, x1.y);
           const float2 fr = __half22float2(hr), fi = __half22float2(hi);
           const __half2 lr = __floats2half2_rn(x0.x - fr.x, x1.x - fr.y);
@@ -201,8 +204,6 @@ __device__ __forceinline__ bool split_stage_epilogue(const SplitPlanes& P, const
 #pragma unroll
         for (int c = 0; c < 16; ++c) {
           float2 x = cmulf(v[c], twiddle(c, w));
-          x.x *= 0.0625f;
-          x.y *= 0.0625f;
           st_pair_split(P, offs[c % PER] + static_cast<uint32_t>(c / PER) * 1024u, x);
         }
       } else {
@@ -210,8 +211,6 @@ __device__ __forceinline__ bool split_stage_epilogue(const SplitPlanes& P, const
 #pragma unroll
         for (int c = 0; c < 16; ++c) {
           float2 x = cmulf(v[c], twiddle(c, w));
-          x.x *= 0.0625f;  // 2^-4 per stage
-          x.y *= 0.0625f;
           const uint32_t mp = static_cast<uint32_t>(Tl::pos(g, jp0 + c * Ns));
           const uint32_t off = krow + (mp >> 6) * 1024u + ((((mp & 63u) >> 3) ^ (rp & 7)) << 4) + (mp & 7u) * 2u;
           st_pair_split(P, off, x);
