@@ -54,6 +54,39 @@ __device__ __forceinline__ void st_quad_split(const SplitPlanes& P, uint32_t off
   *reinterpret_cast<uint2*>(P.il + off) = *reinterpret_cast<uint2*>(il);
 }
 
+// N consecutive m in one K row (N = 2, 4, 8; offset 2N-byte aligned, inside
+// one 16-byte chunk): one 2N-byte store per plane.
+template <int N>
+__device__ __forceinline__ void st_run_split(const SplitPlanes& P, uint32_t off, const float2 (&x)[N]) {
+  static_assert(N == 2 || N == 4 || N == 8, "run length");
+  uint32_t rh[N / 2], rl[N / 2], ih[N / 2], il[N / 2];
+#pragma unroll
+  for (int k = 0; k < N / 2; ++k) {
+    const __half2 hr = __floats2half2_rn(x[2 * k].x, x[2 * k + 1].x);
+    const __half2 hi = __floats2half2_rn(x[2 * k].y, x[2 * k + 1].y);
+    const float2 fr = __half22float2(hr), fi = __half22float2(hi);
+    const __half2 lr = __floats2half2_rn(x[2 * k].x - fr.x, x[2 * k + 1].x - fr.y);
+    const __half2 li = __floats2half2_rn(x[2 * k].y - fi.x, x[2 * k + 1].y - fi.y);
+    rh[k] = *reinterpret_cast<const uint32_t*>(&hr);
+    ih[k] = *reinterpret_cast<const uint32_t*>(&hi);
+    rl[k] = *reinterpret_cast<const uint32_t*>(&lr);
+    il[k] = *reinterpret_cast<const uint32_t*>(&li);
+  }
+  auto put = [&](uint8_t* plane, const uint32_t (&w)[N / 2]) {
+    if constexpr (N == 2) {
+      *reinterpret_cast<uint32_t*>(plane + off) = w[0];
+    } else if constexpr (N == 4) {
+      *reinterpret_cast<uint2*>(plane + off) = make_uint2(w[0], w[1]);
+    } else {
+      *reinterpret_cast<uint4*>(plane + off) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+  };
+  put(P.rh, rh);
+  put(P.ih, ih);
+  put(P.rl, rl);
+  put(P.il, il);
+}
+
 __device__ __forceinline__ float max_abs4(const float2 (&v)[4]) {
   float m = 0.f;
 #pragma unroll
@@ -342,21 +375,25 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
       constexpr int QPL = (L / T) / 4;
       constexpr int ITEMS = G * QPL;
       static_assert(ITEMS <= kPassThreads * U, "one load batch per tile");
+      // item -> (line g, first of four consecutive butterflies j0): a warp's
+      // loads run along one line
+      auto item_g = [](int it) { return it / QPL; };
+      auto item_j0 = [](int it) { return (it % QPL) * 4; };
       typename IO::Raw raw[U][T];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const int it = tid + u * kPassThreads;
 #pragma unroll
         for (int r = 0; r < T; ++r)
-          raw[u][r] = io.fetch_l(line0 + it / QPL, (it % QPL) * 4 + r * (L / T), it < ITEMS);
+          raw[u][r] = io.fetch_l(line0 + item_g(it), item_j0(it) + r * (L / T), it < ITEMS);
       }
       float2 v[U][T][4];
       float lmax = 0.f;
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const int it = tid + u * kPassThreads;
-        const int g = it / QPL;
-        const int j0 = (it % QPL) * 4;
+        const int g = item_g(it);
+        const int j0 = item_j0(it);
 #pragma unroll
         for (int r = 0; r < T; ++r) {
           io.decode_l(raw[u][r], line0 + g, j0 + r * (L / T), v[u][r]);
@@ -368,8 +405,8 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
       for (int u = 0; u < U; ++u) {
         const int it = tid + u * kPassThreads;
         if (ITEMS % (kPassThreads * U) != 0 && it >= ITEMS) continue;
-        const int g = it / QPL;
-        const int j0 = (it % QPL) * 4;
+        const int g = item_g(it);
+        const int j0 = item_j0(it);
 #pragma unroll
         for (int r = 0; r < T; ++r)
 #pragma unroll
@@ -385,6 +422,19 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
             for (int q = 0; q < 4; ++q) st_pair_split(P, Tl::off(g, j0 + q), v[u][0][q]);
           }
         } else {
+          // Output c of butterfly j goes to l' = j*T + c: K row rp = j*T / J
+          // for every c (T divides J), column (j*T + c) % J, twiddle
+          // W_L^(rp c L / (16T)) = W_(16T)^(rp c). When J / T is a multiple
+          // of 4 the item's four butterflies share rp and its T twiddles are
+          // read once.
+          constexpr bool SHARED_RP = ((J / T) % 4) == 0;
+          float2 wt[T];
+          auto load_tw = [&](int rp) {
+            wt[0] = make_float2(1.f, 0.f);
+#pragma unroll
+            for (int c = 1; c < T; ++c) wt[c] = __ldg(core.tw + rp * c * (L / (16 * T)));
+          };
+          if constexpr (SHARED_RP) load_tw((j0 * T) / J);
 #pragma unroll
           for (int q = 0; q < 4; ++q) {
             float2 t[T];
@@ -392,12 +442,15 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
             for (int r = 0; r < T; ++r) t[r] = v[u][r][q];
             small_dft<T, SIGN>(t);
             const int j = j0 + q;
+            if constexpr (!SHARED_RP) load_tw((j * T) / J);
 #pragma unroll
-            for (int c = 0; c < T; ++c) {
-              const int lp = j * T + c;
-              const int rp = lp / J, jp = lp % J;
-              const float2 w = __ldg(core.tw + rp * (jp % T) * (L / (16 * T)));
-              st_pair_split(P, Tl::off(g, lp), cmulf(t[c], w));
+            for (int c = 1; c < T; ++c) t[c] = cmulf(t[c], wt[c]);
+            if constexpr (!LINE_MINOR) {
+              // T consecutive columns of one K row: one store per plane
+              st_run_split<T>(P, Tl::off(g, j * T), t);
+            } else {
+#pragma unroll
+              for (int c = 0; c < T; ++c) st_pair_split(P, Tl::off(g, j * T + c), t[c]);
             }
           }
         }
