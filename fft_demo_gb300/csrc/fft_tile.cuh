@@ -168,6 +168,31 @@ __device__ __forceinline__ void st_quad(uint8_t* re, uint8_t* im, uint32_t off, 
   *reinterpret_cast<uint2*>(im + off) = ii;
 }
 
+// N consecutive m in one K row (N = 2, 4, 8; offset 2N-byte aligned, inside
+// one 16-byte chunk): one 2N-byte store per plane.
+template <int N>
+__device__ __forceinline__ void st_run(uint8_t* re, uint8_t* im, uint32_t off, const float2 (&x)[N]) {
+  static_assert(N == 2 || N == 4 || N == 8, "run length");
+  uint32_t rr[N / 2], ii[N / 2];
+#pragma unroll
+  for (int k = 0; k < N / 2; ++k) {
+    const __half2 hr = __floats2half2_rn(x[2 * k].x, x[2 * k + 1].x);
+    const __half2 hi = __floats2half2_rn(x[2 * k].y, x[2 * k + 1].y);
+    rr[k] = *reinterpret_cast<const uint32_t*>(&hr);
+    ii[k] = *reinterpret_cast<const uint32_t*>(&hi);
+  }
+  if constexpr (N == 2) {
+    *reinterpret_cast<uint32_t*>(re + off) = rr[0];
+    *reinterpret_cast<uint32_t*>(im + off) = ii[0];
+  } else if constexpr (N == 4) {
+    *reinterpret_cast<uint2*>(re + off) = make_uint2(rr[0], rr[1]);
+    *reinterpret_cast<uint2*>(im + off) = make_uint2(ii[0], ii[1]);
+  } else {
+    *reinterpret_cast<uint4*>(re + off) = make_uint4(rr[0], rr[1], rr[2], rr[3]);
+    *reinterpret_cast<uint4*>(im + off) = make_uint4(ii[0], ii[1], ii[2], ii[3]);
+  }
+}
+
 __device__ __forceinline__ void ld_quad(const uint8_t* re, const uint8_t* im, uint32_t off, float2 (&x)[4]) {
   const uint2 rr = *reinterpret_cast<const uint2*>(re + off);
   const uint2 ii = *reinterpret_cast<const uint2*>(im + off);
@@ -802,7 +827,71 @@ __device__ __forceinline__ void permute_raw(const uint8_t* raw, uint8_t* re, uin
   constexpr int J = Sh::J;
   const int tid = threadIdx.x;
   const uint4 zero = make_uint4(0, 0, 0, 0);
-  if constexpr (IO::IN_VEC_L) {
+  if constexpr (IO::IN_VEC_L && LINE_MINOR && G % 4 == 0) {
+    // Line-minor tile from line-major raw input: item = LPI adjacent lines
+    // at one butterfly j (butterflies fastest across lanes, so the raw reads
+    // are consecutive words), so every output is LPI consecutive columns:
+    // one 2*LPI-byte store per plane, one twiddle read shared by the lines.
+    // LPI = 2 for the radix-8 tail keeps the item's values in registers.
+    constexpr int LPI = T == 8 ? 2 : 4;
+    constexpr int JT = L / T;
+    constexpr int ITEMS = (G / LPI) * JT;
+    const uint32_t* raw32 = reinterpret_cast<const uint32_t*>(raw);
+#pragma unroll 2
+    for (int it = tid; it < ITEMS; it += kPassThreads) {
+      const int j = it % JT;
+      const int g0 = (it / JT) * LPI;
+      uint32_t w[T][LPI];
+#pragma unroll
+      for (int r = 0; r < T; ++r)
+#pragma unroll
+        for (int k = 0; k < LPI; ++k)
+          w[r][k] = g0 + k < nval ? raw32[static_cast<uint32_t>(g0 + k) * L + j + r * JT] : 0u;
+      if constexpr (T == 1) {
+        uint2 rr, ii;
+        rr.x = __byte_perm(w[0][0], w[0][1], 0x5410);
+        rr.y = __byte_perm(w[0][2], w[0][3], 0x5410);
+        ii.x = __byte_perm(w[0][0], w[0][1], 0x7632);
+        ii.y = __byte_perm(w[0][2], w[0][3], 0x7632);
+        const uint32_t off = Tl::off(g0, j);
+        *reinterpret_cast<uint2*>(re + off) = rr;
+        *reinterpret_cast<uint2*>(im + off) = ii;
+      } else {
+        float2 v[T][LPI];
+#pragma unroll
+        for (int r = 0; r < T; ++r)
+#pragma unroll
+          for (int k = 0; k < LPI; ++k) v[r][k] = __half22float2(*reinterpret_cast<const __half2*>(&w[r][k]));
+#pragma unroll
+        for (int k = 0; k < LPI; ++k) {
+          float2 t[T];
+#pragma unroll
+          for (int r = 0; r < T; ++r) t[r] = v[r][k];
+          small_dft<T, SIGN>(t);
+#pragma unroll
+          for (int r = 0; r < T; ++r) v[r][k] = t[r];
+        }
+        // output c -> l' = j*T + c, twiddle W_(16T)^(rp c), rp = j*T / J
+        const int rp = (j * T) / J;
+#pragma unroll
+        for (int c = 0; c < T; ++c) {
+          float2 x[LPI];
+#pragma unroll
+          for (int k = 0; k < LPI; ++k) x[k] = v[c][k];
+          if (c > 0) {
+            const float2 tw = __ldg(core.tw + rp * c * (L / (16 * T)));
+#pragma unroll
+            for (int k = 0; k < LPI; ++k) x[k] = cmulf(x[k], tw);
+          }
+          if constexpr (LPI == 4) {
+            st_quad(re, im, Tl::off(g0, j * T + c), x);
+          } else {
+            st_run<2>(re, im, Tl::off(g0, j * T + c), x);
+          }
+        }
+      }
+    }
+  } else if constexpr (IO::IN_VEC_L) {
     constexpr int QPL = (L / T) / 4;
     constexpr int ITEMS = G * QPL;
 #pragma unroll 2
@@ -827,6 +916,17 @@ __device__ __forceinline__ void permute_raw(const uint8_t* raw, uint8_t* re, uin
         float2 v[T][4];
 #pragma unroll
         for (int r = 0; r < T; ++r) unpack_h2x4(w[r], v[r]);
+        // output c of butterfly j -> l' = j*T + c: K row rp = j*T / J for
+        // every c, twiddle W_(16T)^(rp c); the item's four butterflies share
+        // rp when J / T is a multiple of 4
+        constexpr bool SHARED_RP = ((J / T) % 4) == 0 && T <= 4;
+        float2 wt[T];
+        auto load_tw = [&](int rp) {
+          wt[0] = make_float2(1.f, 0.f);
+#pragma unroll
+          for (int c = 1; c < T; ++c) wt[c] = __ldg(core.tw + rp * c * (L / (16 * T)));
+        };
+        if constexpr (T > 1 && SHARED_RP) load_tw((j0 * T) / J);
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           float2 t[T];
@@ -834,15 +934,14 @@ __device__ __forceinline__ void permute_raw(const uint8_t* raw, uint8_t* re, uin
           for (int r = 0; r < T; ++r) t[r] = v[r][q];
           small_dft<T, SIGN>(t);
           const int j = j0 + q;
+          if constexpr (T > 1 && !SHARED_RP) load_tw((j * T) / J);
 #pragma unroll
-          for (int c = 0; c < T; ++c) {
-            const int lp = j * T + c;
-            float2 x = t[c];
-            if constexpr (T > 1) {
-              const int rp = lp / J, jp = lp % J;
-              x = cmulf(x, __ldg(core.tw + rp * (jp % T) * (L / (16 * T))));
-            }
-            st_pair(re, im, Tl::off(g, lp), x);
+          for (int c = 1; c < T; ++c) t[c] = cmulf(t[c], wt[c]);
+          if constexpr (!LINE_MINOR && T > 1) {
+            st_run<T>(re, im, Tl::off(g, j * T), t);  // T consecutive columns of K row rp
+          } else {
+#pragma unroll
+            for (int c = 0; c < T; ++c) st_pair(re, im, Tl::off(g, j * T + c), t[c]);
           }
         }
       }
