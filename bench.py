@@ -398,17 +398,21 @@ def main():
     for _ in range(3):
         e2e_step()
     torch.cuda.synchronize()
+    # three timed windows, median reported: host<->device copy bandwidth on
+    # this shared host varies from run to run with other tenants' traffic
     e2e_steps = max(2, args.steps // 2)
-    barrier(world)
-    t0 = time.perf_counter()
-    q0 = torch.cuda.Event(enable_timing=True)
-    q1 = torch.cuda.Event(enable_timing=True)
-    q0.record(stream)
-    for _ in range(e2e_steps):
-        e2e_step()
-    q1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = max_over_ranks(world, q0.elapsed_time(q1)) / e2e_steps
+    windows = []
+    for _ in range(3):
+        barrier(world)
+        q0 = torch.cuda.Event(enable_timing=True)
+        q1 = torch.cuda.Event(enable_timing=True)
+        q0.record(stream)
+        for _ in range(e2e_steps):
+            e2e_step()
+        q1.record(stream)
+        torch.cuda.synchronize()
+        windows.append(max_over_ranks(world, q0.elapsed_time(q1)) / e2e_steps)
+    e2e_ms = sorted(windows)[1]
     e2e_value = whole_job_rate(step_flops, world, e2e_ms) / 1e9
     # the pipelined results equal the device-timed ones (same inputs)
     e2e_match = all(torch.equal(ho[:2].to(dev), y[:2]) for ho, y in zip(host_out, ys))
@@ -453,6 +457,7 @@ def main():
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "GFLOP/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+                    "ms_per_step_windows": windows,
                     "pipeline": "%d sub-batches per size; copy in, transform, copy out on three streams"
                                 % E2E_CHUNKS, "results_match_device_path": bool(e2e_match)},
             "gpu_launches": gpu_launches,
