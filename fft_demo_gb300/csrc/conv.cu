@@ -104,6 +104,56 @@ __global__ void conv_pointwise_kernel(const E* __restrict__ X, const E* __restri
   }
 }
 
+// Pointwise stage on paired spectra. Input plane q (of nqp) holds
+// Z = X_2q + i X_2q+1, the spectra of two real images (flattened index
+// b * S + s); output plane p holds W = Y_2p + i Y_2p+1 for outputs
+// o = b * F + f. Since each X is the spectrum of a real image,
+// X(k) = conj X(-k), so X_2q = (Z(k) + conj Z(-k)) / 2 and
+// X_2q+1 = (Z(k) - conj Z(-k)) / (2i), -k = ((P - ky) mod P, (P - kx) mod P).
+// A last unpaired image or output is the plane itself.
+template <class E>
+__global__ void conv_pointwise_pair_kernel(const E* __restrict__ Zin, const E* __restrict__ K, E* __restrict__ W,
+                                           int P, int S, int F, long long n_img, long long n_out) {
+  const long long plane = static_cast<long long>(P) * P;
+  const long long n_pairs_out = (n_out + 1) / 2;
+  const long long total = n_pairs_out * plane;
+  for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
+       t += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const long long i = t % plane;
+    const long long po = t / plane;
+    const int ky = static_cast<int>(i / P), kx = static_cast<int>(i % P);
+    const long long im = static_cast<long long>((P - ky) & (P - 1)) * P + ((P - kx) & (P - 1));
+    float2 y[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const long long o = 2 * po + e;
+      if (o >= n_out) break;
+      const long long b = o / F;
+      const int f = static_cast<int>(o % F);
+      float2 acc = make_float2(0.f, 0.f);
+      for (int sidx = 0; sidx < S; ++sidx) {
+        const long long q = b * S + sidx;
+        const long long zq = q / 2;
+        const float2 z = from_elem(Zin[zq * plane + i]);
+        float2 x;
+        if (2 * zq + 1 >= n_img) {
+          x = z;  // unpaired image
+        } else {
+          const float2 zm = from_elem(Zin[zq * plane + im]);
+          x = (q & 1) ? make_float2(0.5f * (z.y + zm.y), 0.5f * (zm.x - z.x))
+                      : make_float2(0.5f * (z.x + zm.x), 0.5f * (z.y - zm.y));
+        }
+        const float2 k = from_elem(K[(static_cast<long long>(f) * S + sidx) * plane + i]);
+        acc.x += x.x * k.x - x.y * k.y;
+        acc.y += x.x * k.y + x.y * k.x;
+      }
+      y[e] = acc;
+    }
+    // W = Y_2p + i Y_2p+1
+    W[t] = to_elem<E>(make_float2(y[0].x - y[1].y, y[0].y + y[1].x));
+  }
+}
+
 }  // namespace
 
 struct tcfftConvImpl {
@@ -171,11 +221,13 @@ T zero_io() {
 // for correlation filters.
 template <class R, class E>
 tcfftStatus conv_row_fwd(tcfftConvImpl* c, int pass, const R* in, E* out, long long count, int rows, int cols,
-                         int flip, float scale, cudaStream_t st) {
+                         int flip, float scale, cudaStream_t st, bool pair = false) {
   auto io = zero_io<IoRealRowIn<R, E>>();
   io.in = in;
   io.out = out;
-  io.total_lines = count * rows;
+  io.pair = pair ? 1 : 0;
+  io.n_images = count;
+  io.total_lines = (pair ? (count + 1) / 2 : count) * rows;
   io.sy = rows;
   io.sx = cols;
   io.P = c->P;
@@ -201,12 +253,17 @@ tcfftStatus conv_col(tcfftConvImpl* c, int pass, int sign_idx, const E* in, E* o
   return conv_launch(c, pass, sign_idx, io, st);
 }
 
+// count = output images; pair: the input holds (count + 1) / 2 paired planes
 template <class E, class RO>
-tcfftStatus conv_row_inv(tcfftConvImpl* c, const E* in, RO* out, long long count, float scale, cudaStream_t st) {
+tcfftStatus conv_row_inv(tcfftConvImpl* c, const E* in, RO* out, long long count, float scale, cudaStream_t st,
+                         bool pair = false) {
   auto io = zero_io<IoRowCropReal<E, RO>>();
   io.in = in;
   io.out = out;
-  io.total_lines = count * c->oy;
+  io.pair = pair ? 1 : 0;
+  io.rows = c->oy;
+  io.n_out = count;
+  io.total_lines = (pair ? (count + 1) / 2 : count) * c->oy;
   io.P = c->P;
   io.c0 = c->c0;
   io.nc = c->ox;
@@ -221,17 +278,28 @@ tcfftStatus conv_run(tcfftConvImpl* c, const RI* images, RI* out, long long batc
   E* Xf = static_cast<E*>(c->Xf);
   E* Y = static_cast<E*>(c->Y);
   E* Z = static_cast<E*>(c->Z);
-  tcfftStatus s = conv_row_fwd<RI, E>(c, kConvRowFwdImg, images, X, batch * c->S, c->sy, c->sx, 0, inv_p, st);
-  if (s == TCFFT_OK) s = conv_col<E>(c, kConvColFwd, 0, X, Xf, batch * c->S, c->sy, 0, c->P, inv_p, st);
+  // Two real images per complex transform (real part, imaginary part) on
+  // both sides whenever there are at least two: the forward passes run on
+  // ceil(batch*S / 2) planes, the inverse ones on ceil(batch*F / 2).
+  const long long n_img = batch * c->S, n_out = batch * c->F;
+  const bool pair = n_img > 1 || n_out > 1;
+  const long long n_img_planes = pair ? (n_img + 1) / 2 : n_img;
+  const long long n_out_planes = pair ? (n_out + 1) / 2 : n_out;
+  tcfftStatus s = conv_row_fwd<RI, E>(c, kConvRowFwdImg, images, X, n_img, c->sy, c->sx, 0, inv_p, st, pair);
+  if (s == TCFFT_OK) s = conv_col<E>(c, kConvColFwd, 0, X, Xf, n_img_planes, c->sy, 0, c->P, inv_p, st);
   if (s == TCFFT_OK) {
     const long long plane = static_cast<long long>(c->P) * c->P;
-    const long long total = batch * c->F * plane;
-    conv_pointwise_kernel<E><<<static_cast<unsigned>(g_conv_sms * 8), 256, 0, st>>>(
-        Xf, static_cast<const E*>(c->K), Y, plane, c->S, c->F, total);
+    if (pair) {
+      conv_pointwise_pair_kernel<E><<<static_cast<unsigned>(g_conv_sms * 8), 256, 0, st>>>(
+          Xf, static_cast<const E*>(c->K), Y, c->P, c->S, c->F, n_img, n_out);
+    } else {
+      conv_pointwise_kernel<E><<<static_cast<unsigned>(g_conv_sms * 8), 256, 0, st>>>(
+          Xf, static_cast<const E*>(c->K), Y, plane, c->S, c->F, n_out * plane);
+    }
     if (cudaGetLastError() != cudaSuccess) s = TCFFT_LAUNCH_FAILED;
   }
-  if (s == TCFFT_OK) s = conv_col<E>(c, kConvColInv, 1, Y, Z, batch * c->F, c->P, c->r0, c->oy, 1.0f, st);
-  if (s == TCFFT_OK) s = conv_row_inv<E, RI>(c, Z, out, batch * c->F, 1.0f, st);
+  if (s == TCFFT_OK) s = conv_col<E>(c, kConvColInv, 1, Y, Z, n_out_planes, c->P, c->r0, c->oy, 1.0f, st);
+  if (s == TCFFT_OK) s = conv_row_inv<E, RI>(c, Z, out, n_out, 1.0f, st, pair);
   return s;
 }
 

@@ -46,54 +46,58 @@ __device__ __forceinline__ float real_from<float>(float v) {
   return v;
 }
 
-struct RawF4 {
-  float a, b, c, d;
+// four elements of a line: real parts re[], imaginary parts im[]
+struct RawRI4 {
+  float re[4], im[4];
 };
 
 // Forward row pass: line = (image, row < sy); reads sx reals (zero beyond),
 // writes P complex values (row `row` of the image's half-spectrum buffer,
 // sy rows of P). Optional filter flip (180-degree rotation) for correlation.
+// pair = 1: line = (image pair, row): image 2p is the real part and image
+// 2p + 1 (zero past the last of n_images) the imaginary part, so one complex
+// transform carries two real images.
 template <class R, class E>
 struct IoRealRowIn {
   static constexpr bool IN_VEC_L = true;
   static constexpr bool OUT_VEC_L = true;
-  using Raw = RawF4;
+  using Raw = RawRI4;
   const R* in;
   E* out;
-  long long total_lines;  // images * sy
+  long long total_lines;  // (images or image pairs) * sy
   int sy, sx, P;
   long long in_image_stride;  // elements between images of `in`
   int flip;                   // 1: read w[sy-1-row][sx-1-l] (correlation filters)
+  int pair;
+  long long n_images;
   float scale;
   bool in_contig, out_contig;
   long long contig_len;
 
-  __device__ __forceinline__ Raw fetch_l(long long line, int l0, bool ok) const {
-    Raw r{0.f, 0.f, 0.f, 0.f};
-    if (!ok || line >= total_lines) return r;
-    const long long img = line / sy;
-    const int row0 = static_cast<int>(line % sy);
-    const int row = flip ? sy - 1 - row0 : row0;
+  __device__ __forceinline__ void load4(long long img, int row, int l0, float (&v)[4]) const {
     const R* p = in + img * in_image_stride + static_cast<long long>(row) * sx;
-    float v[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int l = l0 + q;
       const int col = flip ? sx - 1 - l : l;
       v[q] = (l < sx) ? real_load<R>(p + col) : 0.f;
     }
-    r.a = v[0];
-    r.b = v[1];
-    r.c = v[2];
-    r.d = v[3];
+  }
+  __device__ __forceinline__ Raw fetch_l(long long line, int l0, bool ok) const {
+    Raw r{{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+    if (!ok || line >= total_lines) return r;
+    const long long item = line / sy;
+    const int row0 = static_cast<int>(line % sy);
+    const int row = flip ? sy - 1 - row0 : row0;
+    const long long img = pair ? 2 * item : item;
+    load4(img, row, l0, r.re);
+    if (pair && img + 1 < n_images) load4(img + 1, row, l0, r.im);
     return r;
   }
-  __device__ __forceinline__ Raw fetch_g(long long, int, bool) const { return Raw{0.f, 0.f, 0.f, 0.f}; }
+  __device__ __forceinline__ Raw fetch_g(long long, int, bool) const { return Raw{}; }
   __device__ __forceinline__ void decode_l(const Raw& r, long long, int, float2 (&v)[4]) const {
-    v[0] = make_float2(r.a, 0.f);
-    v[1] = make_float2(r.b, 0.f);
-    v[2] = make_float2(r.c, 0.f);
-    v[3] = make_float2(r.d, 0.f);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) v[q] = make_float2(r.re[q], r.im[q]);
   }
   __device__ __forceinline__ void decode_g(const Raw&, long long, int, float2 (&v)[4]) const {}
   __device__ __forceinline__ void store_row16(long long line, int j, int J, float2 (&v)[16]) const {
@@ -179,7 +183,9 @@ struct IoColMaskCrop {
 
 // Inverse row pass: line = (output image, row) over a [rows][P] complex
 // buffer; writes the real part of columns [c0, c0 + nc), times scale, to a
-// real [rows][nc] output per image.
+// real [rows][nc] output per image. pair = 1: line = (output pair, row); the
+// real part goes to output image 2p and the imaginary part to 2p + 1 (when
+// 2p + 1 < n_out).
 template <class E, class RO>
 struct IoRowCropReal {
   static constexpr bool IN_VEC_L = true;
@@ -191,6 +197,8 @@ struct IoRowCropReal {
   RO* out;
   long long total_lines;
   int P, c0, nc;
+  int pair, rows;  // rows per output image (pair = 1)
+  long long n_out;
   float scale;
   bool in_contig, out_contig;
   long long contig_len;
@@ -223,6 +231,21 @@ struct IoRowCropReal {
   }
   __device__ __forceinline__ void decode_g(const Raw&, long long, int, float2 (&)[4]) const {}
   __device__ __forceinline__ void store_row16(long long line, int j, int J, float2 (&v)[16]) const {
+    if (pair) {
+      const long long o0 = 2 * (line / rows);
+      const long long row = line % rows;
+      RO* p0 = out + (o0 * rows + row) * nc;
+      RO* p1 = o0 + 1 < n_out ? out + ((o0 + 1) * rows + row) * nc : nullptr;
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        const int col = j + c * J - c0;
+        if (col >= 0 && col < nc) {
+          p0[col] = real_from<RO>(v[c].x * scale);
+          if (p1) p1[col] = real_from<RO>(v[c].y * scale);
+        }
+      }
+      return;
+    }
     RO* p = out + line * nc;
 #pragma unroll
     for (int c = 0; c < 16; ++c) {

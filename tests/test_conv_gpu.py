@@ -67,6 +67,25 @@ def test_valid_correlation_multichannel(tc, orc, precision):
         assert err < (REL_L2_CONV_FP16 if precision == tc.FP16 else REL_L2_CONV_SPLIT), err
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_paired_transforms_odd_counts(tc, orc, precision):
+    """Three channels and three filters: two real images share each complex
+    transform on both sides (forward: channels, inverse: filter outputs) and
+    the third of each runs alone."""
+    rng = np.random.default_rng(9)
+    S, F, s, f = 3, 3, 80, 5
+    sig = rng.uniform(-1, 1, (1, S, s, s))
+    filt = rng.uniform(-1, 1, (F, S, f, f))
+    out, _ = run_conv(tc, sig, filt, tc.CONV_VALID_CORR, precision, S, F)
+    if precision == tc.FP16:
+        sig = sig.astype(np.float16).astype(np.float64)
+    ref = orc.corr2d_valid(sig[0], filt)
+    assert out.shape == (1, F, s - f + 1, s - f + 1)
+    for k in range(F):
+        err = orc.rel_l2(out[0, k], ref[k])
+        assert err < (REL_L2_CONV_FP16 if precision == tc.FP16 else REL_L2_CONV_SPLIT), (k, err)
+
+
 @pytest.mark.parametrize("precision,side,f", [(0, 256, 31), (1, 200, 15), (0, 64, 3), (1, 128, 7)])
 def test_same_convolution(tc, orc, precision, side, f):
     """'same' mode, filter N(0,1) normalised to unit L1 (config 3's recipe)."""
