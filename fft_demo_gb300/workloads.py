@@ -5,7 +5,9 @@
              buffers, 256 MiB, rotated)
   2d-conv  : FP16 2D FFT 1024 x 1024, batch 16; 'same' convolution of a
              2048 x 2048 FP16 image (uniform[0,1]) with a 31 x 31 filter
-             (N(0,1) entries scaled to unit L1 norm), P = 4096
+             (N(0,1) entries scaled to unit L1 norm), P = 4096; and two
+             multi-image convolutions (8 images of 1024^2, 31 x 31; 16
+             channels of 512^2 against 16 filters of 5 x 5), FP16 and split
   uneven   : 10,000 1D FFTs with n = 2^k, k uniform on [6, 16], plus 512
              'same' convolutions (image side uniform over 64 .. 1024, filter
              side over {3, 7, 15, 31}); split precision (FP32 storage) and
@@ -153,7 +155,32 @@ def two_d_conv(peak_gbs):
     flops = 2 * _f1d(p * p) + 6 * p * p
     out["conv_same_2048_f31"] = {"ms": ms, "conv_per_s": 1e3 / ms, "gflops": flops / ms / 1e6, "padded": p,
                                  "launches": launches, "rel_l2": err}
-    return {"workload": "2d-fft 1024x1024x16 fp16; conv same 2048^2 * 31^2 fp16", **out}
+    # multi-image convolutions, where two real images share each complex
+    # transform: 8 images of 1024^2 'same' with a 31 x 31 filter, and one
+    # 512^2 input of 16 channels against 16 filters of 5 x 5 ('same')
+    for name, (B, S, F, side, fs) in (("conv_same_1024_b8_f31", (8, 1, 1, 1024, 31)),
+                                      ("conv_same_512_s16_f16_k5", (1, 16, 16, 512, 5))):
+        for prec, pname in ((tc.FP16, "fp16"), (tc.SPLIT_FP32, "split")):
+            dt = torch.float16 if prec == tc.FP16 else torch.float32
+            imgs = torch.from_numpy(rng.uniform(0, 1, (B, S, side, side)).astype(np.float32)).to(dt).cuda()
+            wk = rng.standard_normal((F, S, fs, fs))
+            wk /= np.abs(wk).sum(axis=(1, 2, 3), keepdims=True)
+            cv = tc.Conv2d(S, F, side, side, fs, fs, mode=tc.CONV_SAME, precision=prec, max_batch=B)
+            cv.set_filters(torch.from_numpy(wk.astype(np.float32)).cuda())
+            o = cv.exec(imgs)
+            ms = _timed(lambda: cv.exec(imgs, o), 20)
+            cv.check()
+            x0 = imgs[0].double().cpu().numpy()
+            ref = sum(orc.conv2d_same(x0[c], wk[0, c]) for c in range(S))
+            err = orc.rel_l2(o[0, 0].double().cpu().numpy(), ref)
+            pp = cv.padded
+            fl = (B * S + B * F) * _f1d(pp * pp) + 8 * B * S * F * pp * pp
+            out[name + "_" + pname] = {"ms": ms, "images_per_s": B * 1e3 / ms, "gflops": fl / ms / 1e6,
+                                       "padded": pp, "rel_l2_first_output": err,
+                                       "transforms": "%d forward + %d inverse complex 2D FFTs (two real images each)"
+                                                     % ((B * S + 1) // 2, (B * F + 1) // 2)}
+    return {"workload": "2d-fft 1024x1024x16 fp16; conv same 2048^2 * 31^2 fp16; "
+                        "conv same 8 x 1024^2 * 31^2 and 16-channel 512^2 * 16 filters 5^2, fp16 and split", **out}
 
 
 def uneven(peak_gbs, count=10000, nconv=512, seed=4):
