@@ -138,6 +138,33 @@ def whole_job_rate(units_per_rank, world, ms):
     return units_per_rank * world / (ms * 1e-3)
 
 
+def cufft_times(tensors, reps=5):
+    """Comparator: cuFFT through torch.fft (complex32 / complex64 C2C, batched
+    along the first axis, the plan-many route the reference's cufft.cpp
+    uses) on the same device arrays; ms per transform, or a reason string."""
+    import torch
+    out = []
+    for x in tensors:
+        n = x.shape[1]
+        try:
+            xc = x.view(torch.complex32 if x.dtype == torch.float16 else torch.complex64).squeeze(-1)
+            for _ in range(2):
+                y = torch.fft.fft(xc, dim=-1)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                y = torch.fft.fft(xc, dim=-1)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            out.append({"n": n, "batch": x.shape[0], "ms": ms, "gflops": flops(n, x.shape[0]) / ms / 1e6})
+            del y
+        except Exception as exc:  # comparator only: report, never fail the run
+            out.append({"n": n, "unavailable": str(exc).splitlines()[0][:120]})
+    return out
+
+
 def cpu_fft_sample(seconds_target=12.0, threads=0):
     """FP64 oracle FFT on the host over a bounded sample of the workload."""
     import numpy as np
@@ -420,6 +447,9 @@ def main():
         cp.check()
         cp.destroy()
 
+    # --- comparator: cuFFT on the same arrays (FP16 C2C) ---
+    cufft = cufft_times(xs) if rank == 0 else None
+
     # --- roofline of the dominant transform ---
     dom = max(per_kernel, key=lambda k: k["ms"])
     achieved = dom["alg_bytes"] / (dom["ms"] * 1e-3) / 1e9
@@ -453,6 +483,7 @@ def main():
                              dom["n"], dom["launches"], "es" if dom["launches"] > 1 else ""),
                          "peak_kind": peak_kind},
             "per_transform": per_kernel,
+            "comparator_cufft_fp16": cufft,
             "hbm_frac_step": step_bytes / (ms_step * 1e-3) / 1e9 / peak_gbs,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": "GFLOP/s", "h2d_bytes_per_step": h2d,

@@ -92,6 +92,12 @@ def small(peak_gbs):
         res[name] = {"ms_per_step": ms, "gflops": 2 * _f1d(n) * b / ms / 1e6,
                      "gbs": 2 * 2 * n * b * 4 / ms / 1e6}
     res["cold"]["hbm_frac"] = res["cold"]["gbs"] / peak_gbs
+    # comparator: cuFFT (torch.fft on complex32), forward then inverse, warm
+    try:
+        xd = bufs[0].view(torch.complex32).squeeze(-1)
+        res["cufft_warm_ms_per_step"] = _timed(lambda: torch.fft.ifft(torch.fft.fft(xd, dim=-1), dim=-1), 200)
+    except Exception as exc:
+        res["cufft_unavailable"] = str(exc).splitlines()[0][:120]
     # the same 64 cold steps captured once in a CUDA graph and replayed
     graph = torch.cuda.CUDAGraph()
     side = torch.cuda.Stream()
@@ -137,6 +143,12 @@ def two_d_conv(peak_gbs):
     gb = 2 * nx * ny * b * 4 / ms / 1e6
     out["fft2d"] = {"ms": ms, "gflops": _f1d(nx * ny) * b / ms / 1e6, "gbs": gb, "hbm_frac": gb / peak_gbs,
                     "launches": tc.last_launch_count(), "rel_l2": err}
+    # comparator: cuFFT (torch.fft.fft2 on complex32) on the same array
+    try:
+        xd = x.view(torch.complex32).squeeze(-1)
+        out["fft2d"]["cufft_ms"] = _timed(lambda: torch.fft.fft2(xd), 20)
+    except Exception as exc:
+        out["fft2d"]["cufft_unavailable"] = str(exc).splitlines()[0][:120]
     # 'same' conv 2048 x 2048 with a 31 x 31 filter
     s, f = 2048, 31
     rng = np.random.default_rng(3)
@@ -277,6 +289,13 @@ def large_1d_split(peak_gbs, seed=1):
             row[name] = {"ms": ms, "gflops": _f1d(n) * b / ms / 1e6,
                          "gbs": 2 * n * b * eb / ms / 1e6, "hbm_frac": 2 * n * b * eb / ms / 1e6 / peak_gbs,
                          "launches": tc.last_launch_count()}
+            # comparator: cuFFT (torch.fft, complex64 / complex32 C2C) on the same array
+            try:
+                xd = x.view(torch.complex64 if name == "split" else torch.complex32).squeeze(-1)
+                cms = _timed(lambda: torch.fft.fft(xd, dim=-1), 5)
+                row[name]["cufft_ms"] = cms
+            except Exception as exc:
+                row[name]["cufft_unavailable"] = str(exc).splitlines()[0][:120]
             if name == "split":
                 xs = x[:2].double().cpu().numpy()
                 ys = y[:2].double().cpu().numpy()
