@@ -460,8 +460,14 @@ __device__ __forceinline__ bool run_stages(PassState& st, const IO& io, const Pa
         }
         umma_commit(st.mbar);
       }
-      bool to = !mbar_wait_bounded(st.mbar, st.phase & 1u);
-      if (to && lane == 0) atomicOr(core.err, kErrMmaTimeout);
+      // one thread polls the MMA barrier; the others block at the CTA
+      // barrier (no issue slots spent spinning), which carries the
+      // completion to them
+      bool to = false;
+      if (tid == 0) {
+        to = !mbar_wait_bounded(st.mbar, st.phase & 1u);
+        if (to) atomicOr(core.err, kErrMmaTimeout);
+      }
       st.phase++;
       if (__syncthreads_or(to)) {
         timed_out = true;
@@ -524,10 +530,11 @@ __device__ __forceinline__ bool pass_tile(PassState& st, const IO& io, const Pas
         const uint32_t bytes = static_cast<uint32_t>(nval) * L * 4u;
         mbar_arrive_expect_tx(st.tma_bar, bytes);
         bulk_g2s(re, io.tile_src(line0), bytes, st.tma_bar);
-      }
-      if (!mbar_wait_bounded(st.tma_bar, st.tma_phase & 1u)) {
-        timed_out = true;
-        if (lane == 0) atomicOr(core.err, kErrMmaTimeout);
+        // the issuing thread polls; the others wait at the CTA barrier
+        if (!mbar_wait_bounded(st.tma_bar, st.tma_phase & 1u)) {
+          timed_out = true;
+          atomicOr(core.err, kErrMmaTimeout);
+        }
       }
       st.tma_phase++;
       if (__syncthreads_or(timed_out)) return false;
@@ -806,9 +813,13 @@ __device__ __forceinline__ bool tensor_out(const IO& io) {
 template <class IO>
 __device__ __forceinline__ bool wait_prefetch(PassState& st, const IO& io, const PassCore& core) {
   if ((IO::IN_VEC_L && io.in_contig) || tensor_in(io)) {
-    const bool ok = mbar_wait_bounded(st.tma_bar, st.tma_phase & 1u);
+    // one thread polls the copy barrier, the others wait at the CTA barrier
+    bool ok = true;
+    if (threadIdx.x == 0) {
+      ok = mbar_wait_bounded(st.tma_bar, st.tma_phase & 1u);
+      if (!ok) atomicOr(core.err, kErrMmaTimeout);
+    }
     st.tma_phase++;
-    if (!ok && (threadIdx.x & 31) == 0) atomicOr(core.err, kErrMmaTimeout);
     return !__syncthreads_or(!ok);
   }
   cp_async_wait_all();
