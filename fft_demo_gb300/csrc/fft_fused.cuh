@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(kPassThreads, 2)
     __syncthreads();
     const unsigned int item = s_item;
     if (item >= total) break;
-    // decode: round 0 = P1(0); round r (1..nchunks-1) = P1(r) then P2(r-1); last = P2(nchunks-1)
+    // decode: step 0 = P1(0); step r (1..nchunks-1) = P1(r) then P2(r-1); last = P2(nchunks-1)
     int pass, chunk, t;
     if (item < static_cast<unsigned int>(sc.tiles1)) {
       pass = 1;
