@@ -429,22 +429,77 @@ void fft_conv2d_half::double2half(double* src, half* dst, int x, int y, int item
 }
 
 namespace {
+// Host FP64 in and out (the reference's fft_2d_c2c / ifft_2d_c2c contract,
+// .cpp:79,147): the batch goes in up to 8 sub-batches (the reference's 8
+// streams) over up to 4 streams, each with its own device buffers and plans,
+// so one sub-batch's copies overlap another's conversion and transform. The
+// caller's host buffers are page-locked for the call (cudaHostRegister)
+// unless they already are, so the asynchronous copies run concurrently; if
+// that fails the copies still run, without the overlap.
 void fft_2d_host(fft_conv2d_half* o, double* input, double* output, int x, int y, int batch, int direction) {
-  tcfftPlan p = nullptr;
-  o->last_status = tcfft_plan_2d(&p, y, x, batch, TCFFT_FP16);
-  if (o->last_status != TCFFT_OK) return;
-  const long long n = 2ll * x * y * batch;
-  double* dd = dev_alloc<double>(static_cast<size_t>(n));
-  __half* dh = dev_alloc<__half>(static_cast<size_t>(n));
-  cudaMemcpy(dd, input, sizeof(double) * n, cudaMemcpyHostToDevice);
-  double_to_half_kernel<<<grid_for(n), 256>>>(dd, dh, n);
-  o->last_status = tcfft_exec(p, dh, dh, direction, 1.0f, nullptr);
-  if (o->last_status == TCFFT_OK) o->last_status = tcfft_check(p, nullptr);
-  half_to_double_kernel<<<grid_for(n), 256>>>(dh, dd, n);
-  cudaMemcpy(output, dd, sizeof(double) * n, cudaMemcpyDeviceToHost);
-  cudaFree(dd);
-  cudaFree(dh);
-  tcfft_destroy(p);
+  o->last_status = TCFFT_OK;
+  if (batch <= 0) return;
+  const int nchunks_max = batch < 8 ? batch : 8;
+  const int per = (batch + nchunks_max - 1) / nchunks_max;
+  const int nchunks = (batch + per - 1) / per;
+  const int nst = nchunks < 4 ? nchunks : 4;
+  const long long elems = 2ll * x * y;  // doubles per transform
+  const size_t bytes = sizeof(double) * static_cast<size_t>(elems) * batch;
+  auto pin = [](void* p, size_t n) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type == cudaMemoryTypeHost) return false;
+    cudaGetLastError();  // an unregistered pointer is not an error here
+    if (cudaHostRegister(p, n, cudaHostRegisterDefault) == cudaSuccess) return true;
+    cudaGetLastError();
+    return false;
+  };
+  const bool pinned_in = pin(input, bytes);
+  const bool pinned_out = output != input && pin(output, bytes);
+  cudaStream_t st[4] = {};
+  double* dd[4] = {};
+  __half* dh[4] = {};
+  tcfftPlan plan_full[4] = {}, plan_tail[4] = {};
+  const int tail = batch - (nchunks - 1) * per;  // sub-batch size of the last chunk
+  tcfftStatus status = TCFFT_OK;
+  for (int k = 0; k < nst && status == TCFFT_OK; ++k) {
+    if (cudaStreamCreateWithFlags(&st[k], cudaStreamNonBlocking) != cudaSuccess) status = TCFFT_LAUNCH_FAILED;
+    dd[k] = dev_alloc<double>(static_cast<size_t>(elems) * per);
+    dh[k] = dev_alloc<__half>(static_cast<size_t>(elems) * per);
+    if (!dd[k] || !dh[k]) status = TCFFT_ALLOC_FAILED;
+    if (status == TCFFT_OK) status = tcfft_plan_2d(&plan_full[k], y, x, per, TCFFT_FP16);
+  }
+  for (int c = 0; c < nchunks && status == TCFFT_OK; ++c) {
+    const int k = c % nst;
+    const int nb = c == nchunks - 1 ? tail : per;
+    tcfftPlan p = plan_full[k];
+    if (nb != per) {
+      if (!plan_tail[k]) status = tcfft_plan_2d(&plan_tail[k], y, x, nb, TCFFT_FP16);
+      p = plan_tail[k];
+    }
+    if (status != TCFFT_OK) break;
+    const long long n = elems * nb;
+    const long long off = elems * static_cast<long long>(c) * per;
+    cudaMemcpyAsync(dd[k], input + off, sizeof(double) * n, cudaMemcpyHostToDevice, st[k]);
+    double_to_half_kernel<<<grid_for(n), 256, 0, st[k]>>>(dd[k], dh[k], n);
+    status = tcfft_exec(p, dh[k], dh[k], direction, 1.0f, st[k]);
+    half_to_double_kernel<<<grid_for(n), 256, 0, st[k]>>>(dh[k], dd[k], n);
+    cudaMemcpyAsync(output + off, dd[k], sizeof(double) * n, cudaMemcpyDeviceToHost, st[k]);
+  }
+  for (int k = 0; k < nst; ++k) {
+    if (st[k] && cudaStreamSynchronize(st[k]) != cudaSuccess && status == TCFFT_OK) status = TCFFT_LAUNCH_FAILED;
+    if (plan_full[k] && status == TCFFT_OK) status = tcfft_check(plan_full[k], st[k]);
+    if (plan_tail[k] && status == TCFFT_OK) status = tcfft_check(plan_tail[k], st[k]);
+  }
+  for (int k = 0; k < nst; ++k) {
+    if (plan_full[k]) tcfft_destroy(plan_full[k]);
+    if (plan_tail[k]) tcfft_destroy(plan_tail[k]);
+    cudaFree(dd[k]);
+    cudaFree(dh[k]);
+    if (st[k]) cudaStreamDestroy(st[k]);
+  }
+  if (pinned_in) cudaHostUnregister(input);
+  if (pinned_out) cudaHostUnregister(output);
+  o->last_status = status;
 }
 }  // namespace
 

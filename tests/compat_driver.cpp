@@ -87,11 +87,16 @@ int main(int argc, char** argv) {
     dump(out + "/conv_dx.bin", conv.delta_for_signal, sizeof(double) * s * s * C);
     free(conv.delta_for_filter);
     free(conv.delta_for_signal);
-    std::vector<double> cin(2 * 256 * 256 * 2), cout_(2 * 256 * 256 * 2);
+    // batch 5: five sub-batches over four streams (one stream reused)
+    std::vector<double> cin(5 * 256 * 256 * 2), cout_(5 * 256 * 256 * 2), cback(5 * 256 * 256 * 2);
     for (auto& v : cin) v = next_val();
-    conv.fft_2d_c2c(cin.data(), cout_.data(), 256, 256, 2, __AMPERE__);
+    conv.fft_2d_c2c(cin.data(), cout_.data(), 256, 256, 5, __AMPERE__);
+    std::vector<double> cmid(cout_);  // scaled so the unnormalised inverse stays in FP16 range
+    for (auto& v : cmid) v /= 256.0 * 256.0;
+    conv.ifft_2d_c2c(cmid.data(), cback.data(), 256, 256, 5, __AMPERE__);
     dump(out + "/c2c_in.bin", cin.data(), cin.size() * 8);
     dump(out + "/c2c_out.bin", cout_.data(), cout_.size() * 8);
+    dump(out + "/c2c_back.bin", cback.data(), cback.size() * 8);
   }
   // ---- cuFFT-family full convolution (main.cpp:307-314) ----
   {

@@ -83,9 +83,14 @@ def test_conv_class_backward(driver_out, orc):
 
 
 def test_conv_class_fft_2d_c2c(driver_out, orc):
-    x = cplx(h(load(driver_out, "c2c_in.bin"))).reshape(2, 256, 256)
-    y = cplx(load(driver_out, "c2c_out.bin")).reshape(2, 256, 256)
-    assert orc.rel_l2(y, orc.fft2d(x)) < REL_FP16
+    """Batch 5 in sub-batches over several streams, then the inverse
+    (unnormalised) of the spectrum / (256 * 256) back to x."""
+    x = cplx(h(load(driver_out, "c2c_in.bin"))).reshape(5, 256, 256)
+    y = cplx(load(driver_out, "c2c_out.bin")).reshape(5, 256, 256)
+    for b in range(5):
+        assert orc.rel_l2(y[b], orc.fft2d(x[b])) < REL_FP16, b
+    back = cplx(load(driver_out, "c2c_back.bin")).reshape(5, 256, 256)
+    assert orc.rel_l2(back, x) < 4 * REL_FP16
 
 
 def test_fftconvolve2d_family(driver_out, orc):
