@@ -80,6 +80,24 @@ def test_fft1d_in_place_equals_out_of_place(tc, orc):
     assert np.array_equal(from_dev_f16(a), from_dev_f16(b))
 
 
+def test_fft1d_largest_size(tc, orc):
+    """The largest 1D size, 2^24 (four-step 2^12 x 2^12), one sequence."""
+    err, *_ = _fft_case(tc, orc, 1 << 24, 1, seed=24)
+    assert err < REL_L2_FP16, err
+
+
+def test_fft2d_largest_size(tc, orc):
+    """The largest 2D size, 4096 x 4096, one image."""
+    rng = np.random.default_rng(4096)
+    x = f16_round(uniform_complex(rng, (1, 4096, 4096)))
+    plan = tc.plan_2d(4096, 4096, 1)
+    d = to_dev_f16(x)
+    plan.exec(d)
+    plan.check()
+    err = orc.rel_l2(from_dev_f16(d), orc.fft2d(x))
+    assert err < REL_L2_FP16, err
+
+
 @pytest.mark.parametrize("nx,ny", [(16, 16), (64, 256), (256, 256), (256, 512), (512, 1024),
                                    (1024, 1024)])
 def test_fft2d(tc, orc, nx, ny):

@@ -33,7 +33,7 @@ def test_split_single_pass(tc, orc, n):
     assert err < REL_L2_SPLIT, err
 
 
-@pytest.mark.parametrize("n", [1 << 14, 1 << 16, 1 << 20])
+@pytest.mark.parametrize("n", [1 << 14, 1 << 16, 1 << 20, 1 << 22])
 def test_split_four_step(tc, orc, n):
     err = _case(tc, orc, n, 2, seed=7)
     assert err < REL_L2_SPLIT, err
