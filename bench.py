@@ -176,7 +176,8 @@ def cpu_fft_sample(seconds_target=12.0, threads=0):
     per = seconds_target / len(SIZES)
     detail = []
     for n, batch in SIZES:
-        b = max(1, min(batch, (1 << 22) // n))  # 4 Mi points per trial
+        # 4 Mi points per trial, and at least one sequence per thread
+        b = max(1, min(batch, max(nt, (1 << 22) // n)))
         x = (rng.uniform(-1, 1, (b, n)) + 1j * rng.uniform(-1, 1, (b, n)))
         buf = orc.to_interleaved(x)
         lib = orc.lib()
@@ -204,8 +205,12 @@ def run_reference(args, world, rank):
     lib = orc.lib()
     rng = np.random.default_rng(1)
     bufs = []
+    # equal points per size, as in the GPU workload, and at least one
+    # sequence per host thread for every size (the oracle parallelises over
+    # the batch), so all threads work on every transform
+    points = max(1 << 21, nt * max(n for n, _ in SIZES))
     for n, batch in SIZES:
-        b = max(1, min(batch, (1 << 21) // n))  # 2 Mi points per size per step
+        b = max(1, min(batch, points // n))
         x = rng.uniform(-1, 1, (b, n)) + 1j * rng.uniform(-1, 1, (b, n))
         bufs.append((n, b, orc.to_interleaved(x)))
 
