@@ -231,13 +231,16 @@ void free_plan(tcfftPlanImpl* p) {
 // (stride seq_stride); 4-byte elements, boxes of G lines x min(L, 256)
 // elements. False when the layout breaks a TMA rule (the caller keeps the
 // cp.async path then).
+// esize: bytes per element (4: FP16 complex, 8: FP32 complex).
 bool encode_column_map(CUtensorMap* map, const void* base, long long lines_per_seq, long long nseq, int L,
-                       long long elem_stride, long long seq_stride, int G) {
-  if ((reinterpret_cast<uintptr_t>(base) & 15u) || (elem_stride * 4) % 16 || (seq_stride * 4) % 16 || (G * 4) % 16)
+                       long long elem_stride, long long seq_stride, int G, int esize) {
+  if ((reinterpret_cast<uintptr_t>(base) & 15u) || (elem_stride * esize) % 16 || (seq_stride * esize) % 16 ||
+      (G * esize) % 16)
     return false;
   const cuuint64_t dims[3] = {static_cast<cuuint64_t>(lines_per_seq), static_cast<cuuint64_t>(L),
                               static_cast<cuuint64_t>(nseq)};
-  const cuuint64_t strides[2] = {static_cast<cuuint64_t>(elem_stride * 4), static_cast<cuuint64_t>(seq_stride * 4)};
+  const cuuint64_t strides[2] = {static_cast<cuuint64_t>(elem_stride * esize),
+                                 static_cast<cuuint64_t>(seq_stride * esize)};
   const cuuint32_t box[3] = {static_cast<cuuint32_t>(G), static_cast<cuuint32_t>(L < 256 ? L : 256), 1u};
   const cuuint32_t estr[3] = {1u, 1u, 1u};
   // the driver's encoder, found through the runtime (the library does not
@@ -252,26 +255,33 @@ bool encode_column_map(CUtensorMap* map, const void* base, long long lines_per_s
     return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
   }();
   if (!encode) return false;
-  return encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, const_cast<void*>(base), dims, strides, box, estr,
+  // element type only sets the size: tile copies move bytes unchanged
+  const CUtensorMapDataType dtype = esize == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_UINT32;
+  return encode(map, dtype, 3, const_cast<void*>(base), dims, strides, box, estr,
                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// Prefetching (mid-tile) kernels move column-layout tiles by TMA when every
-// tile lies inside one sequence.
+// Column-layout tiles move by TMA when every tile lies inside one sequence:
+// FP16 prefetching (mid-tile) kernels load and store them that way; the
+// split-precision kernels store narrow tiles (G <= 8 lines, whose direct
+// 8-byte stores touch only G * 8 contiguous bytes per element) that way,
+// since staging waits for every MMA group and wider tiles store well directly.
 template <class IO>
 void attach_tensor_maps(IO& io, int kind, int tile, int logL, int G) {
   if constexpr (TensorMapIo<IO>) {
+    constexpr int esize = static_cast<int>(sizeof(*io.out));
+    constexpr bool split = esize == 8;
     io.in_tma = io.out_tma = false;
-    if (tile != kTileMid || kind == kPassRow) return;
+    if (kind == kPassRow || (!split && tile != kTileMid) || (split && G > 8)) return;
     const long long lps = 1ll << io.lps_log2;
     if (lps % G != 0 || io.total_lines % lps != 0 || G % 4 != 0) return;
     const long long nseq = io.total_lines / lps;
     const int L = 1 << logL;
-    if (!IO::IN_VEC_L && io.in_line == 1)
-      io.in_tma = encode_column_map(&io.in_map, io.in, lps, nseq, L, io.in_elem, io.in_seq, G);
+    if (!split && !IO::IN_VEC_L && io.in_line == 1)
+      io.in_tma = encode_column_map(&io.in_map, io.in, lps, nseq, L, io.in_elem, io.in_seq, G, esize);
     if (!IO::OUT_VEC_L && io.out_line == 1)
-      io.out_tma = encode_column_map(&io.out_map, io.out, lps, nseq, L, io.out_elem, io.out_seq, G);
+      io.out_tma = encode_column_map(&io.out_map, io.out, lps, nseq, L, io.out_elem, io.out_seq, G, esize);
   }
 }
 

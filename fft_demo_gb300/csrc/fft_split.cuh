@@ -112,7 +112,10 @@ __device__ __forceinline__ bool split_stage_epilogue(const SplitPlanes& P, const
   constexpr int Ns = Sh::T << (4 * s);
   constexpr bool LAST = (s == Sh::S - 1);
   bool ok = true;
-  bool planes_free = LAST;
+  // the last stage writes shared memory only when it stages a tensor store
+  bool stage_tensor = false;
+  if constexpr (TensorMapIo<IO> && LINE_MINOR) stage_tensor = LAST && io.out_tma;
+  bool planes_free = LAST && !stage_tensor;
 #pragma unroll 1
   for (int grp = warp >> 2; grp < NG; grp += kPassThreads / 128) {
     const int m = grp * 128 + 32 * (warp & 3) + lane;
@@ -173,7 +176,27 @@ __device__ __forceinline__ bool split_stage_epilogue(const SplitPlanes& P, const
           v[c].x *= out_scale;
           v[c].y *= out_scale;
         }
-        io.store_row16(line, j, J, v);
+        bool staged = false;
+        if constexpr (TensorMapIo<IO> && LINE_MINOR) {
+          if (stage_tensor) {
+            // column-layout copy of the tile (element (g, l) at l * G + g) in
+            // the plane region, for the tensor store issued after the stage;
+            // the planes are rewritten in place, so every group's MMAs first
+            if (!planes_free) {
+              if (!mbar_wait_bounded(mbar + (NG - 1), parity)) {
+                ok = false;
+                continue;
+              }
+              planes_free = true;
+            }
+            io.prepare_row16(line, j, J, v);
+            float2* col = reinterpret_cast<float2*>(P.rh) + g;
+#pragma unroll
+            for (int c = 0; c < 16; ++c) col[(j + c * J) * G] = v[c];
+            staged = true;
+          }
+        }
+        if (!staged) io.store_row16(line, j, J, v);
       }
     } else {
       if (!planes_free) {
@@ -301,6 +324,7 @@ __device__ __forceinline__ void split_setup(SplitState& st, const uint32_t* __re
 
 template <uint32_t TMEM_COLS>
 __device__ __forceinline__ void split_teardown(SplitState& st) {
+  if (threadIdx.x == 0) bulk_wait_all();  // tensor stores complete before the CTA ends
   tc_fence_before_sync();
   __syncthreads();
   if ((threadIdx.x >> 5) == 0) tmem_dealloc(st.tbase, TMEM_COLS);
@@ -347,6 +371,9 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
   if constexpr (L2PrefetchIo<IO>) {
     if (next_line0 >= 0) io.prefetch_tile_l2(next_line0, G, L);
   }
+  // a tensor store of the previous tile reads the plane region: it must be
+  // done reading before this tile's planes are written (no-op otherwise)
+  if (tid == 0) bulk_wait_read_all();
     if (tid == 0) *st.smax = 0;
     __syncthreads();
 
@@ -566,7 +593,8 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
 // Split-precision pass kernel: persistent CTAs over the tiles of one pass.
 // ---------------------------------------------------------------------------
 template <int L, int G, bool LINE_MINOR, int SIGN, class IO>
-__global__ void __launch_bounds__(kPassThreads, 2) fft_pass_split(const IO io, const PassCore core) {
+__global__ void __launch_bounds__(kPassThreads, 2) fft_pass_split(const __grid_constant__ IO io,
+                                                                  const PassCore core) {
   constexpr uint32_t TMEM_COLS = split_tmem_cols<L, G>();
   static_assert(TMEM_COLS >= 32 && (TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM columns");
   SplitState st;
@@ -575,6 +603,21 @@ __global__ void __launch_bounds__(kPassThreads, 2) fft_pass_split(const IO io, c
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const long long next = tile + gridDim.x < ntiles ? (tile + gridDim.x) * G : -1;
     if (!split_tile<L, G, LINE_MINOR, SIGN, IO>(st, io, core, tile * G, next)) break;
+    if constexpr (TensorMapIo<IO> && LINE_MINOR) {
+      if (io.out_tma && threadIdx.x == 0) {
+        // the staged [L][G] tile as L / 256 tensor stores (the host sets the
+        // map only when tiles never straddle a sequence)
+        constexpr int BY = L < 256 ? L : 256;
+        const long long line0 = tile * G;
+        const int seq = static_cast<int>(line0 >> io.lps_log2);
+        const int x0 = static_cast<int>(line0 & ((1ll << io.lps_log2) - 1));
+        const uint8_t* stage = st.smem + kSplitPlaneOffset;
+#pragma unroll
+        for (int r0 = 0; r0 < L; r0 += BY)
+          tma_store_3d(&io.out_map, stage + static_cast<uint32_t>(r0) * G * 8u, x0, r0, seq);
+        bulk_commit();
+      }
+    }
   }
   split_teardown<TMEM_COLS>(st);
 }
@@ -605,6 +648,12 @@ struct IoFloat {
   float scale;
   bool in_contig, out_contig;  // not used by the split kernel (direct loads / stores)
   long long contig_len;
+  // Column-layout output (lines adjacent in memory, out_line == 1) stored by
+  // TMA through a 3D tensor map (x = line within its sequence, y = element,
+  // z = sequence; 8-byte elements), set by the host; the kernel parameter is
+  // __grid_constant__. in_tma is not used by the split kernel.
+  bool in_tma, out_tma;
+  CUtensorMap in_map, out_map;
 
   __device__ __forceinline__ long long in_base(long long line) const {
     return (line >> lps_log2) * in_seq + (line & ((1ll << lps_log2) - 1)) * in_line;
@@ -660,6 +709,25 @@ struct IoFloat {
   }
   __device__ __forceinline__ void decode_l(const Raw& r, long long, int, float2 (&v)[4]) const { unpack(r, v); }
   __device__ __forceinline__ void decode_g(const Raw& r, long long, int, float2 (&v)[4]) const { unpack(r, v); }
+  // Outer twiddle and scale applied in place to outputs l = j + c*J of one
+  // line (same values as store_row16 writes), for the staged tensor store.
+  __device__ __forceinline__ void prepare_row16(long long line, int j, int J, float2 (&v)[16]) const {
+    if (otw.hi) {
+      const long long li = line & ((1ll << lps_log2) - 1);
+      float2 wq[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) wq[q] = otw(li, j + 4 * q * J);
+      const float2 step = otw(li, J);
+      float2 w = wq[0];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        w = (c & 3) == 0 ? wq[c >> 2] : cmulf(w, step);
+        v[c] = cmulf(v[c], w);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 16; ++c) v[c] = make_float2(v[c].x * scale, v[c].y * scale);
+  }
   // Outputs l = j + c*J (c = 0..15) of one line. The outer twiddle
   // W_N^{li*l} is exact (two-level table) at c = 0, 4, 8, 12; in between it
   // follows from the exact step W_N^{li*J} (at most three FP32 products from
