@@ -273,14 +273,14 @@ void attach_tensor_maps(IO& io, int kind, int tile, int logL, int G) {
     constexpr int esize = static_cast<int>(sizeof(*io.out));
     constexpr bool split = esize == 8;
     io.in_tma = io.out_tma = false;
-    if (kind == kPassRow || (!split && tile != kTileMid) || (split && G > 8)) return;
+    if (kind == kPassRow || (!split && tile != kTileMid)) return;
     const long long lps = 1ll << io.lps_log2;
     if (lps % G != 0 || io.total_lines % lps != 0 || G % 4 != 0) return;
     const long long nseq = io.total_lines / lps;
     const int L = 1 << logL;
-    if (!split && !IO::IN_VEC_L && io.in_line == 1)
+    if (!IO::IN_VEC_L && io.in_line == 1)  // split: used for L2 prefetches of the next tile
       io.in_tma = encode_column_map(&io.in_map, io.in, lps, nseq, L, io.in_elem, io.in_seq, G, esize);
-    if (!IO::OUT_VEC_L && io.out_line == 1)
+    if (!IO::OUT_VEC_L && io.out_line == 1 && (!split || G <= 8))
       io.out_tma = encode_column_map(&io.out_map, io.out, lps, nseq, L, io.out_elem, io.out_seq, G, esize);
   }
 }

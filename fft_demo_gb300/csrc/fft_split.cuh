@@ -651,7 +651,8 @@ struct IoFloat {
   // Column-layout output (lines adjacent in memory, out_line == 1) stored by
   // TMA through a 3D tensor map (x = line within its sequence, y = element,
   // z = sequence; 8-byte elements), set by the host; the kernel parameter is
-  // __grid_constant__. in_tma is not used by the split kernel.
+  // __grid_constant__. The split kernel uses the input map only for L2
+  // prefetches of the next tile.
   bool in_tma, out_tma;
   CUtensorMap in_map, out_map;
 
@@ -675,6 +676,17 @@ struct IoFloat {
       }
     } else {
       if (in_line != 1) return;
+      if (in_tma) {
+        // the host set an input map (tiles never straddle a sequence): the
+        // tile as L / 256 box prefetches
+        if (tid == 0) {
+          const int by = l < 256 ? l : 256;
+          const int seq = static_cast<int>(line0 >> lps_log2);
+          const int x0 = static_cast<int>(line0 & ((1ll << lps_log2) - 1));
+          for (int r0 = 0; r0 < l; r0 += by) tma_prefetch_3d(&in_map, x0, r0, seq);
+        }
+        return;
+      }
       const long long rem = total_lines - line0;
       const int lines = rem < g ? static_cast<int>(rem) : g;
       if (lines <= 0 || (lines & 1)) return;  // ranges of whole 16-byte units

@@ -245,6 +245,13 @@ __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc, uin
                "r"(src_bytes)
                : "memory");
 }
+// L2 prefetch of one 3D tensor-map box (a hint: no data moves to the SM).
+__device__ __forceinline__ void tma_prefetch_3d(const void* map, int c0, int c1, int c2) {
+  asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(map), "r"(c0), "r"(c1),
+               "r"(c2)
+               : "memory");
+}
+
 // Bulk prefetch of [gsrc, gsrc + bytes) into L2 (a hint: no data moves to
 // the SM). gsrc 16-byte aligned, bytes a multiple of 16.
 __device__ __forceinline__ void prefetch_l2_bulk(const void* gsrc, uint32_t bytes) {
