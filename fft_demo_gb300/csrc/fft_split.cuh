@@ -290,10 +290,12 @@ struct SplitState {
   uint8_t* bhi;
   uint8_t* blo;
   uint64_t* mbar;  // kSplitMaxGroups mbarriers: MMA completion per 128-row group
+  uint64_t* tma_bar;  // tensor-map tile loads
   uint32_t* tslot;
   int* smax;
   uint32_t tbase;
   uint32_t phase;
+  uint32_t tma_phase;
 };
 
 constexpr int kSplitMaxGroups = 4;  // Mt <= 512
@@ -306,10 +308,13 @@ __device__ __forceinline__ void split_setup(SplitState& st, const uint32_t* __re
   st.mbar = reinterpret_cast<uint64_t*>(st.smem + 4096);
   st.tslot = reinterpret_cast<uint32_t*>(st.smem + 4096 + 8 * kSplitMaxGroups);
   st.smax = reinterpret_cast<int*>(st.smem + 4096 + 8 * kSplitMaxGroups + 8);
+  st.tma_bar = reinterpret_cast<uint64_t*>(st.smem + 4096 + 8 * kSplitMaxGroups + 16);
   const int tid = threadIdx.x;
   for (int i = tid; i < 1024; i += kPassThreads) reinterpret_cast<uint32_t*>(st.bhi)[i] = __ldg(bmat_g + i);
-  if (tid == 0)
+  if (tid == 0) {
     for (int k = 0; k < kSplitMaxGroups; ++k) mbar_init(st.mbar + k, 1);
+    mbar_init(st.tma_bar, 1);
+  }
   if ((tid >> 5) == 0) {
     tmem_alloc(st.tslot, TMEM_COLS);
     tmem_relinquish();
@@ -320,6 +325,7 @@ __device__ __forceinline__ void split_setup(SplitState& st, const uint32_t* __re
   tc_fence_after_sync();
   st.tbase = *st.tslot;
   st.phase = 0;
+  st.tma_phase = 0;
 }
 
 template <uint32_t TMEM_COLS>
@@ -344,7 +350,9 @@ concept L2PrefetchIo = requires(const IO& io) { io.prefetch_tile_l2(0ll, 0, 0); 
 
 // next_line0 >= 0: the tile this CTA processes next, whose input is
 // prefetched into L2 while this one runs.
-template <int L, int G, bool LINE_MINOR, int SIGN, class IO>
+// TMA_IN: the tile arrives by tensor loads (column tiles whose IO carries an
+// input map); a template parameter so each load path is compiled on its own.
+template <int L, int G, bool LINE_MINOR, int SIGN, class IO, bool TMA_IN = false>
 __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const PassCore& core, long long line0,
                                            long long next_line0 = -1) {
   using Sh = LineShape<L>;
@@ -374,6 +382,22 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
   // a tensor store of the previous tile reads the plane region: it must be
   // done reading before this tile's planes are written (no-op otherwise)
   if (tid == 0) bulk_wait_read_all();
+  // column tiles with an input map arrive by tensor loads into the plane
+  // region ([L][G] elements), read back by the threads below
+  constexpr bool tma_in = TMA_IN;
+  if constexpr (TMA_IN) {
+    static_assert(TensorMapIo<IO> && !IO::IN_VEC_L, "tensor loads: column tiles with a map");
+    if (tid == 0) {
+      constexpr int BY = L < 256 ? L : 256;
+      mbar_arrive_expect_tx(st.tma_bar, static_cast<uint32_t>(G) * L * 8u);
+      const int seq = static_cast<int>(line0 >> io.lps_log2);
+      const int x0 = static_cast<int>(line0 & ((1ll << io.lps_log2) - 1));
+#pragma unroll
+      for (int r0 = 0; r0 < L; r0 += BY)
+        tma_load_3d(st.smem + kSplitPlaneOffset + static_cast<uint32_t>(r0) * G * 8u, &io.in_map, x0, r0, seq,
+                    st.tma_bar);
+    }
+  }
     if (tid == 0) *st.smax = 0;
     __syncthreads();
 
@@ -487,11 +511,46 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
       constexpr int ITEMS = GQ * (L / T);
       static_assert(ITEMS <= kPassThreads * U, "one load batch per tile");
       typename IO::Raw raw[U][T];
+      bool loaded = false;
+      if constexpr (TMA_IN) {
+        {
+          // one thread polls the copy barrier, the others wait at the CTA barrier
+          bool to = false;
+          if (tid == 0) {
+            to = !mbar_wait_bounded(st.tma_bar, st.tma_phase & 1u);
+            if (to) {
+              atomicOr(core.err, kErrMmaTimeout);
+              mbar_wait_bounded(st.tma_bar, st.tma_phase & 1u);  // let a late copy land before giving up
+            }
+          }
+          st.tma_phase++;
+          if (__syncthreads_or(to)) return false;
+          const uint8_t* src = st.smem + kSplitPlaneOffset;
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int it = tid + u * kPassThreads;
+          for (int u = 0; u < U; ++u) {
+            const int it = tid + u * kPassThreads;
 #pragma unroll
-        for (int r = 0; r < T; ++r) raw[u][r] = io.fetch_g(line0 + (it % GQ) * 4, it / GQ + r * (L / T), it < ITEMS);
+            for (int r = 0; r < T; ++r) {
+              raw[u][r] = typename IO::Raw{make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
+              if (ITEMS % (kPassThreads * U) == 0 || it < ITEMS) {
+                const uint8_t* p =
+                    src + ((static_cast<uint32_t>(it / GQ + r * (L / T)) * G + (it % GQ) * 4u) << 3);
+                raw[u][r].a = *reinterpret_cast<const uint4*>(p);
+                raw[u][r].b = *reinterpret_cast<const uint4*>(p + 16);
+              }
+            }
+          }
+          loaded = true;
+        }
+      }
+      if (!loaded) {
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int it = tid + u * kPassThreads;
+#pragma unroll
+          for (int r = 0; r < T; ++r)
+            raw[u][r] = io.fetch_g(line0 + (it % GQ) * 4, it / GQ + r * (L / T), it < ITEMS);
+        }
       }
       float2 v[U][T][4];
       float lmax = 0.f;
@@ -600,9 +659,20 @@ __global__ void __launch_bounds__(kPassThreads, 2) fft_pass_split(const __grid_c
   SplitState st;
   split_setup<TMEM_COLS>(st, core.bmat);
   const long long ntiles = (io.total_lines + G - 1) / G;
+  // column tiles with an input map take the tensor-load path (one loop per
+  // path, so each is compiled on its own)
+  bool tma_in = false;
+  if constexpr (TensorMapIo<IO> && !IO::IN_VEC_L) tma_in = io.in_tma;
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const long long next = tile + gridDim.x < ntiles ? (tile + gridDim.x) * G : -1;
-    if (!split_tile<L, G, LINE_MINOR, SIGN, IO>(st, io, core, tile * G, next)) break;
+    bool ok;
+    if constexpr (TensorMapIo<IO> && !IO::IN_VEC_L) {
+      ok = tma_in ? split_tile<L, G, LINE_MINOR, SIGN, IO, true>(st, io, core, tile * G, next)
+                  : split_tile<L, G, LINE_MINOR, SIGN, IO, false>(st, io, core, tile * G, next);
+    } else {
+      ok = split_tile<L, G, LINE_MINOR, SIGN, IO>(st, io, core, tile * G, next);
+    }
+    if (!ok) break;
     if constexpr (TensorMapIo<IO> && LINE_MINOR) {
       if (io.out_tma && threadIdx.x == 0) {
         // the staged [L][G] tile as L / 256 tensor stores (the host sets the
