@@ -211,11 +211,15 @@ def main():
     rows = [8, 10, 12] if args.quick else list(range(6, 15))
     fours = [16, 20] if args.quick else list(range(15, 21))
     results = {FP16: ({}, {}), SPLIT_FP32: ({}, {})}
-    for logn in rows:
-        n = 1 << logn
-        ch = tune(n, gib // n, FP16, reps=10)
-        results[FP16][0].update(ch)
-        print("FP16 2^%d:" % logn, {TILE_NAMES[t]: k for k, t in ch.items()}, flush=True)
+    for prec, per, top in ((FP16, gib, 14), (SPLIT_FP32, gib // 2, 13)):
+        for logn in rows:
+            if logn > top:
+                continue
+            n = 1 << logn
+            ch = tune(n, per // n, prec, reps=10)
+            results[prec][0].update(ch)
+            print("%s 2^%d:" % ("FP16" if prec == FP16 else "split", logn),
+                  {TILE_NAMES[t]: k for k, t in ch.items()}, flush=True)
     for prec, per in ((FP16, gib), (SPLIT_FP32, gib // 2)):
         for logn in fours:
             n = 1 << logn

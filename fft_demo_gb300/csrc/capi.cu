@@ -70,6 +70,7 @@ void init_registry() {
   register_split_row_kernels(g_tab[kPrecSplit][kPassRow]);
   register_split_col_kernels(g_tab[kPrecSplit][kPassCol]);
   register_split_rowt_kernels(g_tab[kPrecSplit][kPassRowT]);
+  register_split_mid_kernels(g_tab[kPrecSplit][kPassRow], g_tab[kPrecSplit][kPassCol], g_tab[kPrecSplit][kPassRowT]);
   register_fused_kernels(g_fused);
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -87,7 +88,7 @@ void init_registry() {
                                    cudaSharedmemCarveoutMaxShared);
           if (e != cudaSuccess) break;
           int occ = 0;
-          e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pk.fn, kPassThreads, pk.smem);
+          e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, pk.fn, pk.threads, pk.smem);
           if (e != cudaSuccess) break;
           // Own bound from the resources a CTA holds (registers, shared memory,
           // threads); the larger of this and the runtime's answer is used.
@@ -95,9 +96,9 @@ void init_registry() {
           e = cudaFuncGetAttributes(&fa, pk.fn);
           if (e != cudaSuccess) break;
           const int regs_per_warp = ((fa.numRegs * 32 + 255) / 256) * 256;
-          const int by_regs = 65536 / (regs_per_warp * (kPassThreads / 32));
+          const int by_regs = 65536 / (regs_per_warp * (pk.threads / 32));
           const int by_smem = (228 * 1024) / (pk.smem + static_cast<int>(fa.sharedSizeBytes) + 1024);
-          const int by_threads = 2048 / kPassThreads;
+          const int by_threads = 2048 / pk.threads;
           int own = by_regs < by_smem ? by_regs : by_smem;
           own = own < by_threads ? own : by_threads;
           if (own > occ) occ = own;
@@ -297,7 +298,7 @@ tcfftStatus launch_pass(int prec, int kind, int logL, int tile, int sign_idx, co
   if (grid < 1) grid = 1;
   if (grid > ntiles) grid = ntiles;
   void* kargs[] = {const_cast<IO*>(&io), const_cast<PassCore*>(&core)};
-  cudaError_t e = cudaLaunchKernel(pk.fn, dim3(static_cast<unsigned>(grid)), dim3(kPassThreads), kargs,
+  cudaError_t e = cudaLaunchKernel(pk.fn, dim3(static_cast<unsigned>(grid)), dim3(pk.threads), kargs,
                                    static_cast<size_t>(pk.smem), stream);
   if (e != cudaSuccess) return TCFFT_LAUNCH_FAILED;
   ++g_last_launches;

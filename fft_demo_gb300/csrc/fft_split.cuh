@@ -100,7 +100,7 @@ __device__ __forceinline__ float max_abs4(const float2 (&v)[4]) {
 // the planes wait for every group (mbar[NG - 1]): the planes are rewritten in
 // place, and a later group's MMAs may still be reading them. Returns false if
 // a bounded wait gave up (the group is then skipped).
-template <int L, int G, bool LINE_MINOR, int s, class IO>
+template <int L, int G, bool LINE_MINOR, int s, class IO, int NT = kPassThreads>
 __device__ __forceinline__ bool split_stage_epilogue(const SplitPlanes& P, const float2* __restrict__ tw,
                                                      uint32_t tbase, int warp, int lane, const IO& io,
                                                      long long line0, float out_scale, uint64_t* mbar,
@@ -117,7 +117,7 @@ __device__ __forceinline__ bool split_stage_epilogue(const SplitPlanes& P, const
   if constexpr (TensorMapIo<IO> && LINE_MINOR) stage_tensor = LAST && io.out_tma;
   bool planes_free = LAST && !stage_tensor;
 #pragma unroll 1
-  for (int grp = warp >> 2; grp < NG; grp += kPassThreads / 128) {
+  for (int grp = warp >> 2; grp < NG; grp += NT / 128) {
     const int m = grp * 128 + 32 * (warp & 3) + lane;
     int g, j;
     Tl::unpos(m, g, j);
@@ -310,7 +310,7 @@ __device__ __forceinline__ void split_setup(SplitState& st, const uint32_t* __re
   st.smax = reinterpret_cast<int*>(st.smem + 4096 + 8 * kSplitMaxGroups + 8);
   st.tma_bar = reinterpret_cast<uint64_t*>(st.smem + 4096 + 8 * kSplitMaxGroups + 16);
   const int tid = threadIdx.x;
-  for (int i = tid; i < 1024; i += kPassThreads) reinterpret_cast<uint32_t*>(st.bhi)[i] = __ldg(bmat_g + i);
+  for (int i = tid; i < 1024; i += blockDim.x) reinterpret_cast<uint32_t*>(st.bhi)[i] = __ldg(bmat_g + i);
   if (tid == 0) {
     for (int k = 0; k < kSplitMaxGroups; ++k) mbar_init(st.mbar + k, 1);
     mbar_init(st.tma_bar, 1);
@@ -352,7 +352,8 @@ concept L2PrefetchIo = requires(const IO& io) { io.prefetch_tile_l2(0ll, 0, 0); 
 // prefetched into L2 while this one runs.
 // TMA_IN: the tile arrives by tensor loads (column tiles whose IO carries an
 // input map); a template parameter so each load path is compiled on its own.
-template <int L, int G, bool LINE_MINOR, int SIGN, class IO, bool TMA_IN = false>
+// NT: threads per CTA (256, or 128 for 256-row tiles run 4 CTAs per SM).
+template <int L, int G, bool LINE_MINOR, int SIGN, class IO, bool TMA_IN = false, int NT = kPassThreads>
 __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const PassCore& core, long long line0,
                                            long long next_line0 = -1) {
   using Sh = LineShape<L>;
@@ -425,7 +426,7 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
     if constexpr (IO::IN_VEC_L) {
       constexpr int QPL = (L / T) / 4;
       constexpr int ITEMS = G * QPL;
-      static_assert(ITEMS <= kPassThreads * U, "one load batch per tile");
+      static_assert(ITEMS <= NT * U, "one load batch per tile");
       // item -> (line g, first of four consecutive butterflies j0): a warp's
       // loads run along one line
       auto item_g = [](int it) { return it / QPL; };
@@ -433,7 +434,7 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
       typename IO::Raw raw[U][T];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const int it = tid + u * kPassThreads;
+        const int it = tid + u * NT;
 #pragma unroll
         for (int r = 0; r < T; ++r)
           raw[u][r] = io.fetch_l(line0 + item_g(it), item_j0(it) + r * (L / T), it < ITEMS);
@@ -442,7 +443,7 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
       float lmax = 0.f;
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const int it = tid + u * kPassThreads;
+        const int it = tid + u * NT;
         const int g = item_g(it);
         const int j0 = item_j0(it);
 #pragma unroll
@@ -454,8 +455,8 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
       scales_from(lmax);
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const int it = tid + u * kPassThreads;
-        if (ITEMS % (kPassThreads * U) != 0 && it >= ITEMS) continue;
+        const int it = tid + u * NT;
+        if (ITEMS % (NT * U) != 0 && it >= ITEMS) continue;
         const int g = item_g(it);
         const int j0 = item_j0(it);
 #pragma unroll
@@ -509,7 +510,7 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
     } else {
       constexpr int GQ = G / 4;
       constexpr int ITEMS = GQ * (L / T);
-      static_assert(ITEMS <= kPassThreads * U, "one load batch per tile");
+      static_assert(ITEMS <= NT * U, "one load batch per tile");
       typename IO::Raw raw[U][T];
       bool loaded = false;
       if constexpr (TMA_IN) {
@@ -528,11 +529,11 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
           const uint8_t* src = st.smem + kSplitPlaneOffset;
 #pragma unroll
           for (int u = 0; u < U; ++u) {
-            const int it = tid + u * kPassThreads;
+            const int it = tid + u * NT;
 #pragma unroll
             for (int r = 0; r < T; ++r) {
               raw[u][r] = typename IO::Raw{make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
-              if (ITEMS % (kPassThreads * U) == 0 || it < ITEMS) {
+              if (ITEMS % (NT * U) == 0 || it < ITEMS) {
                 const uint8_t* p =
                     src + ((static_cast<uint32_t>(it / GQ + r * (L / T)) * G + (it % GQ) * 4u) << 3);
                 raw[u][r].a = *reinterpret_cast<const uint4*>(p);
@@ -546,7 +547,7 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
       if (!loaded) {
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-          const int it = tid + u * kPassThreads;
+          const int it = tid + u * NT;
 #pragma unroll
           for (int r = 0; r < T; ++r)
             raw[u][r] = io.fetch_g(line0 + (it % GQ) * 4, it / GQ + r * (L / T), it < ITEMS);
@@ -556,7 +557,7 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
       float lmax = 0.f;
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const int it = tid + u * kPassThreads;
+        const int it = tid + u * NT;
         const int j = it / GQ;
         const int g0 = (it % GQ) * 4;
 #pragma unroll
@@ -568,8 +569,8 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
       scales_from(lmax);
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const int it = tid + u * kPassThreads;
-        if (ITEMS % (kPassThreads * U) != 0 && it >= ITEMS) continue;
+        const int it = tid + u * NT;
+        if (ITEMS % (NT * U) != 0 && it >= ITEMS) continue;
         const int j = it / GQ;
         const int g0 = (it % GQ) * 4;
 #pragma unroll
@@ -634,7 +635,7 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
           umma_commit(st.mbar + grp);  // this group and every earlier one
         }
       }
-      const bool to = !split_stage_epilogue<L, G, LINE_MINOR, s, IO>(P, core.tw, st.tbase, warp, lane, io, line0,
+      const bool to = !split_stage_epilogue<L, G, LINE_MINOR, s, IO, NT>(P, core.tw, st.tbase, warp, lane, io, line0,
                                                                      out_scale, st.mbar, st.phase & 1u);
       if (to && lane == 0) atomicOr(core.err, kErrMmaTimeout);
       st.phase++;
@@ -651,9 +652,8 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
 // ---------------------------------------------------------------------------
 // Split-precision pass kernel: persistent CTAs over the tiles of one pass.
 // ---------------------------------------------------------------------------
-template <int L, int G, bool LINE_MINOR, int SIGN, class IO>
-__global__ void __launch_bounds__(kPassThreads, 2) fft_pass_split(const __grid_constant__ IO io,
-                                                                  const PassCore core) {
+template <int L, int G, bool LINE_MINOR, int SIGN, class IO, int NT = kPassThreads>
+__global__ void __launch_bounds__(NT, 512 / NT) fft_pass_split(const __grid_constant__ IO io, const PassCore core) {
   constexpr uint32_t TMEM_COLS = split_tmem_cols<L, G>();
   static_assert(TMEM_COLS >= 32 && (TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM columns");
   SplitState st;
@@ -667,10 +667,10 @@ __global__ void __launch_bounds__(kPassThreads, 2) fft_pass_split(const __grid_c
     const long long next = tile + gridDim.x < ntiles ? (tile + gridDim.x) * G : -1;
     bool ok;
     if constexpr (TensorMapIo<IO> && !IO::IN_VEC_L) {
-      ok = tma_in ? split_tile<L, G, LINE_MINOR, SIGN, IO, true>(st, io, core, tile * G, next)
-                  : split_tile<L, G, LINE_MINOR, SIGN, IO, false>(st, io, core, tile * G, next);
+      ok = tma_in ? split_tile<L, G, LINE_MINOR, SIGN, IO, true, NT>(st, io, core, tile * G, next)
+                  : split_tile<L, G, LINE_MINOR, SIGN, IO, false, NT>(st, io, core, tile * G, next);
     } else {
-      ok = split_tile<L, G, LINE_MINOR, SIGN, IO>(st, io, core, tile * G, next);
+      ok = split_tile<L, G, LINE_MINOR, SIGN, IO, false, NT>(st, io, core, tile * G, next);
     }
     if (!ok) break;
     if constexpr (TensorMapIo<IO> && LINE_MINOR) {

@@ -19,7 +19,7 @@ enum PassKind : int {
 
 // Tile-size variants: Mt = butterflies per radix-16 stage in one tile
 // (FP16: small 128, big 1024, mid 512 compiled for 3 CTAs/SM;
-//  split: small 128, big 512).
+//  split: small 128, big 512, mid 256 with 128 threads, 4 CTAs/SM).
 enum TileSel : int { kTileSmall = 0, kTileBig = 1, kTileMid = 2, kNumTileSel = 3 };
 
 enum PrecSel : int { kPrecF16 = 0, kPrecSplit = 1, kNumPrec = 2 };
@@ -32,6 +32,7 @@ struct PassKernel {
   int smem = 0;
   int G = 0;   // lines per tile
   int Mt = 0;  // butterflies per stage per tile
+  int threads = kPassThreads;
 };
 
 using PassTable = PassKernel[kMaxLogL + 1][kNumTileSel][2];
@@ -43,6 +44,7 @@ void register_rowt_kernels(PassTable& tab);
 void register_split_row_kernels(PassTable& tab);
 void register_split_col_kernels(PassTable& tab);
 void register_split_rowt_kernels(PassTable& tab);
+void register_split_mid_kernels(PassTable& row, PassTable& col, PassTable& rowt);
 
 template <int L, int Mt>
 constexpr int tile_lines() {
@@ -82,18 +84,19 @@ void fill_pf_entry(PassTable& tab, int tile) {
   tab[LOG][tile][1] = i;
 }
 
-template <int L, int Mt, bool LINE_MINOR, bool IN_VEC_L, bool OUT_VEC_L>
+template <int L, int Mt, bool LINE_MINOR, bool IN_VEC_L, bool OUT_VEC_L, int NT = kPassThreads>
 void fill_split_entry(PassTable& tab, int tile) {
   constexpr int G = tile_lines<L, Mt>();
   constexpr int LOG = ilog2c(L);
   const int smem = split_smem_bytes<L, G>();
   PassKernel f, i;
   using IO = IoFloat<IN_VEC_L, OUT_VEC_L>;
-  f.fn = reinterpret_cast<const void*>(&fft_pass_split<L, G, LINE_MINOR, -1, IO>);
-  i.fn = reinterpret_cast<const void*>(&fft_pass_split<L, G, LINE_MINOR, +1, IO>);
+  f.fn = reinterpret_cast<const void*>(&fft_pass_split<L, G, LINE_MINOR, -1, IO, NT>);
+  i.fn = reinterpret_cast<const void*>(&fft_pass_split<L, G, LINE_MINOR, +1, IO, NT>);
   f.smem = i.smem = smem;
   f.G = i.G = G;
   f.Mt = i.Mt = Mt;
+  f.threads = i.threads = NT;
   tab[LOG][tile][0] = f;
   tab[LOG][tile][1] = i;
 }
