@@ -20,8 +20,8 @@ import os
 from . import FP16, FORWARD, lib, plan_1d, plan_2d, _check
 
 PASS_ROW, PASS_COL, PASS_ROWT = 0, 1, 2
-TILE_SMALL, TILE_BIG, TILE_MID = 0, 1, 2
-TILE_NAMES = {TILE_SMALL: "small", TILE_BIG: "big", TILE_MID: "mid"}
+TILE_SMALL, TILE_BIG, TILE_MID, TILE_NARROW = 0, 1, 2, 3
+TILE_NAMES = {TILE_SMALL: "small", TILE_BIG: "big", TILE_MID: "mid", TILE_NARROW: "narrow"}
 
 
 def cache_path():

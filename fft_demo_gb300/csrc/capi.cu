@@ -71,6 +71,7 @@ void init_registry() {
   register_split_col_kernels(g_tab[kPrecSplit][kPassCol]);
   register_split_rowt_kernels(g_tab[kPrecSplit][kPassRowT]);
   register_split_mid_kernels(g_tab[kPrecSplit][kPassRow], g_tab[kPrecSplit][kPassCol], g_tab[kPrecSplit][kPassRowT]);
+  register_f16_narrow_kernels(g_tab[kPrecF16][kPassRow], g_tab[kPrecF16][kPassCol], g_tab[kPrecF16][kPassRowT]);
   register_fused_kernels(g_fused);
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -274,7 +275,7 @@ void attach_tensor_maps(IO& io, int kind, int tile, int logL, int G) {
     constexpr int esize = static_cast<int>(sizeof(*io.out));
     constexpr bool split = esize == 8;
     io.in_tma = io.out_tma = false;
-    if (kind == kPassRow || (!split && tile != kTileMid)) return;
+    if (kind == kPassRow || (!split && tile != kTileMid && tile != kTileNarrow)) return;
     const long long lps = 1ll << io.lps_log2;
     if (lps % G != 0 || io.total_lines % lps != 0 || G % 4 != 0) return;
     const long long nseq = io.total_lines / lps;

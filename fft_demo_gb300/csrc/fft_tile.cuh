@@ -215,7 +215,7 @@ __device__ __forceinline__ void ld_quad(const uint8_t* re, const uint8_t* im, ui
 //                       adjacent lines in line-minor order, so every warp store
 //                       is one contiguous segment per output index c).
 // ---------------------------------------------------------------------------
-template <int L, int G, bool LINE_MINOR, int s, class IO>
+template <int L, int G, bool LINE_MINOR, int s, class IO, int NT = kPassThreads>
 __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const float2* __restrict__ tw,
                                                uint32_t tbase, int warp, int lane, const IO& io,
                                                long long line0, bool stage_out) {
@@ -226,7 +226,7 @@ __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const f
   constexpr int Ns = Sh::T << (4 * s);
   constexpr bool LAST = (s == Sh::S - 1);
 #pragma unroll 1
-  for (int grp = warp >> 2; grp < NG; grp += kPassThreads / 128) {
+  for (int grp = warp >> 2; grp < NG; grp += NT / 128) {
     const int m = grp * 128 + 32 * (warp & 3) + lane;
     int g, j;
     Tl::unpos(m, g, j);
@@ -400,7 +400,7 @@ __device__ __forceinline__ void pass_setup(PassState& st, const uint32_t* __rest
   st.tma_bar = reinterpret_cast<uint64_t*>(st.smem + 2056);
   st.tslot = reinterpret_cast<uint32_t*>(st.smem + 2064);
   const int tid = threadIdx.x;
-  for (int i = tid; i < 512; i += kPassThreads) reinterpret_cast<uint32_t*>(st.bmat)[i] = __ldg(bmat_g + i);
+  for (int i = tid; i < 512; i += blockDim.x) reinterpret_cast<uint32_t*>(st.bmat)[i] = __ldg(bmat_g + i);
   if (tid == 0) {
     mbar_init(st.mbar, 1);
     mbar_init(st.tma_bar, 1);
@@ -429,7 +429,7 @@ __device__ __forceinline__ void pass_teardown(PassState& st) {
 
 // The S radix-16 tensor-core stages of one tile held in the planes (MMA
 // batch, commit, bounded wait, epilogue). False if a wait gave up.
-template <int L, int G, bool LINE_MINOR, int SIGN, class IO>
+template <int L, int G, bool LINE_MINOR, int SIGN, class IO, int NT = kPassThreads>
 __device__ __forceinline__ bool run_stages(PassState& st, const IO& io, const PassCore& core, long long line0,
                                            uint8_t* re, uint8_t* im, bool stage_out) {
   using Sh = LineShape<L>;
@@ -474,7 +474,7 @@ __device__ __forceinline__ bool run_stages(PassState& st, const IO& io, const Pa
         return;
       }
       tc_fence_after_sync();
-      stage_epilogue<L, G, LINE_MINOR, s, IO>(re, im, core.tw, st.tbase, warp, lane, io, line0, stage_out);
+      stage_epilogue<L, G, LINE_MINOR, s, IO, NT>(re, im, core.tw, st.tbase, warp, lane, io, line0, stage_out);
       fence_proxy_async_smem();
       tc_fence_before_sync();
       __syncthreads();
@@ -746,7 +746,7 @@ __global__ void __launch_bounds__(kPassThreads, MINB) fft_pass_f16(const IO io, 
 //   raw layout: natural [line][l] half2 (vector-along-line inputs) or
 //               line-minor [l][line] half2 (column inputs)
 // ---------------------------------------------------------------------------
-template <int L, int G, bool LINE_MINOR, class IO>
+template <int L, int G, bool LINE_MINOR, class IO, int NT = kPassThreads>
 __device__ __forceinline__ void prefetch_tile(PassState& st, const IO& io, long long line0, uint8_t* raw) {
   if (IO::IN_VEC_L && io.in_contig) {
     if (threadIdx.x == 0) {
@@ -776,7 +776,7 @@ __device__ __forceinline__ void prefetch_tile(PassState& st, const IO& io, long 
     constexpr int GQ = G / 4;
     constexpr int CH = L * GQ;
 #pragma unroll 4
-    for (int c = threadIdx.x; c < CH; c += kPassThreads) {
+    for (int c = threadIdx.x; c < CH; c += NT) {
       const int l = c / GQ, q = c % GQ;
       bool ok;
       const void* src = io.src_g(line0 + 4 * q, l, ok);
@@ -787,7 +787,7 @@ __device__ __forceinline__ void prefetch_tile(PassState& st, const IO& io, long 
     constexpr int QPL = L / 4;
     constexpr int CH = G * QPL;
 #pragma unroll 4
-    for (int c = threadIdx.x; c < CH; c += kPassThreads) {
+    for (int c = threadIdx.x; c < CH; c += NT) {
       const int g = c / QPL, q = c % QPL;
       bool ok;
       const void* src = io.src_l(line0 + g, 4 * q, ok);
@@ -829,7 +829,7 @@ __device__ __forceinline__ bool wait_prefetch(PassState& st, const IO& io, const
 
 // raw (staged input) -> planes, with the radix-T first stage and the first
 // radix-16 stage's twiddle. Lines >= nval read as zero.
-template <int L, int G, bool LINE_MINOR, int SIGN, class IO>
+template <int L, int G, bool LINE_MINOR, int SIGN, class IO, int NT = kPassThreads>
 __device__ __forceinline__ void permute_raw(const uint8_t* raw, uint8_t* re, uint8_t* im, const PassCore& core,
                                             int nval) {
   using Sh = LineShape<L>;
@@ -849,7 +849,7 @@ __device__ __forceinline__ void permute_raw(const uint8_t* raw, uint8_t* re, uin
     constexpr int ITEMS = (G / LPI) * JT;
     const uint32_t* raw32 = reinterpret_cast<const uint32_t*>(raw);
 #pragma unroll 2
-    for (int it = tid; it < ITEMS; it += kPassThreads) {
+    for (int it = tid; it < ITEMS; it += NT) {
       const int j = it % JT;
       const int g0 = (it / JT) * LPI;
       uint32_t w[T][LPI];
@@ -906,7 +906,7 @@ __device__ __forceinline__ void permute_raw(const uint8_t* raw, uint8_t* re, uin
     constexpr int QPL = (L / T) / 4;
     constexpr int ITEMS = G * QPL;
 #pragma unroll 2
-    for (int it = tid; it < ITEMS; it += kPassThreads) {
+    for (int it = tid; it < ITEMS; it += NT) {
       const int g = it / QPL;
       const int j0 = (it % QPL) * 4;
       uint4 w[T];
@@ -961,7 +961,7 @@ __device__ __forceinline__ void permute_raw(const uint8_t* raw, uint8_t* re, uin
     constexpr int GQ = G / 4;
     constexpr int ITEMS = GQ * (L / T);
 #pragma unroll 2
-    for (int it = tid; it < ITEMS; it += kPassThreads) {
+    for (int it = tid; it < ITEMS; it += NT) {
       const int j = it / GQ;
       const int g0 = (it % GQ) * 4;
       uint4 w[T];
@@ -1012,9 +1012,9 @@ __device__ __forceinline__ void permute_raw(const uint8_t* raw, uint8_t* re, uin
   }
 }
 
-template <int L, int G, bool LINE_MINOR, int SIGN, class IO, int MINB = 3>
-__global__ void __launch_bounds__(kPassThreads, MINB) fft_pass_f16_pf(const __grid_constant__ IO io,
-                                                                      const PassCore core) {
+// NT: threads per CTA (256, or 128 for 256-row tiles run 6 CTAs per SM).
+template <int L, int G, bool LINE_MINOR, int SIGN, class IO, int MINB = 3, int NT = kPassThreads>
+__global__ void __launch_bounds__(NT, MINB) fft_pass_f16_pf(const __grid_constant__ IO io, const PassCore core) {
   using Tl = Tile<L, G, LINE_MINOR>;
   constexpr uint32_t TMEM_COLS = pass_tmem_cols<L, G>();
   static_assert(TMEM_COLS >= 32 && (TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM columns");
@@ -1031,7 +1031,7 @@ __global__ void __launch_bounds__(kPassThreads, MINB) fft_pass_f16_pf(const __gr
   long long tile = blockIdx.x;
   bool pending = false;
   if (tile < ntiles) {
-    prefetch_tile<L, G, LINE_MINOR, IO>(st, io, tile * G, raw);
+    prefetch_tile<L, G, LINE_MINOR, IO, NT>(st, io, tile * G, raw);
     pending = true;
   }
   for (; tile < ntiles; tile += gridDim.x) {
@@ -1045,15 +1045,15 @@ __global__ void __launch_bounds__(kPassThreads, MINB) fft_pass_f16_pf(const __gr
     pending = false;
     if ((stage_out || tensor_store) && threadIdx.x == 0) bulk_wait_read_all();  // previous store has read the planes
     __syncthreads();
-    permute_raw<L, G, LINE_MINOR, SIGN, IO>(raw, re, im, core, nval);
+    permute_raw<L, G, LINE_MINOR, SIGN, IO, NT>(raw, re, im, core, nval);
     fence_proxy_async_smem();
     tc_fence_before_sync();
     __syncthreads();
     if (tile + gridDim.x < ntiles) {
-      prefetch_tile<L, G, LINE_MINOR, IO>(st, io, (tile + gridDim.x) * G, raw);
+      prefetch_tile<L, G, LINE_MINOR, IO, NT>(st, io, (tile + gridDim.x) * G, raw);
       pending = true;
     }
-    if (!run_stages<L, G, LINE_MINOR, SIGN, IO>(st, io, core, line0, re, im, stage_out)) break;
+    if (!run_stages<L, G, LINE_MINOR, SIGN, IO, NT>(st, io, core, line0, re, im, stage_out)) break;
     if (stage_out && threadIdx.x == 0) {
       bulk_s2g(io.tile_dst(line0), re, static_cast<uint32_t>(nval) * L * 4u);
       bulk_commit();

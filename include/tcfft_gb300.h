@@ -243,8 +243,11 @@ int tcfft_last_launch_count(void);
 typedef enum tcfftPassKind { TCFFT_PASS_ROW = 0, TCFFT_PASS_COL = 1, TCFFT_PASS_ROWT = 2 } tcfftPassKind;
 typedef enum tcfftTile {
   TCFFT_TILE_SMALL = 0,  /* 128 MMA rows per tile */
-  TCFFT_TILE_BIG = 1,    /* 1024 rows */
-  TCFFT_TILE_MID = 2     /* 512 rows, next tile prefetched, 3 CTAs/SM */
+  TCFFT_TILE_BIG = 1,    /* FP16 1024 rows; split precision 512 rows */
+  TCFFT_TILE_MID = 2,    /* FP16 512 rows, next tile prefetched, 3 CTAs/SM;
+                            split precision 256 rows on 128 threads, 4 CTAs/SM */
+  TCFFT_TILE_NARROW = 3  /* FP16 256 rows, next tile prefetched, 128 threads,
+                            6 CTAs/SM */
 } tcfftTile;
 /* tile = -1 restores the built-in choice. */
 tcfftStatus tcfft_tune_set(int precision, int pass_kind, int log2_len, int tile);

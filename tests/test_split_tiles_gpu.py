@@ -21,7 +21,7 @@ PASS_ROW, PASS_COL, PASS_ROWT = 0, 1, 2
 
 def _variants(tc, kind, logl):
     out = []
-    for t in range(3):
+    for t in range(4):
         g, c, s = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         if tc.lib().tcfft_pass_info(SPLIT, kind, logl, t, ctypes.byref(g), ctypes.byref(c),
                                     ctypes.byref(s)) == 0:

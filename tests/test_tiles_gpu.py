@@ -18,7 +18,7 @@ PASS_ROW, PASS_COL, PASS_ROWT = 0, 1, 2
 
 def _variants(tc, kind, logl):
     out = []
-    for t in range(3):  # small, big, mid (prefetching)
+    for t in range(4):  # small, big, mid and narrow (prefetching)
         g, c, s = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
         if tc.lib().tcfft_pass_info(0, kind, logl, t, ctypes.byref(g), ctypes.byref(c), ctypes.byref(s)) == 0:
             out.append(t)
