@@ -94,6 +94,14 @@ __device__ __forceinline__ float max_abs4(const float2 (&v)[4]) {
   return m;
 }
 
+// IO types whose row store (and staging) take an extra factor s, applied
+// with their own scale as one multiply.
+template <class IO>
+concept ScaledStoreIo = requires(const IO& io, float2 (&r)[16]) {
+  io.store_row16(0ll, 0, 0, r, 1.0f);
+  io.prepare_row16(0ll, 0, 0, r, 1.0f);
+};
+
 // Each warp waits for its own group's MMAs (mbar[grp], committed per group)
 // before reading that group's accumulator, so TMEM reads (and, in the last
 // stage, the global stores) overlap the MMAs of later groups. Stores into
@@ -171,10 +179,15 @@ __device__ __forceinline__ bool split_stage_epilogue(const SplitPlanes& P, const
     if constexpr (LAST) {
       const long long line = line0 + g;
       if (line < io.total_lines) {
+        // IO types that take an extra factor fold the tile scale into their
+        // own scale (one multiply per value instead of two)
+        constexpr bool FOLD = ScaledStoreIo<IO>;
+        if constexpr (!FOLD) {
 #pragma unroll
-        for (int c = 0; c < 16; ++c) {
-          v[c].x *= out_scale;
-          v[c].y *= out_scale;
+          for (int c = 0; c < 16; ++c) {
+            v[c].x *= out_scale;
+            v[c].y *= out_scale;
+          }
         }
         bool staged = false;
         if constexpr (TensorMapIo<IO> && LINE_MINOR) {
@@ -189,14 +202,24 @@ __device__ __forceinline__ bool split_stage_epilogue(const SplitPlanes& P, const
               }
               planes_free = true;
             }
-            io.prepare_row16(line, j, J, v);
+            if constexpr (FOLD) {
+              io.prepare_row16(line, j, J, v, out_scale);
+            } else {
+              io.prepare_row16(line, j, J, v);
+            }
             float2* col = reinterpret_cast<float2*>(P.rh) + g;
 #pragma unroll
             for (int c = 0; c < 16; ++c) col[(j + c * J) * G] = v[c];
             staged = true;
           }
         }
-        if (!staged) io.store_row16(line, j, J, v);
+        if (!staged) {
+          if constexpr (FOLD) {
+            io.store_row16(line, j, J, v, out_scale);
+          } else {
+            io.store_row16(line, j, J, v);
+          }
+        }
       }
     } else {
       if (!planes_free) {
@@ -793,7 +816,9 @@ struct IoFloat {
   __device__ __forceinline__ void decode_g(const Raw& r, long long, int, float2 (&v)[4]) const { unpack(r, v); }
   // Outer twiddle and scale applied in place to outputs l = j + c*J of one
   // line (same values as store_row16 writes), for the staged tensor store.
-  __device__ __forceinline__ void prepare_row16(long long line, int j, int J, float2 (&v)[16]) const {
+  __device__ __forceinline__ void prepare_row16(long long line, int j, int J, float2 (&v)[16],
+                                                float s = 1.0f) const {
+    const float k = scale * s;
     if (otw.hi) {
       const long long li = line & ((1ll << lps_log2) - 1);
       float2 wq[4];
@@ -808,13 +833,16 @@ struct IoFloat {
       }
     }
 #pragma unroll
-    for (int c = 0; c < 16; ++c) v[c] = make_float2(v[c].x * scale, v[c].y * scale);
+    for (int c = 0; c < 16; ++c) v[c] = make_float2(v[c].x * k, v[c].y * k);
   }
   // Outputs l = j + c*J (c = 0..15) of one line. The outer twiddle
   // W_N^{li*l} is exact (two-level table) at c = 0, 4, 8, 12; in between it
   // follows from the exact step W_N^{li*J} (at most three FP32 products from
-  // an exact value), so a row costs 5 table pairs instead of 16.
-  __device__ __forceinline__ void store_row16(long long line, int j, int J, float2 (&v)[16]) const {
+  // an exact value), so a row costs 5 table pairs instead of 16. The
+  // stored values are scaled by scale * s.
+  __device__ __forceinline__ void store_row16(long long line, int j, int J, float2 (&v)[16],
+                                              float s = 1.0f) const {
+    const float k = scale * s;
     float2* p = out + out_base(line);
     const long long li = line & ((1ll << lps_log2) - 1);
     if (otw.hi) {
@@ -827,12 +855,12 @@ struct IoFloat {
       for (int c = 0; c < 16; ++c) {
         w = (c & 3) == 0 ? wq[c >> 2] : cmulf(w, step);
         const float2 x = cmulf(v[c], w);
-        p[static_cast<long long>(j + c * J) * out_elem] = make_float2(x.x * scale, x.y * scale);
+        p[static_cast<long long>(j + c * J) * out_elem] = make_float2(x.x * k, x.y * k);
       }
     } else {
 #pragma unroll
       for (int c = 0; c < 16; ++c)
-        p[static_cast<long long>(j + c * J) * out_elem] = make_float2(v[c].x * scale, v[c].y * scale);
+        p[static_cast<long long>(j + c * J) * out_elem] = make_float2(v[c].x * k, v[c].y * k);
     }
   }
 };

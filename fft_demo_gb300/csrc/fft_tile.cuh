@@ -252,9 +252,13 @@ __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const f
         if (stage_out) {
           // natural-order half2 copy of the tile for the bulk store
           uint32_t* row = reinterpret_cast<uint32_t*>(re) + static_cast<uint32_t>(g) * L + j;
+          if (io.scale != 1.0f) {
+#pragma unroll
+            for (int c = 0; c < 16; ++c) v[c] = make_float2(v[c].x * io.scale, v[c].y * io.scale);
+          }
 #pragma unroll
           for (int c = 0; c < 16; ++c) {
-            __half2 h = __floats2half2_rn(v[c].x * io.scale, v[c].y * io.scale);
+            __half2 h = __floats2half2_rn(v[c].x, v[c].y);
             row[c * J] = *reinterpret_cast<uint32_t*>(&h);
           }
           staged = true;
