@@ -404,8 +404,11 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
     if (next_line0 >= 0) io.prefetch_tile_l2(next_line0, G, L);
   }
   // a tensor store of the previous tile reads the plane region: it must be
-  // done reading before this tile's planes are written (no-op otherwise)
-  if (tid == 0) bulk_wait_read_all();
+  // done reading before this tile's planes are written (no-op otherwise).
+  // Tensor loads write the plane region, so they wait here; direct loads
+  // fill registers, so they are issued first and the wait comes at the
+  // barrier that precedes the first plane store (scales_from below).
+  if (TMA_IN && tid == 0) bulk_wait_read_all();
   // column tiles with an input map arrive by tensor loads into the plane
   // region ([L][G] elements), read back by the threads below
   constexpr bool tma_in = TMA_IN;
@@ -434,6 +437,9 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) lmax = fmaxf(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
       if (lane == 0) atomicMax(st.smax, __float_as_int(lmax));
+      if constexpr (!TMA_IN) {
+        if (tid == 0) bulk_wait_read_all();
+      }
       __syncthreads();
       const float tmax = __int_as_float(*st.smax) * static_cast<float>(T);
       // sigma: largest value after the radix-T stage maps to <= 2^14
