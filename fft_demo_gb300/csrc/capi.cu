@@ -306,8 +306,9 @@ tcfftStatus launch_pass(int prec, int kind, int logL, int tile, int sign_idx, co
   return TCFFT_OK;
 }
 
-// Tile variant for a pass: the tuned choice if one is set and built,
-// otherwise big tiles, or small ones when big ones would leave SMs idle.
+// Tile variant for a pass: the tuned choice if one is set and built;
+// otherwise narrow or mid tiles when they fill the GPU, else big tiles, or
+// small ones when big ones would leave SMs idle.
 int choose_tile(int prec, int kind, int logL, long long lines) {
   std::call_once(g_tune_once, tune_reset);
   const int t = g_tune[prec][kind][logL];
@@ -315,6 +316,12 @@ int choose_tile(int prec, int kind, int logL, long long lines) {
   const PassKernel& small = g_tab[prec][kind][logL][kTileSmall][0];
   const PassKernel& big = g_tab[prec][kind][logL][kTileBig][0];
   const PassKernel& mid = g_tab[prec][kind][logL][kTileMid][0];
+  const PassKernel& narrow = g_tab[prec][kind][logL][kTileNarrow][0];
+  // FP16 narrow tiles (256 rows on 128 threads, 6 CTAs/SM) when they fill
+  // the GPU and column-layout rows of the tile stay >= 32 bytes (G >= 8):
+  // the tuner's choice at every such length on GB300
+  if (narrow.fn && (kind == kPassRow || narrow.G >= 8) && (lines + narrow.G - 1) / narrow.G >= 6ll * g_num_sms)
+    return kTileNarrow;
   // prefetching mid tiles (3 CTAs/SM) when they fill the GPU, measured fastest
   if (mid.fn && (lines + mid.G - 1) / mid.G >= 3ll * g_num_sms) return kTileMid;
   if (!small.fn || !big.fn) return big.fn ? kTileBig : (mid.fn ? kTileMid : kTileSmall);
