@@ -75,3 +75,52 @@ def test_serving_loop_short_stream(tc):
     # output is small against the FP16-rounded spectra; bound 1e-2
     assert out["rel_l2_fp16_fft_max"] < 2e-3 and out["rel_l2_fp16_conv_max"] < 1e-2
     assert out["rel_l2_split_fft_max"] < 1e-5 and out["rel_l2_split_conv_max"] < 1e-5
+
+
+@pytest.mark.parametrize("precision,tol", [(tcm.FP16, 2e-3), (tcm.SPLIT_FP32, 1e-5)])
+def test_queue_result_same_alone_and_in_mix(tc, precision, tol):
+    """Each request's result submitted alone equals its result inside a mixed
+    submit (1D transforms of several sizes, two of one size, and
+    convolutions), within the precision's tolerance. In the mix, lines of
+    same-size transforms can share a tile (and, in split precision, its
+    scale), so equality is to the tolerance, not bitwise."""
+    import torch
+    rng = np.random.default_rng(21)
+    q = tc.Queue(precision, workspace_bytes=1 << 30, staging_bytes=4 << 20)
+    filters = [rng.standard_normal((f, f)).astype(np.float32) for f in (5, 15)]
+    for i, w in enumerate(filters):
+        q.set_filter(i, w)
+    dt = torch.float16 if precision == tcm.FP16 else torch.float32
+    sizes = [256, 1 << 12, 256, 1 << 16]
+    convs = [(96, 96, 0), (128, 128, 1)]
+    in_off, at = [], 0
+    for n in sizes:
+        in_off.append(at)
+        at += n
+    img_off, at_r = [], 2 * at
+    for s, _, _ in convs:
+        img_off.append(at_r)
+        at_r += s * s + (-(s * s)) % 8
+    arena = torch.from_numpy(rng.uniform(-1, 1, at_r).astype(np.float32)).to(dt).cuda()
+    conv_list = [(s, s, f, tcm.CONV_SAME, o, o) for (s, _, f), o in zip(convs, img_off)]
+    mix = torch.zeros(at_r, dtype=dt, device="cuda")
+    q.submit(sizes, in_off, in_off, conv_list, arena, mix, arena, mix)
+    q.check()
+    m = mix.double().cpu().numpy()
+
+    def rel(a, b):
+        return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+
+    for n, o in zip(sizes, in_off):
+        alone = torch.zeros(at_r, dtype=dt, device="cuda")
+        q.submit([n], [o], [o], x=arena, out=alone)
+        q.check()
+        a = alone.double().cpu().numpy()
+        assert rel(a[2 * o:2 * o + 2 * n], m[2 * o:2 * o + 2 * n]) < tol, n
+    for c, ((s, _, _), o) in enumerate(zip(convs, img_off)):
+        alone = torch.zeros(at_r, dtype=dt, device="cuda")
+        q.submit(convs=[conv_list[c]], conv_in=arena, conv_out=alone)
+        q.check()
+        a = alone.double().cpu().numpy()
+        assert rel(a[o:o + s * s], m[o:o + s * s]) < tol, s
+    q.destroy()
