@@ -74,3 +74,27 @@ def test_tuning_file_names_built_variants():
         else:
             prec, kind, logl = (int(p) for p in parts)
             assert int(val) in built.get((prec, kind, logl), set()), (key, val)
+
+
+def test_autotuner_pass_chain_matches_plan_rule():
+    """autotune.passes_of (the passes the tuner times) follows the plan's
+    built-in rule in capi.cu: single pass up to 2^14 (FP16) / 2^13 (split),
+    else a column pass of 2^a and a transposing pass of 2^(log n - a) with
+    a = min(log n / 2, 10), raised until the row pass is <= 2^12 / 2^11."""
+    from fft_demo_gb300 import FP16, SPLIT_FP32
+    from fft_demo_gb300.autotune import passes_of, PASS_COL, PASS_ROW, PASS_ROWT
+    assert passes_of(1 << 14, FP16) == [(PASS_ROW, 14)]
+    assert passes_of(1 << 15, FP16) == [(PASS_COL, 7), (PASS_ROWT, 8)]
+    assert passes_of(1 << 20, FP16) == [(PASS_COL, 10), (PASS_ROWT, 10)]
+    assert passes_of(1 << 24, FP16) == [(PASS_COL, 12), (PASS_ROWT, 12)]
+    assert passes_of(1 << 13, SPLIT_FP32) == [(PASS_ROW, 13)]
+    assert passes_of(1 << 14, SPLIT_FP32) == [(PASS_COL, 7), (PASS_ROWT, 7)]
+    assert passes_of(1 << 22, SPLIT_FP32) == [(PASS_COL, 11), (PASS_ROWT, 11)]
+    assert passes_of(1 << 20, SPLIT_FP32, split=9) == [(PASS_COL, 9), (PASS_ROWT, 11)]
+    assert passes_of(0, FP16, dims=2, shape2d=(1024, 512)) == [(PASS_ROW, 9), (PASS_COL, 10)]
+    # the same constants in the plan code
+    src = open(os.path.join(CSRC, "capi.cu")).read()
+    assert "const int single_max = precision == TCFFT_FP16 ? kMaxLogL : 13;" in src
+    assert "const int pass_max = precision == TCFFT_FP16 ? 12 : 11;" in src
+    assert "int a = logn / 2 < 10 ? logn / 2 : 10;" in src
+    assert "constexpr int kMaxLogL = 14;" in open(os.path.join(CSRC, "passes.cuh")).read()
