@@ -81,8 +81,14 @@ def _declare(L):
         "tcfft_get_last_error": (i, []),
         "tcfft_status_string": (ctypes.c_char_p, [i]),
         "tcfft_last_launch_count": (i, []),
+        "tcfft_set_wait_limit": (i, [ll]),
         "tcfft_conv2d_plan": (i, [ctypes.POINTER(vp), i, i, i, i, i, i, i, i, ll]),
         "tcfft_conv2d_set_filters": (i, [vp, vp, vp]),
+        "tcfft_conv2d_set_filters_qd": (i, [vp, vp, vp]),
+        "tcfft_qd_plan": (i, [ctypes.POINTER(vp), i, ll, i, i]),
+        "tcfft_qd_exec": (i, [vp, vp, vp, i, vp]),
+        "tcfft_qd_check": (i, [vp, vp]),
+        "tcfft_qd_destroy": (i, [vp]),
         "tcfft_conv2d_exec": (i, [vp, vp, vp, ll, vp]),
         "tcfft_conv2d_shape": (i, [vp, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)]),
         "tcfft_conv2d_check": (i, [vp, vp]),
@@ -116,6 +122,13 @@ def _stream_ptr(stream):
 
 def last_launch_count():
     return lib().tcfft_last_launch_count()
+
+
+def set_wait_limit(polls=-1):
+    """Poll bound of the persistent kernels' dependency waits for later
+    launches (tcfft_set_wait_limit); -1 restores the default, 0 makes every
+    such wait give up at once (the timeout path, for tests)."""
+    _check(lib().tcfft_set_wait_limit(int(polls)), "set_wait_limit")
 
 
 class Plan:
@@ -425,14 +438,16 @@ class Conv2d:
         import torch
         return torch.float16 if self.precision == FP16 else torch.float32
 
-    def set_filters(self, filters, stream=None):
+    def set_filters(self, filters, stream=None, projections=False):
+        """projections=True makes the spectra by line projections
+        (tcfft_conv2d_set_filters_qd) instead of the masked passes."""
         import torch
         if filters.dtype != torch.float32 or not filters.is_cuda or not filters.is_contiguous() or \
                 filters.numel() != self.F * self.S * self.fy * self.fx:
             raise TcfftError(INVALID_VALUE, "filters: contiguous float32 CUDA [F][S][fy][fx]")
         self._filters = filters
-        _check(lib().tcfft_conv2d_set_filters(self._h, _ptr(filters), _stream_ptr(stream)),
-               "set_filters")
+        fn = lib().tcfft_conv2d_set_filters_qd if projections else lib().tcfft_conv2d_set_filters
+        _check(fn(self._h, _ptr(filters), _stream_ptr(stream)), "set_filters")
 
     def exec(self, images, out=None, stream=None):
         import torch
@@ -453,6 +468,45 @@ class Conv2d:
     def destroy(self):
         if self._h:
             lib().tcfft_conv2d_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class QdPlan:
+    """Line-projection 2D DFT (tcfft_qd_*; the reference's qdFFT / fast_fft).
+
+    planes: complex float32 CUDA tensor [planes][n][n][2] whose non-zeros lie
+    in the top-left box_rows x box_cols box; exec returns the unnormalised 2D
+    DFTs in a new tensor of the same shape.
+    """
+
+    def __init__(self, n, planes, box_rows, box_cols):
+        self._h = ctypes.c_void_p()
+        self.n, self.planes = int(n), int(planes)
+        _check(lib().tcfft_qd_plan(ctypes.byref(self._h), self.n, self.planes, int(box_rows), int(box_cols)),
+               "qd_plan")
+
+    def exec(self, planes, out=None, direction=FORWARD, stream=None):
+        import torch
+        if planes.dtype != torch.float32 or not planes.is_cuda or not planes.is_contiguous() or \
+                planes.numel() != self.planes * self.n * self.n * 2:
+            raise TcfftError(INVALID_VALUE, "planes: contiguous float32 CUDA [planes][n][n][2]")
+        if out is None:
+            out = torch.empty_like(planes)
+        _check(lib().tcfft_qd_exec(self._h, _ptr(planes), _ptr(out), direction, _stream_ptr(stream)), "qd_exec")
+        return out
+
+    def check(self, stream=None):
+        _check(lib().tcfft_qd_check(self._h, _stream_ptr(stream)), "qd_check")
+
+    def destroy(self):
+        if self._h:
+            lib().tcfft_qd_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

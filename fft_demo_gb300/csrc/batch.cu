@@ -273,6 +273,7 @@ tcfftStatus build_persistent(tcfftBatchImpl* b) {
     }
   a.bmat = reinterpret_cast<const uint32_t*>(A + off_bmat);
   a.err = b->err;
+  a.wait_polls = dep_wait_polls();  // each launch refreshes it (launch_persistent)
   if (!bl.prep_items.empty()) {
     // filter spectra: the same kernel over the filter items, once
     BatchArgs pa = a;
@@ -321,6 +322,7 @@ tcfftStatus launch_persistent(tcfftBatchImpl* b, const Buffers& io, cudaStream_t
     return TCFFT_LAUNCH_FAILED;
   if (b->nitems == 0) return TCFFT_OK;
   BatchArgs a = b->args;
+  a.wait_polls = dep_wait_polls();
   a.in = io.in;
   a.out = io.out;
   a.conv_in = io.conv_in;

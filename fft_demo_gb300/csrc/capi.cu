@@ -11,6 +11,8 @@
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -156,6 +158,11 @@ const FusedKernel* fused_kernel(int logn, int sign_idx, int* grid_ctas) {
   if (grid_ctas) *grid_ctas = g_num_sms * g_fused_occ[logn][sign_idx];
   return &fk;
 }
+
+static constexpr unsigned int kDefaultWaitPolls = 1u << 24;
+static std::atomic<unsigned int> g_wait_polls{kDefaultWaitPolls};
+
+unsigned int dep_wait_polls() { return g_wait_polls.load(std::memory_order_relaxed); }
 
 tcfftStatus record_status(tcfftStatus s, int launches) {
   g_last_launches = launches;
@@ -450,6 +457,7 @@ tcfftStatus exec_fused(tcfftPlanImpl* p, const void* in, void* out, int sg, floa
   sc.chunk_seqs = p->chunk_seqs;
   sc.batch = p->batch;
   sc.n = p->n;
+  sc.wait_polls = dep_wait_polls();
   if (cudaMemsetAsync(p->counters, 0, sizeof(int) * (1 + 2 * static_cast<size_t>(p->nchunks)), st) != cudaSuccess)
     return TCFFT_LAUNCH_FAILED;
   long long items = static_cast<long long>(sc.nchunks) * (sc.tiles1 + sc.tiles2);
@@ -766,7 +774,9 @@ tcfftStatus tcfft_check(tcfftPlan p, void* stream) {
     return ret(TCFFT_LAUNCH_FAILED);
   if (h != 0) {
     cudaMemset(p->err, 0, sizeof(int));
-    return ret((h & kErrMmaTimeout) ? TCFFT_TIMEOUT : TCFFT_LAUNCH_FAILED);
+    // a bounded wait gave up: on the tensor cores / a copy, or (fused form)
+    // on a work item the item depended on
+    return ret((h & (kErrMmaTimeout | kErrQueueTimeout)) ? TCFFT_TIMEOUT : TCFFT_LAUNCH_FAILED);
   }
   return ret(TCFFT_OK);
 }
@@ -792,6 +802,12 @@ const char* tcfft_status_string(tcfftStatus s) {
     case TCFFT_NO_DEVICE: return "TCFFT_NO_DEVICE";
   }
   return "TCFFT_UNKNOWN";
+}
+
+tcfftStatus tcfft_set_wait_limit(long long polls) {
+  if (polls > static_cast<long long>(kDefaultWaitPolls)) return ret(TCFFT_INVALID_VALUE);
+  g_wait_polls.store(polls < 0 ? kDefaultWaitPolls : static_cast<unsigned int>(polls), std::memory_order_relaxed);
+  return ret(TCFFT_OK);
 }
 
 int tcfft_last_launch_count(void) { return g_last_launches; }

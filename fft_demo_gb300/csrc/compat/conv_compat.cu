@@ -12,6 +12,8 @@
 #include "../../../include/compat/fftconvolve2d.cuh"
 #include "../../../include/compat/tensorcore_fft_conv2d.h"
 #include "../../../include/tcfft_gb300.h"
+#include "../capi_internal.cuh"
+#include "../qd_internal.cuh"
 
 namespace {
 
@@ -249,12 +251,39 @@ void fft_conv2d_half::conv2d_forward(double* input, double* weight, double* out,
 }
 
 void fft_conv2d_half::TENSORCORE_FFT_CONV_2D() {
-  if (output) conv2d_forward(output);
+  if (!output) {
+    last_status = TCFFT_INVALID_VALUE;
+    return;
+  }
+  conv2d_forward(output);
 }
-void fft_conv2d_half::fft_conv2d_inv_rev_pad() {}
-void fft_conv2d_half::readout_fwd(bool) {}
-void fft_conv2d_half::fft_pointwise(float, bool) {}
-void fft_conv2d_half::fft_conv_final_stage() {}
+
+// The reference's constructor pads, flips and transforms the filters here
+// (kernel.cu:1255); the equivalent is rebuilding the plan and its resident
+// filter spectra from `filter`.
+void fft_conv2d_half::fft_conv2d_inv_rev_pad() {
+  if (!filter || S < 1 || F < 1) {
+    last_status = TCFFT_INVALID_VALUE;
+    return;
+  }
+  last_status = make_forward_plan(this);
+}
+
+// readout_fwd copies the cropped, scaled result to `output` (.cpp:275).
+// TENSORCORE_FFT_CONV_2D already wrote `output`, so after a successful one
+// there is nothing left to do; on its own it has no result to read.
+void fft_conv2d_half::readout_fwd(bool) {
+  if (!output || last_status != TCFFT_OK) last_status = TCFFT_UNSUPPORTED;
+}
+
+// The reference's intermediate forward steps (kernel.cu:1101,1141) leave
+// FP32 / FP16 pointwise planes in cu_pointwise_float / cu_pointwise_half.
+// Here the pointwise product and the inverse transform are stages of one
+// pipeline that keeps those planes inside the plan, so the steps cannot run
+// on their own: they report TCFFT_UNSUPPORTED instead of silently doing
+// nothing.
+void fft_conv2d_half::fft_pointwise(float, bool) { last_status = TCFFT_UNSUPPORTED; }
+void fft_conv2d_half::fft_conv_final_stage() { last_status = TCFFT_UNSUPPORTED; }
 
 // Gradients of out[f] = sum_s corr(x_s, w_fs) (valid):
 //   dW[f][s] = corr(x_s, delta_f) (valid, size fy x fx)
@@ -324,11 +353,17 @@ void fft_conv2d_half::conv2d_backward(double* delta_in) {
   }
 }
 
-void fft_conv2d_half::fft_conv2d_rev_pad(double*, double*, half*, half*, int, int, int, int, int) {}
-void fft_conv2d_half::inv_pad_deltain_signal(int) {}
-void fft_conv2d_half::pad_fx_1_circles_of_0(double*, int, int, int) {}
-void fft_conv2d_half::pointwise_for_delta_weight(int) {}
-void fft_conv2d_half::pointwise_for_delta_input(int, half*) {}
+// The reference's intermediate backward steps (kernel.cu:1153,1177,1189,1211,
+// 1314) fill padded FP16 planes that conv2d_backward consumes; here both
+// gradients come out of conv2d_backward's own plans, so the steps cannot run
+// on their own and report TCFFT_UNSUPPORTED.
+void fft_conv2d_half::fft_conv2d_rev_pad(double*, double*, half*, half*, int, int, int, int, int) {
+  last_status = TCFFT_UNSUPPORTED;
+}
+void fft_conv2d_half::inv_pad_deltain_signal(int) { last_status = TCFFT_UNSUPPORTED; }
+void fft_conv2d_half::pad_fx_1_circles_of_0(double*, int, int, int) { last_status = TCFFT_UNSUPPORTED; }
+void fft_conv2d_half::pointwise_for_delta_weight(int) { last_status = TCFFT_UNSUPPORTED; }
+void fft_conv2d_half::pointwise_for_delta_input(int, half*) { last_status = TCFFT_UNSUPPORTED; }
 
 void fft_conv2d_half::gen_rev(int Nx, int Ny) {
   const int r256[2] = {16, 16};
@@ -541,7 +576,7 @@ std::string fft_conv2d_half::toString() { return "fft_conv2d_half(tcfft_gb300)";
 // ----------------------------------------------------------------------------
 namespace {
 int full_conv_host(float* Signal, float* Kernels, int kernelCount, int nRows, int nCols, int kRows, int kCols,
-                   float* results) {
+                   float* results, bool qd_spectra) {
   tcfftConv c = nullptr;
   int st = tcfft_conv2d_plan(&c, 1, kernelCount, nRows, nCols, kRows, kCols, TCFFT_CONV_FULL, TCFFT_SPLIT_FP32, 1);
   if (st != TCFFT_OK) return st;
@@ -554,7 +589,7 @@ int full_conv_host(float* Signal, float* Kernels, int kernelCount, int nRows, in
   if (st == TCFFT_OK) {
     cudaMemcpy(dk, Kernels, sizeof(float) * nk, cudaMemcpyHostToDevice);
     cudaMemcpy(ds, Signal, sizeof(float) * ns, cudaMemcpyHostToDevice);
-    st = tcfft_conv2d_set_filters(c, dk, nullptr);
+    st = qd_spectra ? tcfft_conv2d_set_filters_qd(c, dk, nullptr) : tcfft_conv2d_set_filters(c, dk, nullptr);
     if (st == TCFFT_OK) st = tcfft_conv2d_exec(c, ds, dout, 1, nullptr);
     if (st == TCFFT_OK) st = tcfft_conv2d_check(c, nullptr);
     if (st == TCFFT_OK) cudaMemcpy(results, dout, sizeof(float) * no, cudaMemcpyDeviceToHost);
@@ -600,36 +635,78 @@ int packed_kernel_spectra(float* Kernels, int kernelCount, int fftRows, int fftC
 }
 }  // namespace
 
+// The reference's functions return void; each records its status, which
+// tcfft_get_last_error() (include/tcfft_gb300.h) reports.
 void convolve_direct_fft(float* Signal, float* Kernels, int kernelCount, int nRows, int nCols, int kRows, int kCols,
                          float* results) {
-  full_conv_host(Signal, Kernels, kernelCount, nRows, nCols, kRows, kCols, results);
+  tcfft::record_status(
+      static_cast<tcfftStatus>(full_conv_host(Signal, Kernels, kernelCount, nRows, nCols, kRows, kCols, results, false)),
+      0);
 }
 
 void convolve_turbo_fft_v2(float* Signal, float* Kernels, int kernelCount, int nRows, int nCols, int kRows, int kCols,
                            float* results) {
-  full_conv_host(Signal, Kernels, kernelCount, nRows, nCols, kRows, kCols, results);
+  tcfft::record_status(
+      static_cast<tcfftStatus>(full_conv_host(Signal, Kernels, kernelCount, nRows, nCols, kRows, kCols, results, false)),
+      0);
 }
 
+// turbo v3 = v2 with the filter spectra made by line projections
+// (fftconvolve2d.cu:1263-1500, qdVector_construct / fast_fft).
 void convolve_turbo_fft_v3(float* Signal, float* Kernels, int kernelCount, int nRows, int nCols, int kRows, int kCols,
                            float* results) {
-  full_conv_host(Signal, Kernels, kernelCount, nRows, nCols, kRows, kCols, results);
+  tcfft::record_status(
+      static_cast<tcfftStatus>(full_conv_host(Signal, Kernels, kernelCount, nRows, nCols, kRows, kCols, results, true)),
+      0);
 }
 
 void direct_fft(float* Kernels, int kernelCount, int nRows, int nCols, int kRows, int kCols, cufftComplex* results) {
-  packed_kernel_spectra(Kernels, kernelCount, nRows + kRows - 1, nCols + kCols - 1, kRows, kCols, results,
-                        TCFFT_INVERSE, false);
+  tcfft::record_status(static_cast<tcfftStatus>(packed_kernel_spectra(Kernels, kernelCount, nRows + kRows - 1,
+                                                                      nCols + kCols - 1, kRows, kCols, results,
+                                                                      TCFFT_INVERSE, false)),
+                       0);
 }
 
+// qd_fft (fftconvolve2d.cu:1603): the same spectra as direct_fft, made by line
+// projections of the packed kernel pairs (fast_fft with forward = false). The
+// projections need a square padded plane (fftRows == fftCols).
 void qd_fft(float* Kernels, int kernelCount, int nRows, int nCols, int kRows, int kCols, cufftComplex* results) {
-  packed_kernel_spectra(Kernels, kernelCount, nRows + kRows - 1, nCols + kCols - 1, kRows, kCols, results,
-                        TCFFT_INVERSE, false);
+  const int fr = nRows + kRows - 1, fc = nCols + kCols - 1, groups = kernelCount / 2;
+  tcfftStatus st = TCFFT_OK;
+  if (groups < 1 || fr != fc) st = TCFFT_INVALID_SIZE;
+  tcfftQdImpl* q = nullptr;
+  if (st == TCFFT_OK) st = tcfft::qd_create(&q, fc, groups, kRows, kCols);
+  const long long nk = 2ll * groups * kRows * kCols;
+  const size_t nout = static_cast<size_t>(groups) * fr * fc;
+  float* dk = st == TCFFT_OK ? dev_alloc<float>(static_cast<size_t>(nk)) : nullptr;
+  float2* dout = st == TCFFT_OK ? dev_alloc<float2>(nout) : nullptr;
+  if (st == TCFFT_OK && (!dk || !dout)) st = TCFFT_ALLOC_FAILED;
+  if (st == TCFFT_OK && cudaMemcpy(dk, Kernels, sizeof(float) * nk, cudaMemcpyHostToDevice) != cudaSuccess)
+    st = TCFFT_LAUNCH_FAILED;
+  if (st == TCFFT_OK) st = tcfft::qd_exec_pairs_packed(q, dk, 2ll * groups, dout, TCFFT_INVERSE, nullptr);
+  if (st == TCFFT_OK) st = tcfft::qd_check(q, nullptr);
+  if (st == TCFFT_OK && cudaMemcpy(results, dout, sizeof(float2) * nout, cudaMemcpyDeviceToHost) != cudaSuccess)
+    st = TCFFT_LAUNCH_FAILED;
+  cudaFree(dk);
+  cudaFree(dout);
+  tcfft::qd_free(q);
+  tcfft::record_status(st, 0);
 }
 
-void fast_fft(cufftComplex* d_kernels, int group_num, int fftCols, int fftRows, int, int, cufftComplex* d_results,
+// fast_fft (fftconvolve2d.cu:1011): device planes [group_num][fftRows][fftCols]
+// whose non-zeros lie in the top-left kCols x kCols box (the reference's
+// sparse projection reads exactly that box), 2D DFT by line projections into
+// d_results, forward (true) or inverse sign, unnormalised.
+void fast_fft(cufftComplex* d_kernels, int group_num, int fftCols, int fftRows, int kCols, int, cufftComplex* d_results,
               bool forward) {
-  tcfftPlan p = nullptr;
-  if (tcfft_plan_2d(&p, fftRows, fftCols, group_num, TCFFT_SPLIT_FP32) != TCFFT_OK) return;
-  tcfft_exec(p, d_kernels, d_results, forward ? TCFFT_FORWARD : TCFFT_INVERSE, 1.0f, nullptr);
-  tcfft_check(p, nullptr);
-  tcfft_destroy(p);
+  tcfftStatus st = TCFFT_OK;
+  if (group_num < 1 || fftRows != fftCols || !d_kernels || !d_results) st = TCFFT_INVALID_VALUE;
+  tcfftQdImpl* q = nullptr;
+  if (st == TCFFT_OK) st = tcfft::qd_create(&q, fftCols, group_num, kCols, kCols);
+  if (st == TCFFT_OK)
+    st = tcfft::qd_exec_planes(q, reinterpret_cast<const float2*>(d_kernels), reinterpret_cast<float2*>(d_results),
+                               forward ? TCFFT_FORWARD : TCFFT_INVERSE, nullptr);
+  if (st == TCFFT_OK) st = tcfft::qd_check(q, nullptr);
+  tcfft::qd_free(q);
+  tcfft::record_status(st, 0);
 }

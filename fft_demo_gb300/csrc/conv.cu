@@ -30,6 +30,7 @@
 
 #include "../../include/tcfft_gb300.h"
 #include "conv_kernels.cuh"
+#include "qd_internal.cuh"
 #include "tables.cuh"
 
 using namespace tcfft;
@@ -412,6 +413,29 @@ tcfftStatus tcfft_conv2d_set_filters(tcfftConv c, const float* filters, void* st
       s = conv_col<float2>(c, kConvColFwd, 0, static_cast<float2*>(c->X), static_cast<float2*>(c->K), count, c->fy,
                            0, c->P, 1.0f, st);
   }
+  if (s == TCFFT_OK) c->filters_set = true;
+  return cret(s);
+}
+
+tcfftStatus tcfft_conv2d_set_filters_qd(tcfftConv c, const float* filters, void* stream) {
+  if (!c || !filters) return cret(TCFFT_INVALID_VALUE);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int flip = c->mode == TCFFT_CONV_VALID_CORR ? 1 : 0;
+  const long long count = static_cast<long long>(c->F) * c->S;
+  tcfftQdImpl* q = nullptr;
+  tcfftStatus s = qd_create(&q, c->P, (count + 1) / 2, c->fy, c->fx);
+  if (s == TCFFT_OK) {
+    // same spectra as the masked passes: forward sign, unnormalised
+    if (c->precision == TCFFT_FP16)
+      s = qd_exec_filter_pairs<half2>(q, filters, count, flip, static_cast<half2*>(c->K), TCFFT_FORWARD, st);
+    else
+      s = qd_exec_filter_pairs<float2>(q, filters, count, flip, static_cast<float2*>(c->K), TCFFT_FORWARD, st);
+    // the projections are freed below: finish with them first (and report
+    // a flagged error of their transforms)
+    const tcfftStatus w = qd_check(q, st);
+    if (s == TCFFT_OK) s = w;
+  }
+  qd_free(q);
   if (s == TCFFT_OK) c->filters_set = true;
   return cret(s);
 }

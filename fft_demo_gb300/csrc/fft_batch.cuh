@@ -106,6 +106,7 @@ struct BatchArgs {
   OuterTwiddle otw[kBatchMaxLog + 1];      // W_n factor tables per log2 n
   const uint32_t* bmat;                    // DFT16 B image (hi, lo), this direction
   int* err;
+  unsigned int wait_polls;  // bound of each dependency wait (tcfft_set_wait_limit)
 };
 
 // Whole lines found through per-line offset tables (each line contiguous).
@@ -454,7 +455,7 @@ __global__ void __launch_bounds__(kPassThreads, SPLIT ? 2 : 3) fft_batch_kernel(
     const BatchItem it = a.items[i];
     if (threadIdx.x == 0) {
       bool ok = true;
-      if (it.wait_ctr >= 0) ok = wait_counter(a.ctrs + it.wait_ctr, it.wait_target);
+      if (it.wait_ctr >= 0) ok = wait_counter(a.ctrs + it.wait_ctr, it.wait_target, a.wait_polls);
       if (!ok) atomicOr(a.err, kErrQueueTimeout);
       s_ok = ok;
     }

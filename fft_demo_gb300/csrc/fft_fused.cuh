@@ -17,7 +17,13 @@
 // read of the input and one write of the output.
 //
 // In-place transforms are safe: chunk c's input is fully read by its P1
-// tiles before any P2(c) tile writes chunk c's output.
+// tiles before any P2(c) tile writes chunk c's output. Pass 1 reads the input
+// with non-coherent (ld.global.nc) loads even then: every address of `in` is
+// read only by the P1 tiles of its own chunk, all of which finish (and are
+// counted in done1) before the first P2 tile of that chunk writes it, and it
+// is never read again in the launch; chunks start on sequence boundaries
+// (multiples of 2^15 * 4 bytes), so no cache line holds two chunks. No load
+// can therefore see a line that was written during the launch.
 #pragma once
 #include "fft_io.cuh"
 #include "fft_tile.cuh"
@@ -34,6 +40,7 @@ struct FusedSched {
   int chunk_seqs;         // sequences per chunk
   long long batch;        // sequences in total
   long long n;            // points per sequence
+  unsigned int wait_polls;  // bound of each dependency wait (tcfft_set_wait_limit)
 };
 
 __device__ __forceinline__ int ld_acquire(const int* p) {
@@ -42,9 +49,10 @@ __device__ __forceinline__ int ld_acquire(const int* p) {
   return v;
 }
 
-// Spin (thread 0) until *p >= target; false if the bound was reached.
-__device__ __forceinline__ bool wait_counter(const int* p, int target) {
-  for (uint32_t i = 0; i < (1u << 24); ++i) {
+// Spin (thread 0) until *p >= target; false if max_polls polls passed
+// without it (max_polls = 0 gives up at once).
+__device__ __forceinline__ bool wait_counter(const int* p, int target, uint32_t max_polls) {
+  for (uint32_t i = 0; i < max_polls; ++i) {
     if (ld_acquire(p) >= target) return true;
     __nanosleep(i < 64 ? 32 : 256);
   }
@@ -96,8 +104,8 @@ __global__ void __launch_bounds__(kPassThreads, 2)
     // dependencies (thread 0 waits, the CTA follows)
     if (threadIdx.x == 0) {
       bool ok = true;
-      if (pass == 2) ok = wait_counter(sc.done1 + chunk, sc.tiles1);
-      else if (chunk >= sc.ring) ok = wait_counter(sc.done2 + (chunk - sc.ring), sc.tiles2);
+      if (pass == 2) ok = wait_counter(sc.done1 + chunk, sc.tiles1, sc.wait_polls);
+      else if (chunk >= sc.ring) ok = wait_counter(sc.done2 + (chunk - sc.ring), sc.tiles2, sc.wait_polls);
       if (!ok) atomicOr(core1.err, kErrQueueTimeout);
       s_ok = ok;
     }

@@ -268,6 +268,7 @@ tcfftStatus tcfft_queue_submit(tcfftQueue q, int count, const long long* n, cons
   if (cudaMemcpyAsync(sl.dev, sl.host, at, cudaMemcpyHostToDevice, st) != cudaSuccess)
     return record_status(TCFFT_LAUNCH_FAILED, 0);
   BatchArgs a = q->base;
+  a.wait_polls = dep_wait_polls();
   a.in = in;
   a.out = out;
   a.conv_in = conv_in;

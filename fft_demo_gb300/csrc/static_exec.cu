@@ -4,16 +4,28 @@
 // Scratch layout (kStaticScratchBytes = 17 MiB):
 //   [0, 16 MiB)            workspace ring: two slots of 8 MiB; a chunk is
 //                          2^23 / (4 n) sequences (one sequence at n = 2^21)
-//   [16 MiB, +64 KiB)      word 0: error bits; from byte 256: queue counter,
-//                          done1[nchunks], done2[nchunks] -- all of these must
-//                          be zero when the kernel starts, so every call clears
-//                          them on its stream before the launch
+//   [16 MiB, +64 KiB)      word 0: error bits (sticky: cleared at set-up and
+//                          by a call with wait != 0 after it reads them);
+//                          from byte 256: queue counter, done1[nchunks],
+//                          done2[nchunks] -- these must be zero when the
+//                          kernel starts, so every call clears them on its
+//                          stream before the launch
 //   [16 MiB + 64 KiB, ...) tables, written once per device at set-up: the DFT16
 //                          B images, W_L for L = 2^7 .. 2^11 and the outer
 //                          twiddle factors W_n for n = 2^15 .. 2^21, both signs
 // Every call on a device shares this array: calls whose executions overlap
 // on the GPU (different streams, or host threads without ordering between
 // them) race on the ring and the counters. Calls on one stream are ordered.
+//
+// Set-up (first call on each device, with that device current): the CUDA
+// runtime loads this library's device code onto the device when it is first
+// needed (lazy module loading, the default), which is when the array gets its
+// device memory; cudaGetSymbolAddress triggers that, then the table kernels
+// run on the caller's stream and that stream is synchronised. So the first
+// call is not allocation-free at the driver level and waits for the caller's
+// stream once; it must not be made while the stream is being captured into a
+// CUDA graph (it returns TCFFT_UNSUPPORTED then, and set-up runs on a later
+// call). A failed set-up is retried by the next call.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -84,48 +96,48 @@ constexpr int split_log_n1(int logn) {
 
 constexpr int kMaxDevices = 64;
 struct DeviceScratch {
-  std::once_flag once;
+  std::mutex mu;
+  bool done = false;  // set only after a successful set-up
   unsigned char* base = nullptr;
-  tcfftStatus status = TCFFT_OK;
 };
 DeviceScratch g_dev[kMaxDevices];
 
-// Once per device, with that device current: find the array's device address
-// and write the tables.
-void set_up(DeviceScratch& d) {
+// With the device current and d.mu held: find the array's device address
+// (which loads the module onto the device if it is not yet loaded), write the
+// tables and clear the error word on the caller's stream, and wait for that
+// stream. Returns the status; d.done stays false on failure so that the next
+// call tries again.
+tcfftStatus set_up(DeviceScratch& d, cudaStream_t st) {
   tcfftStatus s = registry_ready();
-  if (s != TCFFT_OK) {
-    d.status = s;
-    return;
-  }
+  if (s != TCFFT_OK) return s;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) return TCFFT_LAUNCH_FAILED;
+  if (cs != cudaStreamCaptureStatusNone) return TCFFT_UNSUPPORTED;  // cannot wait inside a capture
   unsigned char* ptr = nullptr;
-  if (cudaGetSymbolAddress(reinterpret_cast<void**>(&ptr), g_static_scratch) != cudaSuccess || !ptr) {
-    d.status = TCFFT_LAUNCH_FAILED;
-    return;
-  }
+  if (cudaGetSymbolAddress(reinterpret_cast<void**>(&ptr), g_static_scratch) != cudaSuccess || !ptr)
+    return TCFFT_LAUNCH_FAILED;
   const TableLayout t = table_layout();
   unsigned char* tab = ptr + kRingBytes + kCtrBytes;
-  cudaError_t e = cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(ptr + kRingBytes, 0, sizeof(int), st);
   for (int sg = 0; sg < 2 && e == cudaSuccess; ++sg) {
     const int sign = sg == 0 ? -1 : 1;
     uint16_t* bm = reinterpret_cast<uint16_t*>(tab + t.bmat[sg]);
-    e = gen_dft16_bmat(bm, sign, 0, 0);
-    if (e == cudaSuccess) e = gen_dft16_bmat(bm + 1024, sign, 1, 0);
+    e = gen_dft16_bmat(bm, sign, 0, st);
+    if (e == cudaSuccess) e = gen_dft16_bmat(bm + 1024, sign, 1, st);
     for (int l = kStaticMinPass; l <= kStaticMaxPass && e == cudaSuccess; ++l)
-      e = gen_twiddles(reinterpret_cast<float2*>(tab + t.tw[sg][l]), 1ll << l, l, 0, sign, 0);
+      e = gen_twiddles(reinterpret_cast<float2*>(tab + t.tw[sg][l]), 1ll << l, l, 0, sign, st);
     for (int l = kStaticMinLog; l <= kStaticMaxLog && e == cudaSuccess; ++l) {
       const int sh = outer_shift(l);
-      e = gen_twiddles(reinterpret_cast<float2*>(tab + t.otw_lo[sg][l]), 1ll << sh, l, 0, sign, 0);
+      e = gen_twiddles(reinterpret_cast<float2*>(tab + t.otw_lo[sg][l]), 1ll << sh, l, 0, sign, st);
       if (e == cudaSuccess)
-        e = gen_twiddles(reinterpret_cast<float2*>(tab + t.otw_hi[sg][l]), 1ll << (l - sh), l, sh, sign, 0);
+        e = gen_twiddles(reinterpret_cast<float2*>(tab + t.otw_hi[sg][l]), 1ll << (l - sh), l, sh, sign, st);
     }
   }
-  if (e == cudaSuccess) e = cudaDeviceSynchronize();
-  if (e != cudaSuccess) {
-    d.status = TCFFT_LAUNCH_FAILED;
-    return;
-  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return TCFFT_LAUNCH_FAILED;
   d.base = ptr;
+  d.done = true;
+  return TCFFT_OK;
 }
 
 static_assert(kStaticMaxLog - split_log_n1(kStaticMaxLog) <= kStaticMaxPass, "pass table range");
@@ -154,8 +166,14 @@ extern "C" tcfftStatus tcfft_exec_static(const void* in, void* out, long long n,
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return record_status(TCFFT_NO_DEVICE, 0);
   DeviceScratch& d = g_dev[dev];
-  std::call_once(d.once, [&d] { set_up(d); });
-  if (!d.base) return record_status(d.status != TCFFT_OK ? d.status : TCFFT_LAUNCH_FAILED, 0);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  {
+    std::lock_guard<std::mutex> lock(d.mu);
+    if (!d.done) {
+      const tcfftStatus s = set_up(d, st);
+      if (s != TCFFT_OK) return record_status(s, 0);
+    }
+  }
 
   const int sg = direction == TCFFT_FORWARD ? 0 : 1;
   int grid_ctas = 0;
@@ -210,11 +228,11 @@ extern "C" tcfftStatus tcfft_exec_static(const void* in, void* out, long long n,
   sc.chunk_seqs = static_cast<int>(chunk_seqs);
   sc.batch = batch;
   sc.n = n;
+  sc.wait_polls = dep_wait_polls();
 
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  // error word, queue counter and done counters start at zero
-  if (cudaMemsetAsync(d.base + kRingBytes, 0, kCtrStart + sizeof(int) * (1 + 2 * static_cast<size_t>(nchunks)), st) !=
-      cudaSuccess)
+  // queue counter and done counters start at zero; the error word keeps any
+  // bit an earlier call with wait == 0 left, for the next call that waits
+  if (cudaMemsetAsync(ctr, 0, sizeof(int) * (1 + 2 * static_cast<size_t>(nchunks)), st) != cudaSuccess)
     return record_status(TCFFT_LAUNCH_FAILED, 0);
   const long long items = nchunks * (sc.tiles1 + sc.tiles2);
   long long grid = grid_ctas > 0 ? grid_ctas : 1;
@@ -224,10 +242,12 @@ extern "C" tcfftStatus tcfft_exec_static(const void* in, void* out, long long n,
                        static_cast<size_t>(fk->smem), st) != cudaSuccess)
     return record_status(TCFFT_LAUNCH_FAILED, 0);
   if (!wait) return record_status(TCFFT_OK, 1);
+  // this call's error bits and any left by earlier calls with wait == 0
   int flag = 0;
   if (cudaMemcpyAsync(&flag, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return record_status(TCFFT_LAUNCH_FAILED, 1);
+  if (flag && cudaMemsetAsync(err, 0, sizeof(int), st) != cudaSuccess) return record_status(TCFFT_LAUNCH_FAILED, 1);
   if (flag & (kErrMmaTimeout | kErrQueueTimeout)) return record_status(TCFFT_TIMEOUT, 1);
   if (flag) return record_status(TCFFT_INVALID_VALUE, 1);
   return record_status(TCFFT_OK, 1);

@@ -18,11 +18,11 @@ i+1 while the GPU runs batch i.
 Latency = completion (a CUDA event after the batch's output copy, on a
 clock aligned with the host's) minus arrival; reported as p50 / p99 with
 req/s, GFLOP/s (5 N log2 N per 1D FFT; 5 P^2 log2 P^2 per 2D transform, two
-per convolution plus the pointwise product) and per-request relative-L2
-error against the FP64 oracle for a sample of requests, per precision and
-kind. FP16 convolution errors run higher than FP16 FFT errors for these
-filters: the spectra are rounded relative to |image| * |filter|, while the
-output of a zero-mean filter is much smaller than that.
+per convolution plus the pointwise product) and, for a sample of requests,
+the error against FP64 references (numpy / scipy): relative L2 for 1D FFTs,
+and for convolutions the error relative to ||image||_2 ||filter||_1
+(conv_scaled_err), the scale FP16 spectra are rounded at; the output of a
+zero-mean filter is much smaller than that scale.
 """
 import argparse
 import collections
@@ -284,10 +284,21 @@ def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, s
             "t_end": t_end}
 
 
+def conv_scaled_err(y, ref, img, w):
+    """||y - ref||_2 / (||img||_2 ||w||_1): the error of one convolution
+    against the scale of its inputs. FP16 convolutions round the image and
+    filter spectra (entries bounded by ||img||_1 and ||w||_1), so their output
+    error is bounded relative to this scale, while the output itself can be
+    much smaller (zero-mean filters cancel); the plain relative L2 would
+    measure that cancellation, not the transform."""
+    return float(np.linalg.norm(y - ref) / (np.linalg.norm(img) * np.abs(w).sum()))
+
+
 def errors(res, max_samples=60):
-    """Relative L2 vs the FP64 oracle for sampled requests, per precision."""
-    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle"))
-    import pyoracle as orc
+    """Errors of sampled requests against FP64 references computed with
+    numpy / scipy (complex128 FFT, float64 FFT convolution): relative L2 for
+    1D FFTs, conv_scaled_err for convolutions; per precision and kind."""
+    from scipy import signal
     wl, filters, lanes = res["wl"], res["filters"], res["lanes"]
     out = {(p, kind): [] for p in (tc.FP16, tc.SPLIT_FP32) for kind in ("fft", "conv")}
     for i, y in res["samples"][:max_samples]:
@@ -297,22 +308,25 @@ def errors(res, max_samples=60):
         if wl["conv"][i]:
             s = int(wl["side"][i])
             img = lane.pool[("img", s, j)][1].astype(np.float64)
-            ref = orc.conv2d_same(img, filters[wl["fid"][i]].astype(np.float64))
-            out[(p, "conv")].append(orc.rel_l2(y[:s * s].reshape(s, s), ref))
+            w = filters[wl["fid"][i]].astype(np.float64)
+            ref = signal.fftconvolve(img, w, mode="same")
+            out[(p, "conv")].append(conv_scaled_err(y[:s * s].reshape(s, s), ref, img, w))
         else:
             kk = int(wl["k"][i])
             x = lane.pool[("fft", kk, j)][1].astype(np.float64)
-            ref = orc.fft1d(x[:, 0] + 1j * x[:, 1])
+            ref = np.fft.fft(x[:, 0] + 1j * x[:, 1])
             n = 1 << kk
             yy = y[:2 * n].reshape(n, 2)
-            out[(p, "fft")].append(orc.rel_l2(yy[:, 0] + 1j * yy[:, 1], ref))
+            got = yy[:, 0] + 1j * yy[:, 1]
+            out[(p, "fft")].append(float(np.linalg.norm(got - ref) / np.linalg.norm(ref)))
     return out
 
 
 def summarize(res, errs):
     lat = res["lat"]
     ok = lat[~np.isnan(lat)]
-    worst = {"rel_l2_%s_%s_max" % ("fp16" if p == tc.FP16 else "split", kind): (float(max(v)) if v else None)
+    worst = {"%s_%s_%s_max" % ("rel_l2" if kind == "fft" else "scaled_err", "fp16" if p == tc.FP16 else "split",
+                                kind): (float(max(v)) if v else None)
              for (p, kind), v in errs.items()}
     return {
         **worst,

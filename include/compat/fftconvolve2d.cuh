@@ -7,19 +7,26 @@
 //       (fftconvolve2d.cu:184, :626, :1263): results[k][nRows+kRows-1]
 //       [nCols+kCols-1] = full linear convolution of Signal [nRows][nCols]
 //       with kernel k of Kernels [kernelCount][kRows][kCols] (the reference's
-//       1/fftSize cancels its unnormalised C2R inverse). The three reference
-//       variants differ only in how cuFFT is driven; here they share one path.
-//   direct_fft / qd_fft (fftconvolve2d.cu:1510, :1603): spectra of kernel
-//       pairs packed as (re = kernel 2g, im = kernel 2g+1), zero-padded to
+//       1/fftSize cancels its unnormalised C2R inverse). v3 makes its filter
+//       spectra by line projections (qdFFT), like the reference; the others
+//       by the masked row/column passes.
+//   direct_fft (fftconvolve2d.cu:1510): spectra of kernel pairs packed as
+//       (re = kernel 2g, im = kernel 2g+1), zero-padded to
 //       (nRows+kRows-1) x (nCols+kCols-1), unnormalised inverse-sign 2D DFT;
-//       results [kernelCount/2][fftRows][fftCols] (host). qd_fft's line
-//       projections compute the same DFT, so both return it directly.
-//   fast_fft (fftconvolve2d.cu:1011): device arrays; 2D DFT of each of
-//       group_num fftRows x fftCols complex planes, forward or inverse sign.
-// Limits: padded extents must be powers of two (<= 2048 x 8192); the
-// reference's own call sites (main.cpp:312, main_2d.cpp:199) use 256 x 256.
-// Unlike the reference there is no requirement that kernelCount be a
-// multiple of 16.
+//       results [kernelCount/2][fftRows][fftCols] (host).
+//   qd_fft (fftconvolve2d.cu:1603): the same spectra by line projections:
+//       3n/2 projections of the kRows x kCols box, a 1D DFT of each, gathered
+//       into the 2D spectrum (fftRows == fftCols == n required).
+//   fast_fft (fftconvolve2d.cu:1011): device arrays; 2D DFT by line
+//       projections of each of group_num n x n complex planes whose non-zeros
+//       lie in the top-left kCols x kCols box (the box the reference's sparse
+//       projection reads), forward or inverse sign, unnormalised.
+// The reference's functions return void and check nothing; here each records
+// its status for tcfft_get_last_error() (include/tcfft_gb300.h).
+// Limits: padded extents must be powers of two (<= 2048 x 8192; <= 4096 for
+// the projection route); the reference's own call sites (main.cpp:312,
+// main_2d.cpp:199) use 256 x 256. Unlike the reference there is no
+// requirement that kernelCount be a multiple of 16.
 #ifndef FFTCONVOLVE2D_CUH
 #define FFTCONVOLVE2D_CUH
 #include <cufft.h>

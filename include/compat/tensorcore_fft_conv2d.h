@@ -139,9 +139,13 @@ public:
     double *cu_conv2d_forward_result_padded;
 
     // The reference's internal forward steps. The whole pipeline runs in
-    // conv2d_forward here; these entry points run it too (fft_conv2d_inv_rev_pad
-    // and fft_pointwise/fft_conv_final_stage/readout_fwd are no-ops that keep
-    // the names available; TENSORCORE_FFT_CONV_2D computes into `output`).
+    // conv2d_forward here. TENSORCORE_FFT_CONV_2D computes into `output`;
+    // fft_conv2d_inv_rev_pad rebuilds the plan and its filter spectra from
+    // `filter`; readout_fwd has nothing left to do after a successful
+    // TENSORCORE_FFT_CONV_2D (last_status stays TCFFT_OK) and reports
+    // TCFFT_UNSUPPORTED otherwise. fft_pointwise and fft_conv_final_stage
+    // cannot run on their own (the planes they would fill live inside the
+    // plan): they set last_status = TCFFT_UNSUPPORTED.
     void fft_conv2d_inv_rev_pad();
     void conv2d_forward(double *output);
     void TENSORCORE_FFT_CONV_2D();
@@ -171,8 +175,9 @@ public:
     double *delta_for_filter;
     double *delta_for_signal;
 
-    // Internal backward steps of the reference: kept as names (no-ops);
-    // conv2d_backward computes both gradients.
+    // Internal backward steps of the reference: kept as names so code that
+    // names them compiles; conv2d_backward computes both gradients, and these
+    // set last_status = TCFFT_UNSUPPORTED when called on their own.
     void fft_conv2d_rev_pad(double *siganl, double *filter, half *signal_padded, half *filter_padded, int padded_x,
                             int sx, int fx, int S, int F);
     void inv_pad_deltain_signal(int padded_x);

@@ -103,16 +103,24 @@ tcfftStatus tcfft_destroy(tcfftPlan plan);
  * without any device allocation, for callers that cannot allocate: the
  * fused four-step kernel of tcfft_exec runs with its workspace ring,
  * counters, error word and tables in one file-scope device array of 17 MiB
- * (fixed at load time; the tables are written on the first call on each
- * device). out = scale * FFT_direction(in), in == out allowed, 16-byte
+ * (see "First call" below). out = scale * FFT_direction(in), in == out allowed, 16-byte
  * aligned device buffers of n * batch interleaved complex halves.
  * Limits: n = 2^k with 2^15 <= n <= 2^21 (TCFFT_INVALID_SIZE below the
  * range or for other n, TCFFT_CAPACITY above it) and
  * ceil(batch / (2^21 / n)) <= 8159 (TCFFT_CAPACITY beyond that).
  * Every call on a device shares the array, so calls that overlap on the GPU
  * (other streams, unordered host threads) race; calls on one stream do not.
- * wait != 0: synchronise `stream` and report a flagged kernel error
- * (TCFFT_TIMEOUT); wait == 0: asynchronous, errors unreported. */
+ * wait != 0: synchronise `stream` and report a kernel error flagged by this
+ * call or by earlier calls made with wait == 0 (TCFFT_TIMEOUT), then clear
+ * it; wait == 0: asynchronous, a flagged error stays recorded for the next
+ * call that waits.
+ * First call on each device: it sets the array up -- the CUDA runtime loads
+ * the library's device code onto the device (lazy module loading, the
+ * default; CUDA_MODULE_LOADING=EAGER does it at context creation instead),
+ * which gives the array its device memory, then the tables are written on
+ * `stream` and `stream` is synchronised once. Make that first call before
+ * any stream capture and outside latency-critical code; during a capture it
+ * returns TCFFT_UNSUPPORTED. A failed set-up is retried by the next call. */
 tcfftStatus tcfft_exec_static(const void *in, void *out, long long n, long long batch, int direction,
                               float scale, void *stream, int wait);
 
@@ -152,11 +160,35 @@ tcfftStatus tcfft_conv2d_plan(tcfftConv *conv, int S, int F, int sy, int sx, int
 tcfftStatus tcfft_conv2d_set_filters(tcfftConv conv, const float *filters, void *stream);
 /* out = conv(images) for `batch` <= max_batch images (device buffers). */
 tcfftStatus tcfft_conv2d_exec(tcfftConv conv, const void *images, void *out, long long batch, void *stream);
+/* Same contract as tcfft_conv2d_set_filters, with the filter spectra made by
+ * line projections (tcfft_qd_* below) instead of the masked row and column
+ * passes: the route convolve_turbo_fft_v3 (fftconvolve2d.cu:1263) takes to
+ * its filter spectra. Results agree with tcfft_conv2d_set_filters to the
+ * plan's precision. */
+tcfftStatus tcfft_conv2d_set_filters_qd(tcfftConv conv, const float *filters, void *stream);
 /* Output window and padded transform size of the plan. */
 tcfftStatus tcfft_conv2d_shape(tcfftConv conv, int *out_rows, int *out_cols, int *padded);
 /* Synchronise `stream`, report a flagged device error. */
 tcfftStatus tcfft_conv2d_check(tcfftConv conv, void *stream);
 tcfftStatus tcfft_conv2d_destroy(tcfftConv conv);
+
+/* ------------------------------------------------------------------------
+ * Line-projection 2D DFT ("qdFFT"; replaces fast_fft's projection, batched
+ * 1D FFT and scatter, fftconvolve2d.cu:884,1011, fft_utils.cu:161-700).
+ * Input: `planes` complex float planes [planes][n][n] (device) whose
+ * non-zeros lie in the top-left box_rows x box_cols box (only the box is
+ * read). Output: their unnormalised 2D DFTs (direction), [planes][n][n]
+ * complex float, out != planes. For each of the 3n/2 directions (1, s),
+ * (2q, 1) the box is projected onto lines p x + s y = t (mod n); a 1D DFT of
+ * each projection gives the spectrum along one line through the origin.
+ * 16 <= n <= 4096, n a power of two; FP32 data, split-precision transforms.
+ * ------------------------------------------------------------------------ */
+typedef struct tcfftQdImpl *tcfftQd;
+tcfftStatus tcfft_qd_plan(tcfftQd *qd, int n, long long planes, int box_rows, int box_cols);
+tcfftStatus tcfft_qd_exec(tcfftQd qd, const void *planes, void *out, int direction, void *stream);
+/* Synchronise `stream`, report a flagged device error of the transforms. */
+tcfftStatus tcfft_qd_check(tcfftQd qd, void *stream);
+tcfftStatus tcfft_qd_destroy(tcfftQd qd);
 
 /* ------------------------------------------------------------------------
  * Uneven batches: many 1D transforms of different power-of-two sizes
@@ -226,6 +258,18 @@ tcfftStatus tcfft_queue_submit(tcfftQueue queue, int count, const long long *n, 
                                void *conv_out, void *stream);
 tcfftStatus tcfft_queue_check(tcfftQueue queue, void *stream);
 tcfftStatus tcfft_queue_destroy(tcfftQueue queue);
+
+/* Bound of the dependency waits inside the persistent kernels (the fused
+ * four-step launch, tcfft_exec_static, the uneven-batch and serving
+ * kernels): a work item waits at most `polls` polls for the items it depends
+ * on, then gives up, skips its work and flags TCFFT_TIMEOUT, which the
+ * plan's check call reports. Applies to launches made after the call (a CUDA
+ * graph captured earlier keeps its bound). polls < 0 restores the default,
+ * 2^24 (seconds); 0 makes every such wait give up at once, a deterministic
+ * way to exercise the timeout path. Waits on the tensor cores and on copies
+ * keep their own bound. No counterpart in the reference, whose kernels never
+ * wait on one another. */
+tcfftStatus tcfft_set_wait_limit(long long polls);
 
 /* Last status returned on this thread, and a readable name for a status. */
 tcfftStatus tcfft_get_last_error(void);

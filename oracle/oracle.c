@@ -284,3 +284,40 @@ double orc_max_abs(const double *tested, const double *standard, long count) {
   }
   return m;
 }
+
+/* Line-projection 2D DFT of n x n complex planes whose non-zeros lie in the
+ * top-left box_rows x box_cols box, as the reference computes filter spectra
+ * in fast_fft (fftconvolve2d.cu:1011-1260; find_input_index :155,
+ * qdVector_construct :884, scatter qdVectorReconstruct fft_utils.cu:587):
+ * directions (p, s) = (1, i) for i < n and (2(i - n), 1) for n <= i < 3n/2;
+ * projection v[t] = sum of the box entries with p x + s y = t (mod n); its
+ * 1D DFT (sign) is written to frequency (t p mod n, t s mod n), in the
+ * reference's order (direction-major, later lines overwrite earlier ones). */
+void orc_qd_fft2d(const double *planes, double *out, int n, long count, int box_rows, int box_cols, int sign) {
+  const int ndir = n + n / 2;
+  double *v = (double *)malloc(sizeof(double) * 2 * (size_t)n);
+  double *w = (double *)malloc(sizeof(double) * 2 * (size_t)n);
+  for (long g = 0; g < count; ++g) {
+    const double *pl = planes + (size_t)g * 2 * n * n;
+    double *o = out + (size_t)g * 2 * n * n;
+    for (int i = 0; i < ndir; ++i) {
+      const long p = i < n ? 1 : 2L * (i - n), s = i < n ? i : 1;
+      for (int t = 0; t < 2 * n; ++t) v[t] = 0.0;
+      for (int x = 0; x < box_rows; ++x)
+        for (int y = 0; y < box_cols; ++y) {
+          const long t = (p * x + s * y) % n;
+          v[2 * t] += pl[2 * ((size_t)x * n + y)];
+          v[2 * t + 1] += pl[2 * ((size_t)x * n + y) + 1];
+        }
+      for (int t = 0; t < 2 * n; ++t) w[t] = v[t];
+      orc_fft1d(w, n, 1, sign, 1);
+      for (int t = 0; t < n; ++t) {
+        const long u = (t * p) % n, vv = (t * s) % n;
+        o[2 * (u * n + vv)] = w[2 * t];
+        o[2 * (u * n + vv) + 1] = w[2 * t + 1];
+      }
+    }
+  }
+  free(v);
+  free(w);
+}

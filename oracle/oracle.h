@@ -24,6 +24,8 @@
  *                            kernelCount filters (convolve_direct_fft,
  *                            fftconvolve2d.cu:184: its 1/fftSize
  *                            cancels the unnormalised C2R inverse).
+ *   orc_qd_fft2d           - fast_fft's line-projection 2D DFT of box-limited
+ *                            planes (fftconvolve2d.cu:1011, :884, :155).
  *   orc_clipped_error      - get_error (main.cpp:118).
  *
  * Parity pins: the FFT against the direct DFT and known-answer vectors; the
@@ -64,6 +66,10 @@ void orc_conv2d_full(const double *img, const double *kern, double *out, int kc,
                      int ky, int kx, int nthreads);
 
 /* Mean over all components of min(1, |t - s| / |s|). */
+/* Line-projection ("qdFFT") 2D DFT of box-limited planes (fast_fft,
+ * fftconvolve2d.cu:1011): interleaved complex [count][n][n] in and out. */
+void orc_qd_fft2d(const double *planes, double *out, int n, long count, int box_rows, int box_cols, int sign);
+
 double orc_clipped_error(const double *tested, const double *standard, long count);
 /* ||t - s||_2 / ||s||_2 and max |t - s| over count doubles. */
 double orc_rel_l2(const double *tested, const double *standard, long count);

@@ -37,6 +37,7 @@ def lib():
             "orc_corr2d_valid": (None, [p, p, p, i, i, i, i, i, i, i]),
             "orc_conv2d_same": (None, [p, p, p, i, i, i, i, i, i]),
             "orc_conv2d_full": (None, [p, p, p, i, i, i, i, i, i]),
+            "orc_qd_fft2d": (None, [p, p, i, l, i, i, i]),
             "orc_clipped_error": (d, [p, p, l]),
             "orc_rel_l2": (d, [p, p, l]),
             "orc_max_abs": (d, [p, p, l]),
@@ -98,6 +99,18 @@ def fft2d(x, sign=-1, nthreads=0):
     buf = to_interleaved(x.reshape(batch, nx, ny)).copy()
     lib().orc_fft2d(_p(buf), nx, ny, batch, sign, nthreads)
     return to_complex(buf).reshape(x.shape)
+
+
+def qd_fft2d(planes, box_rows, box_cols, sign=-1):
+    """Line-projection 2D DFT (fast_fft, fftconvolve2d.cu:1011) of complex
+    planes [..., n, n] whose non-zeros lie in the top-left box."""
+    x = np.asarray(planes)
+    n = x.shape[-1]
+    count = int(np.prod(x.shape[:-2])) if x.ndim > 2 else 1
+    src = to_interleaved(x.reshape(count, n, n)).copy()
+    dst = np.zeros_like(src)
+    lib().orc_qd_fft2d(_p(src), _p(dst), n, count, box_rows, box_cols, sign)
+    return to_complex(dst).reshape(x.shape)
 
 
 def gen_rev(n, radices):
@@ -166,6 +179,33 @@ def max_abs(tested, standard):
         t, s = to_interleaved(t), to_interleaved(s)
     t, s = _as_f64(t).ravel(), _as_f64(s).ravel()
     return lib().orc_max_abs(_p(t), _p(s), t.size)
+
+
+def conv_scaled_err(out, ref, images, filters):
+    """Convolution error measured against the scale of its inputs:
+    ||out - ref||_2 / sqrt(sum_o b_o^2), b_o = sum_s ||x_s||_2 * ||w_os||_1,
+    over output planes o = (image b, filter f). out, ref: [B][F][...];
+    images: [B][S][sy][sx]; filters: [F][S][fy][fx].
+
+    Why this norm: an FFT convolution in FP16 rounds the image spectrum
+    (entries bounded by ||x||_1, energy P^2 ||x||_2^2) and the filter
+    spectrum (entries bounded by ||w||_1); the output error is their
+    product's roundoff pushed through the inverse transform, so
+    ||e||_2 <~ c u ||x||_2 ||w||_1 with u = 2^-11 and c a small constant from
+    the log2(P^2) stages. The plain relative L2 divides by ||out||, which for a
+    zero-mean filter (N(0,1) entries scaled to unit L1) is much smaller than
+    ||x||_2 ||w||_1, so it measures the filter's cancellation, not the
+    transform."""
+    out = _as_f64(out)
+    ref = _as_f64(ref)
+    x = _as_f64(images)
+    w = _as_f64(filters)
+    B, S = x.shape[:2]
+    F = w.shape[0]
+    xn = np.sqrt((x.reshape(B, S, -1) ** 2).sum(-1))        # [B][S]
+    wn = np.abs(w.reshape(F, S, -1)).sum(-1)                  # [F][S]
+    b = xn @ wn.T                                             # [B][F]
+    return float(np.linalg.norm((out - ref).ravel()) / np.sqrt((b ** 2).sum()))
 
 
 def max_threads():

@@ -1,5 +1,5 @@
-"""Run the reference's own tcFFT kernels (cubins compiled from its source by
-oracle/ref_build.sh) through the CUDA driver API.
+"""Run the reference's own tcFFT and FFT-convolution kernels (cubins compiled
+from its source by oracle/ref_build.sh) through the CUDA driver API.
 
 TEST INFRASTRUCTURE ONLY: used to make parity fixtures (the reference's own
 output on seeded inputs) and by the GPU parity tests when the cubins are
@@ -14,7 +14,13 @@ What is restated here, from yuelingfan/fft_demo:
   - tcfftExec_2d (tcfft_half_2d.cu:1128-1149): row pass with RADIX = Ny, then
     layer_1[m1] with step = Ny, RADIX = Nx;
   - the input permutation setup()/setup_2d() apply (gen_rev), taken from the
-    committed fixture tests/golden/reference_perm.npz.
+    committed fixture tests/golden/reference_perm.npz;
+  - fft_conv2d_half's forward convolution (tensorcore_fft_conv2d.cpp:12-58
+    constructor, :250-289 TENSORCORE_FFT_CONV_2D / readout_fwd;
+    tensorcore_fft_conv2d_kernel.cu:1101-1150 fft_pointwise and
+    fft_conv_final_stage, :1255-1275 fft_conv2d_inv_rev_pad, :1399
+    read_out_scale_double2double, :1495-1525 TensorCoreFFTExec) with its
+    _A100 kernel wiring (:1565-1571), in run_conv_valid.
 """
 import ctypes
 import os
@@ -138,3 +144,109 @@ def run_2d(x_perm_h2, nx, ny, batch, mergings, variant="A100"):
     d.launch(fn, (ny // cont1, nx * ny * batch // ny // nx), (32, 8), nx * 4 * cont1, [st, p_data, p_fr, p_fi])
     torch.cuda.synchronize()
     return data.cpu().numpy()
+
+
+# ---------------------------------------------------------------------------
+# fft_conv2d_half::conv2d_forward (valid cross-correlation), reference kernels
+# ---------------------------------------------------------------------------
+CONV_CUBIN = "ref_conv.cubin"
+_CONV_K = {
+    "inv": "_Z25fft_conv2d_inverse_filterPdii",
+    "inv_odd": "_Z29fft_conv2d_inverse_filter_oddPdii",
+    "pad": "_Z46fft_conv2d_bit_rev_real_pad_to_cpx_double2halfPdP6__halfPiS2_iiii",
+    "mul_add": "_Z26fft_cpx_point_wise_mul_addP6__halfS0_Pfiiii",
+    "q1": "_Z27fft_cpx_point_wise_quant_p1PfS_ii",
+    "q2": "_Z27fft_cpx_point_wise_quant_p2PfS_ii",
+    "q3": "_Z27fft_cpx_point_wise_quant_p3PfP6__halfS_PiS2_ii",
+    "deq": "_Z26fft_cpx_point_wise_dequantP6__halfPdPfii",
+    "read": "_Z35read_out_scale_double2double_kernelPdS_iiiiid",
+}
+
+
+def conv_available():
+    return os.path.exists(os.path.join(REF_DIR, CONV_CUBIN))
+
+
+def _conv_stage(base, m, with_step):
+    cont = N_CONT[m]
+    name = base + "_A100"
+    args = "iP7__half2P6__halfS3_i" if with_step else "P7__half2P6__halfS3_i"
+    return "_Z%d%sILi%dELi8EEv%s" % (len(name), name, cont, args)
+
+
+def _tc_exec_2d(d, cubin, data, P, batch, fft):
+    """TensorCoreFFTExec (kernel.cu:1526-1555) of a P x P plan, fft = +-1."""
+    import torch
+    m = {256: 0, 512: 1}[P]
+    fr, fi = dft16_tables(sign=-1 if fft == 1 else 1)
+    f_re = torch.from_numpy(fr.ravel().copy()).cuda()
+    f_im = torch.from_numpy(fi.ravel().copy()).cuda()
+    p_data = ctypes.c_void_p(data.data_ptr())
+    p_fr, p_fi = ctypes.c_void_p(f_re.data_ptr()), ctypes.c_void_p(f_im.data_ptr())
+    cont = N_CONT[m]
+    fn = d.function(cubin, _conv_stage(L0[m], m, False))
+    d.launch(fn, (P * P * batch // cont // P, 1), (32, 8), P * 4 * cont, [p_data, p_fr, p_fi, ctypes.c_int(fft)])
+    fn = d.function(cubin, _conv_stage(L1[m], m, True))
+    d.launch(fn, (P // cont, P * P * batch // P // P), (32, 8), P * 4 * cont,
+             [ctypes.c_int(P), p_data, p_fr, p_fi, ctypes.c_int(fft)])
+    torch.cuda.synchronize()
+
+
+def run_conv_valid(signal, filters, rev_tables):
+    """The reference's fft_conv2d_half(signal, filter, S, F, sy, sx, fy, fx,
+    __AMPERE__) followed by conv2d_forward(output).
+    signal [S][sy][sx], filters [F][S][fy][fx] (float64); rev_tables: {256:
+    rev_256, 512: rev_512} (the header's tables, tests/golden/
+    reference_perm.npz). Returns output [F][sy-fy+1][sx-fx+1] (float64).
+    One deviation, for determinism: the FP32 pointwise buffer is zeroed before
+    fft_cpx_point_wise_mul_add accumulates into it (the reference accumulates
+    into a fresh cudaMalloc, kernel.cu:1107)."""
+    import torch
+    d = driver()
+    cubin = os.path.join(REF_DIR, CONV_CUBIN)
+    S, sy, sx = signal.shape
+    F, S2, fy, fx = filters.shape
+    assert S == S2
+    P = 256 if sx + fx - 1 <= 256 else 512
+    oy, ox = sy - fy + 1, sx - fx + 1
+    dev = torch.device("cuda")
+    cu_signal = torch.from_numpy(np.ascontiguousarray(signal, dtype=np.float64)).to(dev)
+    cu_filter = torch.from_numpy(np.ascontiguousarray(filters, dtype=np.float64)).to(dev)
+    sig_pad = torch.zeros(S * P * P * 2, dtype=torch.float16, device=dev)
+    filt_pad = torch.zeros(F * S * P * P * 2, dtype=torch.float16, device=dev)
+    rev = torch.zeros(1024, dtype=torch.int32, device=dev)
+    rev[:P] = torch.from_numpy(np.asarray(rev_tables[P], dtype=np.int32))
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    I = ctypes.c_int  # noqa: E741
+    fn = lambda k: d.function(cubin, _CONV_K[k])  # noqa: E731
+    # fft_conv2d_inv_rev_pad (kernel.cu:1255): rotate the filters in place, pad
+    d.launch(fn("inv"), (F * S, fy // 2), (fx, 1), 0, [ptr(cu_filter), I(fx), I(fy)])
+    if fy & 1 and fx // 2 > 0:
+        d.launch(fn("inv_odd"), (F * S, 1), (fx // 2, 1), 0, [ptr(cu_filter), I(fx), I(fy)])
+    d.launch(fn("pad"), (S, P), (P, 1), 0, [ptr(cu_signal), ptr(sig_pad), ptr(rev), ptr(rev), I(P), I(P), I(sx), I(sy)])
+    d.launch(fn("pad"), (F * S, P), (P, 1), 0,
+             [ptr(cu_filter), ptr(filt_pad), ptr(rev), ptr(rev), I(P), I(P), I(fx), I(fy)])
+    torch.cuda.synchronize()
+    _tc_exec_2d(d, cubin, sig_pad, P, S, 1)
+    _tc_exec_2d(d, cubin, filt_pad, P, F * S, 1)
+    # fft_pointwise (kernel.cu:1101): FP32 sum over channels, per-filter
+    # power-of-ten quantisation, digit-reversed FP16 planes
+    pw_f = torch.zeros(F * P * P * 2, dtype=torch.float32, device=dev)
+    pw_h = torch.zeros(F * P * P * 2, dtype=torch.float16, device=dev)
+    max_line = torch.zeros(F * P, dtype=torch.float32, device=dev)
+    max_tile = torch.zeros(F, dtype=torch.float32, device=dev)
+    d.launch(fn("mul_add"), (F, P), (P, 1), 0, [ptr(sig_pad), ptr(filt_pad), ptr(pw_f), I(S), I(F), I(P), I(P)])
+    d.launch(fn("q1"), (F, 1), (P, 1), 0, [ptr(pw_f), ptr(max_line), I(P), I(P)])
+    d.launch(fn("q2"), (1, 1), (F, 1), 0, [ptr(max_line), ptr(max_tile), I(P), I(P)])
+    d.launch(fn("q3"), (F, P), (P, 1), 0, [ptr(pw_f), ptr(pw_h), ptr(max_tile), ptr(rev), ptr(rev), I(P), I(P)])
+    torch.cuda.synchronize()
+    _tc_exec_2d(d, cubin, pw_h, P, F, -1)
+    # fft_conv_final_stage (kernel.cu:1141) and readout_fwd (.cpp:275)
+    padded = torch.zeros(F * P * P * 2, dtype=torch.float64, device=dev)
+    d.launch(fn("deq"), (F, P), (P, 1), 0, [ptr(pw_h), ptr(padded), ptr(max_tile), I(P), I(P)])
+    out = torch.zeros(F * oy * ox, dtype=torch.float64, device=dev)
+    scale = float(np.float32(1.0) / np.float32(P * P))
+    d.launch(fn("read"), (F, oy), (ox, 1), 0,
+             [ptr(padded), ptr(out), I(P), I(P), I(ox), I(oy), I(fx), ctypes.c_double(scale)])
+    torch.cuda.synchronize()
+    return out.cpu().numpy().reshape(F, oy, ox)

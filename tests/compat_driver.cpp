@@ -10,10 +10,13 @@
 #include <string>
 #include <vector>
 
+#include <cuda_runtime.h>
+
 #include "fftconvolve2d.cuh"
 #include "tcfft_half.h"
 #include "tcfft_half_2d.h"
 #include "tensorcore_fft_conv2d.h"
+#include "tcfft_gb300.h"
 
 static unsigned long long g_state = 42;
 static double next_val() {  // seeded values in {0, 0.1, ..., 0.9}, like generate_data (main.cpp:32)
@@ -114,6 +117,87 @@ int main(int argc, char** argv) {
     std::vector<cufftComplex> spec((kernelCount / 2) * 256 * 256);
     direct_fft(ker.data(), kernelCount, o, o, f, f, spec.data());
     dump(out + "/direct_fft.bin", spec.data(), spec.size() * sizeof(cufftComplex));
+  }
+  // ---- TensorCoreFFTCreate / TensorCoreFFTExec (kernel.cu:1557,1495,1526) ----
+  // [batch][nx][ny] complex, both axes digit-reversed by the class's rev()
+  // (its gen_rev tables), forward (fft = 1, default stream) and inverse
+  // (fft = -1, stream overload); nx = 256 rows of ny = 512 elements.
+  {
+    const int nx = 256, ny = 512, batch = 3;
+    const size_t cnt = 2ull * nx * ny * batch;
+    std::vector<double> x(cnt), fwd(cnt), inv(cnt);
+    for (auto& v : x) v = next_val() - 0.45;
+    double* d = nullptr;
+    half *h1 = nullptr, *h2 = nullptr;
+    cudaMalloc(&d, sizeof(double) * cnt);
+    cudaMalloc(&h1, sizeof(half) * cnt);
+    cudaMalloc(&h2, sizeof(half) * cnt);
+    cudaMemcpy(d, x.data(), sizeof(double) * cnt, cudaMemcpyHostToDevice);
+    fft_conv2d_half obj;
+    obj.rev(d, h1, ny, nx, batch, 0, nullptr);  // x = elements per row, y = rows
+    obj.rev(d, h2, ny, nx, batch, 0, nullptr);
+    fftPlan pf, pi;
+    obj.TensorCoreFFTCreate(&pf, nx, ny, batch, 1, __AMPERE__);
+    obj.TensorCoreFFTCreate(&pi, nx, ny, batch, -1, __AMPERE__);
+    obj.TensorCoreFFTExec(pf, h1);
+    cudaStream_t st;
+    cudaStreamCreate(&st);
+    obj.TensorCoreFFTExec(pi, h2, st);
+    cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+    printf("TensorCoreFFTExec status %d\n", obj.last_status);
+    obj.half2double(h1, d, nx, ny, 2, batch, nullptr);
+    cudaMemcpy(fwd.data(), d, sizeof(double) * cnt, cudaMemcpyDeviceToHost);
+    obj.half2double(h2, d, nx, ny, 2, batch, nullptr);
+    cudaMemcpy(inv.data(), d, sizeof(double) * cnt, cudaMemcpyDeviceToHost);
+    obj.TensorCoreFFTDestroy(&pf);
+    obj.TensorCoreFFTDestroy(&pi);
+    cudaFree(d);
+    cudaFree(h1);
+    cudaFree(h2);
+    dump(out + "/tc_in.bin", x.data(), cnt * 8);
+    dump(out + "/tc_fwd.bin", fwd.data(), cnt * 8);
+    dump(out + "/tc_inv.bin", inv.data(), cnt * 8);
+    // internal pipeline steps that cannot run on their own report it
+    obj.fft_pointwise();
+    printf("fft_pointwise status %d\n", obj.last_status);
+  }
+  // ---- qdFFT route: qd_fft, fast_fft, convolve_turbo_fft_v3 ----
+  {
+    const int kernelCount = 16, f = 13, o = 244, P = 256;
+    std::vector<float> sig(o * o), ker(f * f * kernelCount), res((o + f - 1) * (o + f - 1) * kernelCount);
+    for (auto& v : sig) v = static_cast<float>(next_val());
+    for (auto& v : ker) v = static_cast<float>(next_val() - 0.45);
+    dump(out + "/qd_sig.bin", sig.data(), sig.size() * 4);
+    dump(out + "/qd_ker.bin", ker.data(), ker.size() * 4);
+    convolve_turbo_fft_v3(sig.data(), ker.data(), kernelCount, o, o, f, f, res.data());
+    printf("turbo_v3 status %d\n", tcfft_get_last_error());
+    dump(out + "/qd_v3.bin", res.data(), res.size() * 4);
+    std::vector<cufftComplex> spec((kernelCount / 2) * P * P);
+    qd_fft(ker.data(), kernelCount, o, o, f, f, spec.data());
+    printf("qd_fft status %d\n", tcfft_get_last_error());
+    dump(out + "/qd_fft.bin", spec.data(), spec.size() * sizeof(cufftComplex));
+    // fast_fft on device planes: pairs packed as (re, im), zero-padded to P x P
+    const int groups = kernelCount / 2;
+    std::vector<cufftComplex> planes(static_cast<size_t>(groups) * P * P), fres(planes.size());
+    for (auto& c : planes) c.x = c.y = 0.f;
+    for (int g = 0; g < groups; ++g)
+      for (int y = 0; y < f; ++y)
+        for (int x = 0; x < f; ++x) {
+          cufftComplex& c = planes[(static_cast<size_t>(g) * P + y) * P + x];
+          c.x = ker[(2 * g) * f * f + y * f + x];
+          c.y = ker[(2 * g + 1) * f * f + y * f + x];
+        }
+    cufftComplex *dp = nullptr, *dr = nullptr;
+    cudaMalloc(&dp, sizeof(cufftComplex) * planes.size());
+    cudaMalloc(&dr, sizeof(cufftComplex) * planes.size());
+    cudaMemcpy(dp, planes.data(), sizeof(cufftComplex) * planes.size(), cudaMemcpyHostToDevice);
+    fast_fft(dp, groups, P, P, f, f, dr, true);
+    printf("fast_fft status %d\n", tcfft_get_last_error());
+    cudaMemcpy(fres.data(), dr, sizeof(cufftComplex) * fres.size(), cudaMemcpyDeviceToHost);
+    cudaFree(dp);
+    cudaFree(dr);
+    dump(out + "/fast_fft.bin", fres.data(), fres.size() * sizeof(cufftComplex));
   }
   printf("compat driver done\n");
   return 0;

@@ -16,7 +16,7 @@ it. Everything is taken from the reference's compiled source or header text:
   conv_rev_256/512    first N entries of rev_256 / rev_512
                       (tensorcore_fft_conv2d.h:72,96), parsed from the header
 
-Usage: python tests/golden/make_golden.py [reference_dir]
+Usage: python tests/golden/make_golden.py REFERENCE_DIR  (or FFT_DEMO_REF=...)
 """
 import ctypes
 import os
@@ -55,7 +55,9 @@ SIZES_2D = (256, 512, 1024)
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("FFT_DEMO_REF", "")
+    if not ref:
+        raise SystemExit("usage: make_golden.py REFERENCE_DIR (or set FFT_DEMO_REF)")
     lib1 = os.path.join(REPO, "oracle", "_ref", "libref_tcfft1d.so")
     lib2 = os.path.join(REPO, "oracle", "_ref", "libref_tcfft2d.so")
     if not (os.path.exists(lib1) and os.path.exists(lib2)):

@@ -9,10 +9,21 @@ natural-order input is its inverse permutation) and the reference's output.
 The committed copies are trimmed to a few lines per case (KEEP_LINES); the
 large cases keep only the A100 wiring.
 
+Convolution fixtures (ref_conv_*.npz): the reference's fft_conv2d_half
+forward pass (valid cross-correlation, _A100 wiring, oracle/_ref/
+ref_conv.cubin through ref_launch.run_conv_valid) at both padded sizes it
+supports, P = 256 (128 x 128 image, S = 2 channels, F = 3 filters of
+13 x 13) and P = 512 (256 x 256 image, the reference's main.cpp:322-328
+shape with F = 2 filters). Inputs are multiples of 1/16 (exact in FP16),
+stored as small integers: signal = k / 16 (k in [0, 16)), filters = j / 16
+(j in [-8, 8)); outputs as float32.
+
 Usage: python tests/golden/make_ref_gpu_fixtures.py OUT_DIR
+       python tests/golden/make_ref_gpu_fixtures.py --conv OUT_DIR
        python tests/golden/make_ref_gpu_fixtures.py --trim FULL_DIR OUT_DIR
-The second form trims full-size outputs of the first form written earlier
-with TRIM=0. The committed copies live in tests/golden/ref_tcfft_*.npz.
+The second form writes only the convolution fixtures; the third trims
+full-size outputs of the first form written earlier with TRIM=0. The
+committed copies live in tests/golden/ref_tcfft_*.npz and ref_conv_*.npz.
 """
 import os
 import sys
@@ -46,9 +57,29 @@ def trim(src_dir, out_dir):
         save({k: d[k] for k in d.files}, out_dir, name)
 
 
+CASES_CONV = [("conv_256", 2, 3, 128, 13, 31), ("conv_512", 1, 2, 256, 13, 32)]  # name, S, F, side, f, seed
+
+
+def conv_fixtures(out_dir):
+    g = np.load(os.path.join(HERE, "reference_perm.npz"))
+    rev = {256: g["conv_rev_256"], 512: g["conv_rev_512"]}
+    for name, S, F, side, f, seed in CASES_CONV:
+        rng = np.random.default_rng(seed)
+        k_sig = rng.integers(0, 16, (S, side, side)).astype(np.int8)
+        k_filt = rng.integers(-8, 8, (F, S, f, f)).astype(np.int8)
+        out = ref_launch.run_conv_valid(k_sig / 16.0, k_filt / 16.0, rev)
+        np.savez_compressed(os.path.join(out_dir, "ref_%s.npz" % name), signal_x16=k_sig, filters_x16=k_filt,
+                            out=out.astype(np.float32))
+        print(name, "done", out.shape)
+
+
 def main():
     if len(sys.argv) == 4 and sys.argv[1] == "--trim":
         trim(sys.argv[2], sys.argv[3])
+        return
+    if len(sys.argv) == 3 and sys.argv[1] == "--conv":
+        os.makedirs(sys.argv[2], exist_ok=True)
+        conv_fixtures(sys.argv[2])
         return
     out_dir = sys.argv[1] if len(sys.argv) > 1 else HERE
     os.makedirs(out_dir, exist_ok=True)
@@ -91,6 +122,7 @@ def main():
             res["out_" + variant] = ref_launch.run_2d(xp, nx, ny, batch, mergings, variant)
         save(res, out_dir, "2d_%d" % nx)
         print("2d", nx, "done")
+    conv_fixtures(out_dir)
 
 
 if __name__ == "__main__":

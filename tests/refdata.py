@@ -1,6 +1,7 @@
-"""Loaders for tests/golden/ref_tcfft_*.npz: outputs of the reference's own
-tcFFT kernels (tcfft_half.cu, tcfft_half_2d.cu, compiled from its source and
-run on a GB300 by tests/golden/make_ref_gpu_fixtures.py).
+"""Loaders for tests/golden/ref_tcfft_*.npz and ref_conv_*.npz: outputs of the
+reference's own tcFFT kernels (tcfft_half.cu, tcfft_half_2d.cu) and of its
+FFT convolution (fft_conv2d_half, tensorcore_fft_conv2d_kernel.cu), compiled
+from its source and run on a GB300 by tests/golden/make_ref_gpu_fixtures.py.
 
 Each case holds the digit-reversed FP16 input the reference consumes
 (`input_permuted`, as setup() / setup_2d() build it, main.cpp:171,189), the
@@ -15,6 +16,7 @@ import numpy as np
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES_1D = [256, 512, 1024, 131072]
 CASES_2D = [256, 512]
+CASES_CONV = [256, 512]
 
 
 def _perm():
@@ -52,3 +54,14 @@ def load_2d(n):
     x[:, rev] = t
     outs = {v: _cplx(d["out_" + v]) for v in ("A100", "V100") if "out_" + v in d.files}
     return _cplx(x), xp, [int(r) for r in d["radices_x"]], [int(r) for r in d["radices_y"]], outs
+
+
+def conv_available(p):
+    return os.path.exists(os.path.join(GOLDEN, "ref_conv_%d.npz" % p))
+
+
+def load_conv(p):
+    """Convolution case at padded size p: (signal [S][s][s], filters
+    [F][S][f][f], the reference's valid cross-correlation [F][s-f+1][s-f+1])."""
+    d = np.load(os.path.join(GOLDEN, "ref_conv_%d.npz" % p))
+    return d["signal_x16"] / 16.0, d["filters_x16"] / 16.0, d["out"].astype(np.float64)

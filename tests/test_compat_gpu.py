@@ -23,6 +23,7 @@ def driver_out(tc, tmp_path_factory):
     exe = str(out / "compat_driver")
     libdir = os.path.join(REPO, "fft_demo_gb300")
     cmd = ["nvcc", "-std=c++17", "-O2", "-I" + os.path.join(REPO, "include", "compat"),
+           "-I" + os.path.join(REPO, "include"),
            os.path.join(REPO, "tests", "compat_driver.cpp"), "-o", exe, "-L" + libdir, "-ltcfft_gb300",
            "-Xlinker", "-rpath=" + libdir, "-lcufft"]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -30,6 +31,7 @@ def driver_out(tc, tmp_path_factory):
     r = subprocess.run([exe, str(out)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "compat driver done" in r.stdout
+    (out / "stdout.txt").write_text(r.stdout)
     return out
 
 
@@ -106,3 +108,46 @@ def test_fftconvolve2d_family(driver_out, orc):
     packed = np.zeros((8, 256, 256), complex)
     packed[:, :13, :13] = ker[0::2] + 1j * ker[1::2]
     assert orc.rel_l2(spec, orc.fft2d(packed, sign=+1)) < REL_SPLIT
+
+
+def _status(d, what):
+    for line in (d / "stdout.txt").read_text().splitlines():
+        if line.startswith(what + " status"):
+            return int(line.split()[2])
+    raise AssertionError("no status line for " + what)
+
+
+def test_tensorcore_fft_exec_both_directions(driver_out, orc):
+    """TensorCoreFFTCreate/Exec (tensorcore_fft_conv2d_kernel.cu:1557,1495,1526)
+    on input digit-reversed by the class's rev(): fft = 1 is the forward and
+    fft = -1 the unnormalised inverse 2D DFT, through both Exec overloads."""
+    assert _status(driver_out, "TensorCoreFFTExec") == 0
+    x = cplx(h(load(driver_out, "tc_in.bin"))).reshape(3, 256, 512)
+    fwd = cplx(load(driver_out, "tc_fwd.bin")).reshape(3, 256, 512)
+    inv = cplx(load(driver_out, "tc_inv.bin")).reshape(3, 256, 512)
+    assert orc.rel_l2(fwd, orc.fft2d(x)) < REL_FP16
+    assert orc.rel_l2(inv, orc.fft2d(x, sign=+1)) < REL_FP16
+
+
+def test_internal_pipeline_steps_report_unsupported(driver_out):
+    assert _status(driver_out, "fft_pointwise") == 2  # TCFFT_UNSUPPORTED
+
+
+def test_qd_route(driver_out, orc):
+    """qd_fft, fast_fft and convolve_turbo_fft_v3 (fftconvolve2d.cu:1603,1011,
+    1263): spectra by line projections equal the 2D DFT of the zero-padded
+    kernel pairs; v3's convolution equals the FP64 full convolution."""
+    for what in ("turbo_v3", "qd_fft", "fast_fft"):
+        assert _status(driver_out, what) == 0, what
+    sig = load(driver_out, "qd_sig.bin", np.float32).astype(np.float64).reshape(244, 244)
+    ker = load(driver_out, "qd_ker.bin", np.float32).astype(np.float64).reshape(16, 13, 13)
+    v3 = load(driver_out, "qd_v3.bin", np.float32).reshape(16, 256, 256)
+    assert orc.rel_l2(v3, orc.conv2d_full(sig, ker)) < REL_SPLIT
+    packed = np.zeros((8, 256, 256), complex)
+    packed[:, :13, :13] = ker[0::2] + 1j * ker[1::2]
+    spec = load(driver_out, "qd_fft.bin", np.float32)
+    spec = (spec[0::2] + 1j * spec[1::2]).reshape(8, 256, 256)
+    assert orc.rel_l2(spec, orc.fft2d(packed, sign=+1)) < REL_SPLIT
+    fspec = load(driver_out, "fast_fft.bin", np.float32)
+    fspec = (fspec[0::2] + 1j * fspec[1::2]).reshape(8, 256, 256)
+    assert orc.rel_l2(fspec, orc.fft2d(packed, sign=-1)) < REL_SPLIT

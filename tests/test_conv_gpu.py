@@ -4,7 +4,11 @@ Oracles (oracle/liborc.so): valid cross-correlation summed over channels
 (restating naive_fft_conv2d_ss_sf_valid, main.cpp:97), 'same' and full
 linear convolution, all FP64 direct sums.
 Tolerances (relative L2 vs FP64): FP16 plans 3e-3 (REL_L2_CONV_FP16),
-split plans 1e-5 (REL_L2_CONV_SPLIT).
+split plans 1e-5 (REL_L2_CONV_SPLIT), on non-negative filters. With
+zero-mean filters the output is much smaller than the scale FP16 spectra are
+rounded at, so those cases are held to the error against the inputs' scale
+||x||_2 ||w||_1 (pyoracle.conv_scaled_err): FP16 2e-3 (CONV_SCALED_FP16),
+about four FP16 unit roundoffs (2^-11).
 """
 import numpy as np
 import pytest
@@ -13,6 +17,7 @@ pytestmark = pytest.mark.gpu
 
 REL_L2_CONV_FP16 = 3e-3
 REL_L2_CONV_SPLIT = 1e-5
+CONV_SCALED_FP16 = 2e-3
 
 
 def reference_data(s, f, C, F, seed=42):
@@ -130,3 +135,29 @@ def test_conv_errors(tc):
         tc.Conv2d(1, 1, 8, 8, 9, 9, mode=tc.CONV_VALID_CORR)  # filter larger than image
     with pytest.raises(tc.TcfftError):
         tc.Conv2d(1, 1, 3000, 3000, 31, 31, mode=tc.CONV_SAME, precision=tc.SPLIT_FP32)
+
+
+def test_config3_same_convolution_2048(tc, orc):
+    """The stated large convolution: a 2048 x 2048 FP16 image, U[0,1], 'same'
+    convolution with a 31 x 31 filter of N(0,1) entries scaled to unit L1,
+    zero-padded to P = next_pow2(2048 + 32) = 4096, against the FP64 direct
+    'same' convolution of the FP16-rounded image. The filter is zero-mean,
+    so the error is held to CONV_SCALED_FP16 of the inputs' scale; the plain
+    relative L2 is reported in the assertion message."""
+    import torch
+    rng = np.random.default_rng(3)
+    img = rng.uniform(0, 1, (2048, 2048))
+    w = rng.standard_normal((31, 31))
+    w /= np.abs(w).sum()
+    conv = tc.Conv2d(1, 1, 2048, 2048, 31, 31, mode=tc.CONV_SAME, precision=tc.FP16)
+    assert conv.padded == 4096
+    x = torch.from_numpy(img).half().cuda()
+    conv.set_filters(torch.from_numpy(w).float().cuda())
+    out = conv.exec(x.view(1, 1, 2048, 2048))
+    conv.check()
+    xh = img.astype(np.float16).astype(np.float64)
+    ref = orc.conv2d_same(xh, w)
+    got = out.double().cpu().numpy()[0, 0]
+    err = orc.conv_scaled_err(got[None, None], ref[None, None], xh[None, None], w[None, None])
+    assert err < CONV_SCALED_FP16, (err, orc.rel_l2(got, ref))
+    conv.destroy()

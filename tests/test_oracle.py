@@ -134,3 +134,39 @@ def test_clipped_error_semantics(orc):
     s = np.array([1.0, 1.0, 0.0, 0.0])
     assert abs(orc.clipped_error(t, s) - (0 + 1 + 1 + 1) / 4) < 1e-15
     assert abs(orc.clipped_error(np.array([1.1]), np.array([1.0])) - 0.1) < 1e-12
+
+
+@pytest.mark.parametrize("n,br,bc", [(16, 16, 16), (64, 7, 5), (256, 13, 13)])
+def test_qd_restatement_is_the_2d_dft(orc, n, br, bc):
+    """The line-projection restatement (fast_fft's method) equals the FP64 2D
+    DFT for planes whose non-zeros lie in the box, both signs: every
+    frequency lies on one of the 3n/2 lines through the origin."""
+    rng = np.random.default_rng(n)
+    x = np.zeros((2, n, n), complex)
+    x[:, :br, :bc] = rng.uniform(-1, 1, (2, br, bc)) + 1j * rng.uniform(-1, 1, (2, br, bc))
+    for sign in (-1, 1):
+        assert orc.rel_l2(orc.qd_fft2d(x, br, bc, sign), orc.fft2d(x, sign)) < 1e-13
+
+
+def test_qd_canonical_owner(orc):
+    """Closed form the CUDA gather uses to pick one (direction, k) per
+    frequency (fft_demo_gb300/csrc/qd.cu, qd_owner): restated here, every
+    (u, v) of an n x n plane must lie on its owner's line at position k."""
+    for logn in (4, 6, 8):
+        n = 1 << logn
+        for u in range(n):
+            for v in range(n):
+                if u == 0 and v == 0:
+                    d, k = 0, 0
+                else:
+                    a = (u & -u).bit_length() - 1 if u else logn
+                    b = (v & -v).bit_length() - 1 if v else logn
+                    if a <= b:
+                        m = n >> a
+                        d, k = ((v >> a) * pow(u >> a, -1, m)) % m, u
+                    else:
+                        m = n >> b
+                        d, k = n + ((((u >> b) * pow(v >> b, -1, m)) % m) >> 1), v
+                p, s = (1, d) if d < n else (2 * (d - n), 1)
+                assert 0 <= d < n + n // 2
+                assert ((k * p) % n, (k * s) % n) == (u, v), (n, u, v, d, k)

@@ -14,6 +14,7 @@ import pytest
 import refdata
 
 REF_REL_MAX = 3e-3
+REF_CONV_REL_MAX = 2e-2  # FP16 accumulation plus a power-of-ten FP16 quantisation of the product
 
 
 @pytest.mark.parametrize("n", refdata.CASES_1D)
@@ -44,3 +45,16 @@ def test_fixture_permutation_matches_oracle_gen_rev(orc):
     for n in (256, 512, 1024):
         _, _, radices, _ = refdata.load_1d(n)
         assert np.array_equal(g["gen_rev_%d" % n], orc.gen_rev(n, radices))
+
+
+@pytest.mark.parametrize("p", refdata.CASES_CONV)
+def test_reference_conv_is_valid_correlation(orc, p):
+    """The reference's fft_conv2d_half forward output (its own kernels, _A100
+    wiring) is the valid cross-correlation the oracle restates
+    (naive_fft_conv2d_ss_sf_valid, main.cpp:97), to FP16 accuracy: this pins
+    orc_corr2d_valid to the reference itself."""
+    if not refdata.conv_available(p):
+        pytest.skip("fixture not generated")
+    sig, filt, out = refdata.load_conv(p)
+    err = orc.rel_l2(out, orc.corr2d_valid(sig, filt))
+    assert err < REF_CONV_REL_MAX, err

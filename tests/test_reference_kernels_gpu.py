@@ -65,3 +65,28 @@ def test_2d_matches_reference_kernels(tc, orc, n):
     print("2d n=%d ours %.3e reference %.3e" % (n, e_ours, e_ref))
     assert e_ours <= REF_SLACK * e_ref
     assert orc.rel_l2(y, outs["A100"]) <= e_ours + e_ref
+
+
+@pytest.mark.parametrize("p", refdata.CASES_CONV)
+def test_conv_matches_reference_conv(tc, orc, p):
+    """The valid cross-correlation of fft_conv2d_half::conv2d_forward
+    (tensorcore_fft_conv2d.cpp:283) on the reference's own output: same rule
+    as the transforms (ours at least as accurate against FP64, and the two
+    within the sum of their errors)."""
+    import torch
+    if not refdata.conv_available(p):
+        pytest.skip("fixture not generated")
+    sig, filt, ref_out = refdata.load_conv(p)
+    S, s = sig.shape[0], sig.shape[1]
+    F, f = filt.shape[0], filt.shape[2]
+    conv = tc.Conv2d(S, F, s, s, f, f, mode=tc.CONV_VALID_CORR, precision=tc.FP16)
+    conv.set_filters(torch.from_numpy(filt).float().cuda())
+    out = conv.exec(torch.from_numpy(sig).half().cuda().view(1, S, s, s))
+    conv.check()
+    y = out.double().cpu().numpy()[0]
+    exact = orc.corr2d_valid(sig, filt)
+    e_ours, e_ref = orc.rel_l2(y, exact), orc.rel_l2(ref_out, exact)
+    print("conv P=%d ours %.3e reference %.3e" % (p, e_ours, e_ref))
+    assert e_ours <= REF_SLACK * e_ref
+    assert orc.rel_l2(y, ref_out) <= e_ours + e_ref
+    conv.destroy()

@@ -6,8 +6,10 @@ with plan-owned memory): bit-identical results, on two calls in a row (the
 second call reuses the scratch the first one left behind), in both
 directions, in place, and with batches that cycle the workspace ring.
 The same checks run once more in a fresh process, where the first call also
-sets the scratch up. The file is named to be collected after every other
-test file.
+sets the scratch up; there the device memory the first call takes (module
+load of the library's device code and the array) is measured and bounded,
+and later calls must take none. The file is named to be collected after
+every other test file.
 """
 import os
 import subprocess
@@ -75,6 +77,28 @@ def test_matches_plan_entry_point(tc):
     run_checks(tc)
 
 
+def test_error_from_an_unwaited_call_is_reported_by_the_next_wait(tc):
+    """A kernel error flagged during a call made with wait == 0 stays in the
+    scratch array until a call with wait != 0 reports it (TCFFT_TIMEOUT) and
+    clears it. The error is provoked without any hang: the dependency waits of
+    the fused kernel get a poll bound of zero (tcfft_set_wait_limit(0)), so
+    they give up at once."""
+    import torch
+    n, batch = 1 << 15, 200
+    x = _input(n, batch, seed=3)
+    out = torch.zeros_like(x)
+    L = tc.lib()
+    tc.set_wait_limit(0)
+    try:
+        assert L.tcfft_exec_static(x.data_ptr(), out.data_ptr(), n, batch, tc.FORWARD, 1.0, None, 0) == tc.OK
+    finally:
+        tc.set_wait_limit(-1)
+    torch.cuda.synchronize()
+    assert L.tcfft_exec_static(x.data_ptr(), out.data_ptr(), n, batch, tc.FORWARD, 1.0, None, 1) == tc.TIMEOUT
+    assert L.tcfft_exec_static(x.data_ptr(), out.data_ptr(), n, batch, tc.FORWARD, 1.0, None, 1) == tc.OK
+    assert torch.equal(out, _plan_out(tc, x, n, batch, tc.FORWARD, 1.0))
+
+
 def test_rejects_sizes_beyond_the_scratch(tc):
     import torch
     buf = torch.zeros((1 << 16,), dtype=torch.float16, device="cuda")
@@ -95,7 +119,31 @@ def test_fresh_process():
     assert "no-alloc checks passed" in r.stdout
 
 
+def first_call_memory(tc):
+    """Device memory the first call on a fresh device context takes: the
+    library's device code and the static array, loaded when first needed
+    (lazy module loading; the first call of the library also loads the
+    kernels its registry sets attributes on). Bounded by the array plus four
+    times the size of the library file (code, constant banks and the local
+    memory the driver reserves for them); later calls take nothing
+    (run_checks)."""
+    import torch
+    n, batch = CASES[0]
+    x = _input(n, batch, seed=9)
+    out = torch.zeros_like(x)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    tc.exec_static(x, n, batch, out)
+    torch.cuda.synchronize()
+    used = free0 - torch.cuda.mem_get_info()[0]
+    lib_bytes = os.path.getsize(tc.LIB_PATH)
+    assert 0 <= used <= (17 << 20) + 4 * lib_bytes, used
+    return used
+
+
 if __name__ == "__main__":
     import fft_demo_gb300 as tc_mod
+    first = first_call_memory(tc_mod)
     run_checks(tc_mod)
+    print("first call took %.1f MiB of device memory" % (first / 2**20))
     print("no-alloc checks passed")
