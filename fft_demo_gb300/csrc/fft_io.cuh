@@ -138,16 +138,7 @@ struct IoHalf {
   // The outer twiddle and scale store_row16 applies, in place (for outputs
   // that go out through a staged tensor store instead).
   __device__ __forceinline__ void prepare_row16(long long line, int j, int J, float2 (&v)[16]) const {
-    if (otw.hi) {
-      const long long li = line & ((1ll << lps_log2) - 1);
-      float2 w = otw(li, j);
-      const float2 step = otw(li, J);
-#pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        v[c] = cmulf(v[c], w);
-        w = cmulf(w, step);
-      }
-    }
+    if (otw.hi) outer_twiddle16(line, j, J, v);
     if (scale != 1.0f) {
 #pragma unroll
       for (int c = 0; c < 16; ++c) v[c] = make_float2(v[c].x * scale, v[c].y * scale);
@@ -155,18 +146,23 @@ struct IoHalf {
   }
   // Outputs l = j + c*J (c = 0..15) of one line. The outer twiddle
   // W_N^{li*l} is formed as W_N^{li*j} * (W_N^{li*J})^c (FP32 recurrence).
+  // v[c] *= W_N^{li*(j + c*J)} for c = 0..15: W_N^{li*j} * (W_N^{li*J})^c,
+  // an FP32 recurrence over pairs of outputs (packed instructions).
+  __device__ __forceinline__ void outer_twiddle16(long long line, int j, int J, float2 (&v)[16]) const {
+    const long long li = line & ((1ll << lps_log2) - 1);
+    TwPairSeq tws(otw(li, j), otw(li, J));
+#pragma unroll
+    for (int c = 0; c < 16; c += 2) {
+      float2 yr, yi;
+      cmul_pair(make_float2(v[c].x, v[c + 1].x), make_float2(v[c].y, v[c + 1].y), tws.w, yr, yi);
+      if (c + 2 < 16) tws.next();
+      v[c] = make_float2(yr.x, yi.x);
+      v[c + 1] = make_float2(yr.y, yi.y);
+    }
+  }
   __device__ __forceinline__ void store_row16(long long line, int j, int J, float2 (&v)[16]) const {
     half2* p = out + out_base(line);
-    if (otw.hi) {
-      const long long li = line & ((1ll << lps_log2) - 1);
-      float2 w = otw(li, j);
-      const float2 step = otw(li, J);
-#pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        v[c] = cmulf(v[c], w);
-        w = cmulf(w, step);
-      }
-    }
+    if (otw.hi) outer_twiddle16(line, j, J, v);
     const long long step = static_cast<long long>(J) * out_elem;
     half2* q = p + static_cast<long long>(j) * out_elem;
     if (scale == 1.0f) {

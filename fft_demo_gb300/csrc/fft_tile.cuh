@@ -80,6 +80,52 @@ __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 
+// Packed FP32 pairs: one sm_100-family instruction does the same operation on
+// two lanes of work (a float2 held in an aligned register pair), so complex
+// arithmetic over two outputs at a time costs half the issue slots.
+__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 f2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 f2bcast(float v) { return make_float2(v, v); }
+
+// Twiddles of two outputs as pairs of components: re = (w0.x, w1.x),
+// im = (w0.y, w1.y), and nim = -im (kept so that no product needs a negation).
+struct TwPair {
+  float2 re, im, nim;
+};
+__device__ __forceinline__ TwPair twpair(float2 w0, float2 w1) {
+  return TwPair{make_float2(w0.x, w1.x), make_float2(w0.y, w1.y), make_float2(-w0.y, -w1.y)};
+}
+// Multiplies both twiddles by the complex scalar s, given as broadcast pairs
+// sr = (s.x, s.x), si = (s.y, s.y), nsi = -si.
+__device__ __forceinline__ void twpair_step(TwPair& w, float2 sr, float2 si, float2 nsi) {
+  const float2 re = f2fma(w.im, nsi, f2mul(w.re, sr));
+  const float2 im = f2fma(w.im, sr, f2mul(w.re, si));
+  const float2 nim = f2fma(w.nim, sr, f2mul(w.re, nsi));
+  w.re = re;
+  w.im = im;
+  w.nim = nim;
+}
+// (yr, yi) = (xr + i xi) * w for two outputs: xr = (x0.x, x1.x), xi = (x0.y, x1.y).
+__device__ __forceinline__ void cmul_pair(float2 xr, float2 xi, const TwPair& w, float2& yr, float2& yi) {
+  yr = f2fma(xi, w.nim, f2mul(xr, w.re));
+  yi = f2fma(xi, w.re, f2mul(xr, w.im));
+}
+// Twiddle recurrence over 16 outputs c = 0..15 as 8 pairs (c, c + 1):
+// W^(e0 + c de) from w = W^e0 and step = W^de; pair k+1 = pair k * step^2.
+struct TwPairSeq {
+  TwPair w;
+  float2 sr, si, nsi;
+  __device__ __forceinline__ TwPairSeq(float2 w0, float2 step) {
+    w = twpair(w0, cmulf(w0, step));
+    const float2 s2 = cmulf(step, step);
+    sr = f2bcast(s2.x);
+    si = f2bcast(s2.y);
+    nsi = f2bcast(-s2.y);
+  }
+  __device__ __forceinline__ void next() { twpair_step(w, sr, si, nsi); }
+};
+
 // In-register radix-T DFT (T in {1,2,4,8}), SIGN = -1 forward, +1 inverse.
 template <int T, int SIGN>
 __device__ __forceinline__ void small_dft(float2 (&v)[T]) {
@@ -292,18 +338,17 @@ __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const f
       if constexpr (Ns == 1 && !LINE_MINOR) {
         // 16 outputs -> 16 consecutive columns: two 16-byte stores per plane
         uint32_t pr[8], pi[8];
-        // twiddles by recurrence: two table reads per row (FP32 error ~1e-6,
-        // far below the FP16 rounding that follows)
-        float2 w = w_pre;
-        const float2 wstep = wstep_pre;
+        // twiddles by recurrence, two outputs per packed instruction: two
+        // table reads per row (FP32 error ~1e-6, far below the FP16 rounding
+        // that follows)
+        TwPairSeq tws(w_pre, wstep_pre);
 #pragma unroll
         for (int c = 0; c < 16; c += 2) {
-          const float2 w0 = w;
-          const float2 w1 = cmulf(w0, wstep);
-          w = cmulf(w1, wstep);
-          const float2 x0 = cmulf(make_float2(__uint_as_float(d[c]), __uint_as_float(d[16 + c])), w0);
-          const float2 x1 = cmulf(make_float2(__uint_as_float(d[c + 1]), __uint_as_float(d[17 + c])), w1);
-          __half2 hr = __floats2half2_rn(x0.x, x1.x), hi = __floats2half2_rn(x0.y, x1.y);
+          float2 yr, yi;
+          cmul_pair(make_float2(__uint_as_float(d[c]), __uint_as_float(d[c + 1])),
+                    make_float2(__uint_as_float(d[16 + c]), __uint_as_float(d[17 + c])), tws.w, yr, yi);
+          if (c + 2 < 16) tws.next();
+          __half2 hr = __float22half2_rn(yr), hi = __float22half2_rn(yi);
           pr[c / 2] = *reinterpret_cast<uint32_t*>(&hr);
           pi[c / 2] = *reinterpret_cast<uint32_t*>(&hi);
         }
@@ -321,8 +366,20 @@ __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const f
         *reinterpret_cast<uint4*>(re + off1) = sw ? rlo : rhi;
         *reinterpret_cast<uint4*>(im + off1) = sw ? ilo : ihi;
       } else {
-        float2 w = w_pre;
-        const float2 wstep = wstep_pre;
+        // the 16 twiddled outputs, two per packed instruction
+        float2 y[16];
+        {
+          TwPairSeq tws(w_pre, wstep_pre);
+#pragma unroll
+          for (int c = 0; c < 16; c += 2) {
+            float2 yr, yi;
+            cmul_pair(make_float2(__uint_as_float(d[c]), __uint_as_float(d[c + 1])),
+                      make_float2(__uint_as_float(d[16 + c]), __uint_as_float(d[17 + c])), tws.w, yr, yi);
+            if (c + 2 < 16) tws.next();
+            y[c] = make_float2(yr.x, yi.x);
+            y[c + 1] = make_float2(yr.y, yi.y);
+          }
+        }
         // column step between consecutive outputs: Ns (line-major) or Ns*G
         // (line-minor); when it is a multiple of 64 (one swizzle atom) the
         // swizzled offset moves by a compile-time amount per output
@@ -332,11 +389,7 @@ __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const f
           const uint32_t off0 =
               krow + (mp0 >> 6) * 1024u + ((((mp0 & 63u) >> 3) ^ (rp & 7)) << 4) + (mp0 & 7u) * 2u;
 #pragma unroll
-          for (int c = 0; c < 16; ++c) {
-            const float2 x = cmulf(make_float2(__uint_as_float(d[c]), __uint_as_float(d[16 + c])), w);
-            w = cmulf(w, wstep);
-            st_pair(re, im, off0 + static_cast<uint32_t>(c) * (CSTEP / 64u) * 1024u, x);
-          }
+          for (int c = 0; c < 16; ++c) st_pair(re, im, off0 + static_cast<uint32_t>(c) * (CSTEP / 64u) * 1024u, y[c]);
         } else if constexpr (CSTEP >= 8 && (CSTEP & (CSTEP - 1)) == 0) {
           // the column moves by CSTEP < 64 per output: the swizzled offsets
           // repeat with period PER = 64 / CSTEP, shifted by one 1 KiB atom
@@ -350,19 +403,13 @@ __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const f
             offs[k] = krow + (mp >> 6) * 1024u + ((((mp & 63u) >> 3) ^ (rp & 7)) << 4) + (mp & 7u) * 2u;
           }
 #pragma unroll
-          for (int c = 0; c < 16; ++c) {
-            const float2 x = cmulf(make_float2(__uint_as_float(d[c]), __uint_as_float(d[16 + c])), w);
-            w = cmulf(w, wstep);
-            st_pair(re, im, offs[c % PER] + static_cast<uint32_t>(c / PER) * 1024u, x);
-          }
+          for (int c = 0; c < 16; ++c) st_pair(re, im, offs[c % PER] + static_cast<uint32_t>(c / PER) * 1024u, y[c]);
         } else {
 #pragma unroll
           for (int c = 0; c < 16; ++c) {
-            const float2 x = cmulf(make_float2(__uint_as_float(d[c]), __uint_as_float(d[16 + c])), w);
-            w = cmulf(w, wstep);
             const uint32_t mp = static_cast<uint32_t>(Tl::pos(g, jp0 + c * Ns));
             const uint32_t off = krow + (mp >> 6) * 1024u + ((((mp & 63u) >> 3) ^ (rp & 7)) << 4) + (mp & 7u) * 2u;
-            st_pair(re, im, off, x);
+            st_pair(re, im, off, y[c]);
           }
         }
       }
