@@ -165,68 +165,63 @@ def cufft_times(tensors, reps=5):
     return out
 
 
-def cpu_fft_sample(seconds_target=12.0, threads=0):
-    """FP64 oracle FFT on the host over a bounded sample of the workload."""
+def cpu_sample(nt):
+    """The bounded CPU sample of the workload, the same for the GPU arm's
+    cpu_baseline and for the reference arm: per size, max(nt, 2^22 / N)
+    sequences (4 Mi points, at least one sequence per host thread), seeded
+    uniform[-1, 1] complex data. One pass over it is one CPU step."""
     import numpy as np
     import pyoracle as orc
-    orc.build()
-    nt = threads if threads > 0 else orc.max_threads()
     rng = np.random.default_rng(1)
-    total_flops, total_t = 0.0, 0.0
-    per = seconds_target / len(SIZES)
-    detail = []
+    out = []
     for n, batch in SIZES:
-        # 4 Mi points per trial, and at least one sequence per thread
         b = max(1, min(batch, max(nt, (1 << 22) // n)))
-        x = (rng.uniform(-1, 1, (b, n)) + 1j * rng.uniform(-1, 1, (b, n)))
-        buf = orc.to_interleaved(x)
-        lib = orc.lib()
-        t_size, f_size, reps = 0.0, 0.0, 0
-        while t_size < per:
-            t0 = time.perf_counter()
-            lib.orc_fft1d(orc._p(buf), n, b, -1, nt)
-            dt = time.perf_counter() - t0
-            t_size += dt
-            f_size += flops(n, b)
-            reps += 1
-        total_flops += f_size
-        total_t += t_size
-        detail.append("N=%d x %d seqs x %d reps" % (n, b, reps))
-    return total_flops / total_t / 1e9, nt, "; ".join(detail)
+        x = rng.uniform(-1, 1, (b, n)) + 1j * rng.uniform(-1, 1, (b, n))
+        out.append((n, b, orc.to_interleaved(x)))
+    return out
+
+
+def cpu_step(bufs, nt):
+    """One pass of the FP64 oracle FFT (OpenMP over the batch) over the sample; flops."""
+    import pyoracle as orc
+    lib = orc.lib()
+    f = 0.0
+    for n, b, buf in bufs:
+        lib.orc_fft1d(orc._p(buf), n, b, -1, nt)
+        f += flops(n, b)
+    return f
+
+
+def cpu_fft_sample(seconds_target=12.0):
+    """GPU arm's cpu_baseline: repeated CPU steps for about seconds_target."""
+    import pyoracle as orc
+    orc.build()
+    nt = orc.max_threads()
+    bufs = cpu_sample(nt)
+    cpu_step(bufs, nt)  # warm-up
+    total_flops, total_t, reps = 0.0, 0.0, 0
+    while total_t < seconds_target:
+        t0 = time.perf_counter()
+        total_flops += cpu_step(bufs, nt)
+        total_t += time.perf_counter() - t0
+        reps += 1
+    sample = "; ".join("N=%d x %d seqs" % (n, b) for n, b, _ in bufs)
+    return total_flops / total_t / 1e9, nt, "%s per step, %d steps" % (sample, reps)
 
 
 def run_reference(args, world, rank):
     if rank != 0:
         return 0
-    import numpy as np
     import pyoracle as orc
     orc.build()
     nt = orc.max_threads()
-    lib = orc.lib()
-    rng = np.random.default_rng(1)
-    bufs = []
-    # equal points per size, as in the GPU workload, and at least one
-    # sequence per host thread for every size (the oracle parallelises over
-    # the batch), so all threads work on every transform
-    points = max(1 << 21, nt * max(n for n, _ in SIZES))
-    for n, batch in SIZES:
-        b = max(1, min(batch, points // n))
-        x = rng.uniform(-1, 1, (b, n)) + 1j * rng.uniform(-1, 1, (b, n))
-        bufs.append((n, b, orc.to_interleaved(x)))
-
-    def step():
-        f = 0.0
-        for n, b, buf in bufs:
-            lib.orc_fft1d(orc._p(buf), n, b, -1, nt)
-            f += flops(n, b)
-        return f
-
+    bufs = cpu_sample(nt)
     for _ in range(args.warmup):
-        step()
+        cpu_step(bufs, nt)
     t0 = time.perf_counter()
     fl = 0.0
     for _ in range(args.steps):
-        fl += step()
+        fl += cpu_step(bufs, nt)
     dt = time.perf_counter() - t0
     value = fl / dt / 1e9
     sample = "; ".join("N=%d x %d seqs" % (n, b) for n, b, _ in bufs)
@@ -238,7 +233,7 @@ def run_reference(args, world, rank):
         "config": {"workload": "large-1d-fp16", "sizes": [[n, b] for n, b in SIZES],
                    "sample_per_step": sample},
         "cpu_baseline": {"value": value, "unit": "GFLOP/s", "cores": nt, "kind": "port",
-                         "sample": sample + " per step (FP64 oracle FFT; FFTW absent)"},
+                         "sample": sample + " per step (FP64 oracle FFT, OpenMP over the batch; FFTW absent)"},
         "e2e": {"value": value, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -288,21 +283,23 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the other stated configurations (bench_workloads.extras) in the default line")
     ap.add_argument("--case", default=None,
                     help="profiling case N,BATCH[,REPS[,PREC]]: REPS forward transforms of one size, no timing "
                          "(PREC fp16 or split); the target of the ncu captures kept under profiles/")
     ap.add_argument("--workload", default="large-1d",
                     choices=["large-1d", "large-1d-split", "small", "2d-conv", "uneven", "serving"],
                     help="large-1d: the headline run (default); the others print one JSON line each "
-                         "(fft_demo_gb300/workloads.py)")
+                         "(bench_workloads.py)")
     args = ap.parse_args()
     if args.case:
         return run_case(args.case)
     if args.workload != "large-1d":
         load_tuning()
-        from fft_demo_gb300 import workloads
+        import bench_workloads
         peak, kind = load_peaks()
-        res = workloads.WORKLOADS[args.workload](peak)
+        res = bench_workloads.WORKLOADS[args.workload](peak)
         res.update({"peak_gbs": peak, "peak_kind": kind, "data": "synthetic (seeded)", "n_gpus": 1})
         print(json.dumps(res), flush=True)
         return 0
@@ -446,8 +443,8 @@ def main():
         windows.append(max_over_ranks(world, q0.elapsed_time(q1)) / e2e_steps)
     e2e_ms = sorted(windows)[1]
     e2e_value = whole_job_rate(step_flops, world, e2e_ms) / 1e9
-    # the pipelined results equal the device-timed ones (same inputs)
-    e2e_match = all(torch.equal(ho[:2].to(dev), y[:2]) for ho, y in zip(host_out, ys))
+    # the pipelined results equal the device-timed ones (same inputs), every sequence
+    e2e_match = all(torch.equal(ho.to(dev), y) for ho, y in zip(host_out, ys))
     for cp in chunk_plans:
         cp.check()
         cp.destroy()
@@ -470,7 +467,18 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, cores, sample = cpu_fft_sample()
         cpu = {"value": v, "unit": "GFLOP/s", "cores": cores, "kind": "port",
-               "sample": sample + " (FP64 oracle FFT, OpenMP over the batch)"}
+               "sample": sample + " (FP64 oracle FFT, OpenMP over the batch; the reference arm's step)"}
+
+    # --- the other stated configurations, compact (one GPU only) ---
+    extras = None
+    if rank == 0 and world == 1 and not args.no_extras:
+        import bench_workloads
+        for p in plans:
+            p.destroy()
+        plans = []
+        del xs, ys, host_in, host_out
+        torch.cuda.empty_cache()
+        extras = bench_workloads.extras(peak_gbs)
 
     if rank == 0:
         line = {
@@ -498,6 +506,7 @@ def main():
                                 % E2E_CHUNKS, "results_match_device_path": bool(e2e_match)},
             "gpu_launches": gpu_launches,
             "clocks": clocks,
+            "extras": extras,
         }
         print(json.dumps(line), flush=True)
     for p in plans:

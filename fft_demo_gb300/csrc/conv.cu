@@ -29,6 +29,7 @@
 #include <new>
 
 #include "../../include/tcfft_gb300.h"
+#include "capi_internal.cuh"
 #include "conv_kernels.cuh"
 #include "qd_internal.cuh"
 #include "tables.cuh"
@@ -37,11 +38,9 @@ using namespace tcfft;
 
 namespace {
 
-thread_local tcfftStatus g_conv_last = TCFFT_OK;
-tcfftStatus cret(tcfftStatus s) {
-  g_conv_last = s;
-  return s;
-}
+// every entry point records its status (tcfft_get_last_error) and, for an
+// exec, its launch count (tcfft_last_launch_count)
+tcfftStatus cret(tcfftStatus s, int launches = 0) { return record_status(s, launches); }
 
 ConvTable g_ctab[2];  // [precision]
 int g_cocc[2][kNumConvPass][kConvMaxLogP + 1];
@@ -172,6 +171,7 @@ struct tcfftConvImpl {
   uint16_t* bmat[2] = {nullptr, nullptr};
   int* err = nullptr;
   bool filters_set = false;
+  int last_launches = 0;  // launches of the last exec (tcfft_last_launch_count)
 };
 
 namespace {
@@ -272,6 +272,49 @@ tcfftStatus conv_row_inv(tcfftConvImpl* c, const E* in, RO* out, long long count
   return conv_launch(c, kConvRowInv, 1, io, st);
 }
 
+// Fused middle pass (conv_fused.cuh): forward column FFT of the row pass's
+// output X (rows past the image zero), product with the one filter spectrum
+// K and 1/P, inverse column FFT, output rows [r0, r0 + oy) to Z.
+tcfftStatus conv_mid(tcfftConvImpl* c, const half2* X, half2* Z, long long planes, cudaStream_t st) {
+  const ConvKernel& k = g_ctab[0][kConvColMid][c->logP];
+  if (!k.fn) return TCFFT_UNSUPPORTED;
+  auto fio = zero_io<IoConvMidFwd<half2>>();
+  fio.in = X;
+  fio.total_lines = planes * c->P;
+  fio.P = c->P;
+  fio.lps_log2 = c->logP;
+  fio.valid_rows = c->sy;
+  fio.r0 = 0;
+  fio.nr = c->P;
+  fio.scale = 1.0f / static_cast<float>(c->P);
+  fio.K = static_cast<const half2*>(c->K);
+  auto iio = zero_io<IoColMaskCrop<half2>>();
+  iio.out = Z;
+  iio.total_lines = planes * c->P;
+  iio.P = c->P;
+  iio.lps_log2 = c->logP;
+  iio.valid_rows = c->P;
+  iio.r0 = c->r0;
+  iio.nr = c->oy;
+  iio.scale = 1.0f;
+  PassCore cf, ci;
+  cf.tw = c->tw[0];
+  cf.bmat = reinterpret_cast<const uint32_t*>(c->bmat[0]);
+  cf.err = c->err;
+  ci.tw = c->tw[1];
+  ci.bmat = reinterpret_cast<const uint32_t*>(c->bmat[1]);
+  ci.err = c->err;
+  const long long ntiles = (fio.total_lines + k.G - 1) / k.G;
+  long long grid = static_cast<long long>(g_conv_sms) * g_cocc[0][kConvColMid][c->logP];
+  if (grid > ntiles) grid = ntiles;
+  if (grid < 1) grid = 1;
+  void* args[] = {&fio, &iio, &cf, &ci};
+  if (cudaLaunchKernel(k.fn, dim3(static_cast<unsigned>(grid)), dim3(kPassThreads), args, static_cast<size_t>(k.smem),
+                       st) != cudaSuccess)
+    return TCFFT_LAUNCH_FAILED;
+  return TCFFT_OK;
+}
+
 template <class E, class RI>
 tcfftStatus conv_run(tcfftConvImpl* c, const RI* images, RI* out, long long batch, cudaStream_t st) {
   const float inv_p = 1.0f / static_cast<float>(c->P);
@@ -287,6 +330,17 @@ tcfftStatus conv_run(tcfftConvImpl* c, const RI* images, RI* out, long long batc
   const long long n_img_planes = pair ? (n_img + 1) / 2 : n_img;
   const long long n_out_planes = pair ? (n_out + 1) / 2 : n_out;
   tcfftStatus s = conv_row_fwd<RI, E>(c, kConvRowFwdImg, images, X, n_img, c->sy, c->sx, 0, inv_p, st, pair);
+  if constexpr (sizeof(E) == 4) {
+    // one filter: the column passes and the product run as one pass
+    // (the paired planes need no separation: Z K = X_a K + i X_b K)
+    if (c->S == 1 && c->F == 1 && g_ctab[0][kConvColMid][c->logP].fn) {
+      if (s == TCFFT_OK) s = conv_mid(c, X, Z, n_img_planes, st);
+      if (s == TCFFT_OK) s = conv_row_inv<E, RI>(c, Z, out, n_out, 1.0f, st, pair);
+      c->last_launches = 3;
+      return s;
+    }
+  }
+  c->last_launches = 5;
   if (s == TCFFT_OK) s = conv_col<E>(c, kConvColFwd, 0, X, Xf, n_img_planes, c->sy, 0, c->P, inv_p, st);
   if (s == TCFFT_OK) {
     const long long plane = static_cast<long long>(c->P) * c->P;
@@ -450,7 +504,7 @@ tcfftStatus tcfft_conv2d_exec(tcfftConv c, const void* images, void* out, long l
     s = conv_run<half2, __half>(c, static_cast<const __half*>(images), static_cast<__half*>(out), batch, st);
   else
     s = conv_run<float2, float>(c, static_cast<const float*>(images), static_cast<float*>(out), batch, st);
-  return cret(s);
+  return cret(s, s == TCFFT_OK ? c->last_launches : 0);
 }
 
 tcfftStatus tcfft_conv2d_shape(tcfftConv c, int* out_rows, int* out_cols, int* padded) {

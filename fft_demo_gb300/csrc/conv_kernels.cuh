@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "conv_fused.cuh"
 #include "conv_io.cuh"
 #include "fft_split.cuh"
 #include "fft_tile.cuh"
@@ -18,7 +19,8 @@ enum ConvPassSel : int {
   kConvColFwd = 2,      // columns, zero rows masked -> full spectrum
   kConvColInv = 3,      // columns inverse, crop rows
   kConvRowInv = 4,      // rows inverse, crop columns, real part out
-  kNumConvPass = 5
+  kConvColMid = 5,      // columns forward, times the filter spectrum, inverse, crop rows (one filter)
+  kNumConvPass = 6
 };
 
 struct ConvKernel {
@@ -55,9 +57,21 @@ ConvKernel conv_entry_split() {
   return k;
 }
 
+template <int P, int Mt>
+ConvKernel conv_entry_mid_f16() {
+  constexpr int G = Mt * 16 / P;
+  ConvKernel k;
+  k.fn = reinterpret_cast<const void*>(&conv_mid_f16<P, G, half2>);
+  k.smem = mid_smem_bytes<P, G>();
+  k.G = G;
+  k.Mt = Mt;
+  return k;
+}
+
 template <int P>
 void conv_fill_f16(ConvTable& t) {
   constexpr int LOG = ilog2c(P);
+  if constexpr (LineShape<P>::T == 1) t[kConvColMid][LOG] = conv_entry_mid_f16<P, 1024>();
   t[kConvRowFwdImg][LOG] = conv_entry_f16<P, 1024, false, -1, IoRealRowIn<__half, half2>>();
   t[kConvRowFwdFilt][LOG] = conv_entry_f16<P, 1024, false, -1, IoRealRowIn<float, half2>>();
   t[kConvColFwd][LOG] = conv_entry_f16<P, 1024, true, -1, IoColMaskCrop<half2>>();

@@ -76,6 +76,14 @@ concept TensorMapIo = requires(const IO& io) {
   io.out_map;
 };
 
+// IO policies whose last stage stays on chip: the outputs, after the
+// policy's product16 (e.g. a pointwise product), are written back into the
+// planes in natural order -- element j + c*J of line g at K row c, column
+// pos(g, j) -- which is exactly the input layout of a following transform of
+// the same tile whose length is a power of 16 (no radix-T stage).
+template <class IO>
+concept PlanesOutIo = requires { IO::TO_PLANES; };
+
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
@@ -287,7 +295,21 @@ __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const f
     uint32_t d[32];
     tmem_ld_x32(tbase + (static_cast<uint32_t>(32 * (warp & 3)) << 16) + grp * 32u, d);
     tmem_ld_wait();
-    if constexpr (LAST) {
+    if constexpr (LAST && PlanesOutIo<IO>) {
+      static_assert(Sh::T == 1, "on-chip hand-off needs a power-of-16 length");
+      const long long line = line0 + g;
+      float2 v[16];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) v[c] = make_float2(__uint_as_float(d[c]), __uint_as_float(d[16 + c]));
+      if (line < io.total_lines) {
+        io.product16(line, j, J, v);
+      } else {
+#pragma unroll
+        for (int c = 0; c < 16; ++c) v[c] = make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int c = 0; c < 16; ++c) st_pair(re, im, Tl::off(g, j + c * J), v[c]);
+    } else if constexpr (LAST) {
       // final outputs X[j + c*J] of line line0 + g
       const long long line = line0 + g;
       if (line < io.total_lines) {
@@ -537,9 +559,11 @@ __device__ __forceinline__ bool run_stages(PassState& st, const IO& io, const Pa
 }
 
 // ---------------------------------------------------------------------------
-// One tile: G lines of length L starting at line0 (FP16 storage, FP32
-// accumulation and twiddles). Returns false if a bounded wait gave up (the
-// error word is set; the caller stops and tears down).
+// Load phase of one tile: G lines of length L starting at line0 from global
+// memory into the planes re / im (the radix-T stage and the first radix-16
+// stage's twiddle applied), ending with the CTA barrier that hands the planes
+// to the tensor core. False if a bounded wait gave up (the error word is set;
+// the caller stops and tears down).
 //   L          line length
 //   G          lines per tile (G * L / 16 must be 128, 256, 512 or 1024)
 //   LINE_MINOR butterfly order in the tile (true for column passes)
@@ -547,30 +571,21 @@ __device__ __forceinline__ bool run_stages(PassState& st, const IO& io, const Pa
 //   IO         global-memory policy (see fft_io.cuh)
 // ---------------------------------------------------------------------------
 template <int L, int G, bool LINE_MINOR, int SIGN, class IO>
-__device__ __forceinline__ bool pass_tile(PassState& st, const IO& io, const PassCore& core, long long line0) {
+__device__ __forceinline__ bool tile_load(PassState& st, const IO& io, const PassCore& core, long long line0, uint8_t* re,
+                                          uint8_t* im) {
   using Sh = LineShape<L>;
   using Tl = Tile<L, G, LINE_MINOR>;
   constexpr int T = Sh::T;
-  constexpr int S = Sh::S;
   constexpr int J = Sh::J;
   constexpr int Mt = Tl::Mt;
-  constexpr int NG = Mt / 128;
-  constexpr uint32_t PLANE = Tl::PLANE;
-  constexpr uint32_t KSTRIDE = Tl::KSTRIDE;
   static_assert(Mt % 128 == 0 && Mt <= 1024, "tile size");
   static_assert(G % 4 == 0 || IO::IN_VEC_L, "line-vectorised loads need G % 4 == 0");
   static_assert(G % 4 == 0 || IO::OUT_VEC_L, "line-vectorised stores need G % 4 == 0");
-  constexpr uint32_t IDESC = make_idesc_f16_f32(128, 32, true, false);
-  uint8_t* re = st.smem + kPlaneOffset;
-  uint8_t* im = re + PLANE;
   const int tid = threadIdx.x;
-  const int warp = tid >> 5;
-  const int lane = tid & 31;
   bool timed_out = false;
   // Contiguous tiles (element (line, l) at base + line*L + l) move with bulk
   // TMA copies: one 2*PLANE-byte copy in, one out, through the tile region.
   const bool tma_in = IO::IN_VEC_L && io.in_contig;
-  const bool stage_out = IO::OUT_VEC_L && io.out_contig && !LINE_MINOR;
     const long long rem = io.total_lines - line0;
     const int nval = rem < G ? static_cast<int>(rem) : G;
 
@@ -758,14 +773,29 @@ __device__ __forceinline__ bool pass_tile(PassState& st, const IO& io, const Pas
     fence_proxy_async_smem();
     tc_fence_before_sync();
     __syncthreads();
-
-    if (!run_stages<L, G, LINE_MINOR, SIGN, IO>(st, io, core, line0, re, im, stage_out)) return false;
-    if (stage_out && tid == 0) {
-      // the last stage left the tile in natural order: one bulk store
-      bulk_s2g(io.tile_dst(line0), re, static_cast<uint32_t>(nval) * L * 4u);
-      bulk_commit();
-    }
     return true;
+}
+
+// One tile: load, the S radix-16 tensor-core stages, store (FP16 storage,
+// FP32 accumulation and twiddles). False if a bounded wait gave up.
+template <int L, int G, bool LINE_MINOR, int SIGN, class IO>
+__device__ __forceinline__ bool pass_tile(PassState& st, const IO& io, const PassCore& core, long long line0) {
+  using Tl = Tile<L, G, LINE_MINOR>;
+  uint8_t* re = st.smem + kPlaneOffset;
+  uint8_t* im = re + Tl::PLANE;
+  if (!tile_load<L, G, LINE_MINOR, SIGN, IO>(st, io, core, line0, re, im)) return false;
+  // Contiguous tiles (element (line, l) at base + line*L + l) leave by one
+  // bulk TMA store from the tile region.
+  const bool stage_out = IO::OUT_VEC_L && io.out_contig && !LINE_MINOR;
+  const long long rem = io.total_lines - line0;
+  const int nval = rem < G ? static_cast<int>(rem) : G;
+  if (!run_stages<L, G, LINE_MINOR, SIGN, IO>(st, io, core, line0, re, im, stage_out)) return false;
+  if (stage_out && threadIdx.x == 0) {
+    // the last stage left the tile in natural order: one bulk store
+    bulk_s2g(io.tile_dst(line0), re, static_cast<uint32_t>(nval) * L * 4u);
+    bulk_commit();
+  }
+  return true;
 }
 
 template <int L, int G>

@@ -223,7 +223,7 @@ def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, s
                 t_done = lane.e0.elapsed_time(ev) * 1e-3
                 for (i, off) in reqs:
                     lat[i] = t_done - wl["arrival"][i]
-                    if i % sample_every == 0:
+                    if sample_every and i % sample_every == 0:
                         samples.append((i, lane.host_out[off:off + out_elems[i]].float().numpy().copy()))
                 done += len(reqs)
         # arrivals -> per-precision waiting lines

@@ -161,3 +161,36 @@ def test_config3_same_convolution_2048(tc, orc):
     err = orc.conv_scaled_err(got[None, None], ref[None, None], xh[None, None], w[None, None])
     assert err < CONV_SCALED_FP16, (err, orc.rel_l2(got, ref))
     conv.destroy()
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+def test_one_filter_fused_column_pass(tc, orc, mode):
+    """One filter at P = 256 (a power of 16): the column transforms and the
+    product run as one pass (three launches per exec), for a batch of three
+    images -- one pair sharing a complex plane and one unpaired image."""
+    import torch
+    rng = np.random.default_rng(30 + mode)
+    side, f, B = 200, 31, 3
+    if mode == tc.CONV_VALID_CORR:
+        side = 256
+    img = rng.uniform(0, 1, (B, 1, side, side))
+    w = rng.standard_normal((1, 1, f, f))
+    w /= np.abs(w).sum()
+    conv = tc.Conv2d(1, 1, side, side, f, f, mode=mode, precision=tc.FP16, max_batch=B)
+    assert conv.padded == 256
+    conv.set_filters(torch.from_numpy(w).float().cuda())
+    out = conv.exec(torch.from_numpy(img).half().cuda())
+    assert tc.last_launch_count() == 3
+    conv.check()
+    xh = img.astype(np.float16).astype(np.float64)
+    for b in range(B):
+        if mode == tc.CONV_VALID_CORR:
+            ref = orc.corr2d_valid(xh[b], w)[0]
+        elif mode == tc.CONV_SAME:
+            ref = orc.conv2d_same(xh[b, 0], w[0, 0])
+        else:
+            ref = orc.conv2d_full(xh[b, 0], w[0])[0]
+        got = out.double().cpu().numpy()[b, 0]
+        err = orc.conv_scaled_err(got[None, None], ref[None, None], xh[b][None], w)
+        assert err < CONV_SCALED_FP16, (b, err)
+    conv.destroy()
