@@ -209,6 +209,42 @@ def cpu_fft_sample(seconds_target=12.0):
     return total_flops / total_t / 1e9, nt, "%s per step, %d steps" % (sample, reps)
 
 
+# Shapes at which the reference's own GPU kernels run (its tcfftCreate,
+# tcfftCreate_2d and fft_conv2d_half support only these families); both
+# arms time them, the reference arm with its kernels and ours in extras.
+REF_GPU_CASES = {"1d_256x4096": ("1d", 256, 4096), "2d_256x256x64": ("2d", 256, 64),
+                 "2d_512x512x16": ("2d", 512, 16), "conv_valid_128_f13_F16": ("conv", 128, 13, 16),
+                 "conv_valid_256_f13_F16": ("conv", 256, 13, 16)}
+
+
+def reference_gpu_times():
+    """The reference's own GPU kernels (its sources compiled by
+    oracle/ref_build.sh into oracle/_ref/*.cubin, _A100 wiring, launched as
+    its tcfftExec / tcfftExec_2d / conv2d_forward do) timed with CUDA events
+    at REF_GPU_CASES; ms per call."""
+    try:
+        import numpy as np
+        import torch
+        import ref_launch
+        if not torch.cuda.is_available():
+            return {"unavailable": "no GPU"}
+        if not (ref_launch.available("1d") and ref_launch.available("2d") and ref_launch.conv_available()):
+            return {"unavailable": "reference cubins not built (oracle/ref_build.sh needs the reference tree)"}
+        g = np.load(os.path.join(REPO, "tests", "golden", "reference_perm.npz"))
+        rev = {256: g["conv_rev_256"], 512: g["conv_rev_512"]}
+        out = {}
+        for name, case in REF_GPU_CASES.items():
+            if case[0] == "1d":
+                out[name] = {"ms": ref_launch.time_1d(case[1], case[2])}
+            elif case[0] == "2d":
+                out[name] = {"ms": ref_launch.time_2d(case[1], case[2])}
+            else:
+                out[name] = {"ms": ref_launch.time_conv_valid(1, case[3], case[1], case[2], rev)}
+        return out
+    except Exception as exc:  # a comparator: report, never fail the run
+        return {"unavailable": str(exc).splitlines()[0][:160]}
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return 0
@@ -235,6 +271,7 @@ def run_reference(args, world, rank):
         "cpu_baseline": {"value": value, "unit": "GFLOP/s", "cores": nt, "kind": "port",
                          "sample": sample + " per step (FP64 oracle FFT, OpenMP over the batch; FFTW absent)"},
         "e2e": {"value": value, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_gpu_kernels": reference_gpu_times(),
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -478,7 +515,7 @@ def main():
         plans = []
         del xs, ys, host_in, host_out
         torch.cuda.empty_cache()
-        extras = bench_workloads.extras(peak_gbs)
+        extras = bench_workloads.extras(peak_gbs, REF_GPU_CASES)
 
     if rank == 0:
         line = {

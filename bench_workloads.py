@@ -363,21 +363,25 @@ def uneven(peak_gbs, count=10000, nconv=512, seed=4, precisions=((tc.SPLIT_FP32,
     return {"workload": "uneven batch: 10000 1D FFTs 2^6..2^16 + 512 same convs", **out}
 
 
-def serving(peak_gbs, rate=20000.0, seconds=1.0, sweep=(40000.0, 80000.0, 160000.0), sweep_seconds=0.5):
-    """Config 5 at the offered 20k req/s, then a sweep of higher offered rates:
-    the saturation point is where the achieved rate stops following the
-    offered one."""
+def serving(peak_gbs, rate=20000.0, seconds=1.0, sweep=(8000.0, 12000.0, 16000.0, 24000.0), sweep_seconds=0.5,
+            p99_bound_ms=50.0, max_side=2048):
+    """Config 5 at the offered 20k req/s (image sides 64 .. max_side), then a
+    sweep of offered rates: the saturation rate is the largest achieved rate
+    whose p99 latency stays within p99_bound_ms."""
     from fft_demo_gb300 import serve
-    res = serve.run(rate=rate, seconds=seconds)
+    res = serve.run(rate=rate, seconds=seconds, max_side=max_side)
     out = serve.summarize(res, serve.errors(res))
     rates = []
     for r in sweep:
-        rr = serve.run(rate=r, seconds=sweep_seconds, sample_every=0)
+        rr = serve.run(rate=r, seconds=sweep_seconds, sample_every=0, max_side=max_side)
         s = serve.summarize(rr, {})
         rates.append({"offered": r, "req_per_s": s["req_per_s"], "p50_ms": s["p50_ms"], "p99_ms": s["p99_ms"]})
     out["rate_sweep"] = rates
-    return {"workload": "serving: Poisson %.0f req/s, %.1f s, 1D FFT 2^6..2^20 + same convs, FP16/split"
-            % (rate, seconds), **out}
+    ok = [x["req_per_s"] for x in rates + [{"req_per_s": out["req_per_s"], "p99_ms": out["p99_ms"]}]
+          if x["p99_ms"] <= p99_bound_ms]
+    out["saturation_req_per_s_p99_bound"] = {"p99_ms_bound": p99_bound_ms, "req_per_s": max(ok) if ok else None}
+    return {"workload": "serving: Poisson %.0f req/s, %.1f s, 1D FFT 2^6..2^20 + same convs (image sides "
+            "64..%d), FP16/split, inputs copied from host per batch" % (rate, seconds, max_side), **out}
 
 
 def large_1d_split(peak_gbs, seed=1):
@@ -415,7 +419,39 @@ def large_1d_split(peak_gbs, seed=1):
                         "FP16 over the same element counts", **res}
 
 
-def extras(peak_gbs):
+def reference_sizes(cases):
+    """Ours at the shapes the reference's GPU kernels support (bench.py
+    REF_GPU_CASES; the reference arm times its own kernels there): ms per
+    call of the same operation -- a forward 1D / 2D FP16 transform, and the
+    FP16 valid cross-correlation of one image with F filters."""
+    import torch
+    out = {}
+    for name, case in cases.items():
+        if case[0] == "1d":
+            n, b = case[1], case[2]
+            x = (torch.rand((b, n, 2), device="cuda") * 2 - 1).half()
+            y = torch.empty_like(x)
+            p = tc.plan_1d(n, b)
+            out[name] = {"ms": _timed(lambda: p.exec(x, y), 50), "launches": tc.last_launch_count()}
+        elif case[0] == "2d":
+            n, b = case[1], case[2]
+            x = (torch.rand((b, n, n, 2), device="cuda") * 2 - 1).half()
+            y = torch.empty_like(x)
+            p = tc.plan_2d(n, n, b)
+            out[name] = {"ms": _timed(lambda: p.exec(x, y), 50), "launches": tc.last_launch_count()}
+        else:
+            side, f, F = case[1], case[2], case[3]
+            img = torch.rand((1, 1, side, side), device="cuda").half()
+            w = torch.rand((F, 1, f, f), device="cuda")
+            cv = tc.Conv2d(1, F, side, side, f, f, mode=tc.CONV_VALID_CORR, precision=tc.FP16)
+            cv.set_filters(w)
+            o = cv.exec(img)
+            out[name] = {"ms": _timed(lambda: cv.exec(img, o), 50), "launches": tc.last_launch_count()}
+            cv.destroy()
+    return out
+
+
+def extras(peak_gbs, ref_cases=None):
     """Compact form of every other stated configuration, for the default
     bench line: config 1 (small), config 2 in split precision, config 3's
     convolution, config 4 (persistent vs grouped per-size, split and FP16),
@@ -443,6 +479,10 @@ def extras(peak_gbs):
         for name, r in un.items() if isinstance(r, dict)}
     sv = serving(peak_gbs)
     out["config5_serving"] = {k: v for k, v in sv.items() if k != "workload"}
+    sv = serving(peak_gbs, sweep=(20000.0, 30000.0, 40000.0, 60000.0), max_side=1024)
+    out["config5_serving_sides_to_1024"] = {k: v for k, v in sv.items() if k != "workload"}
+    if ref_cases:
+        out["reference_sizes"] = reference_sizes(ref_cases)
     out["extras_seconds"] = time.time() - t0
     return out
 

@@ -72,6 +72,7 @@ def _declare(L):
         "tcfft_queue_submit": (i, [vp, i, vp, vp, vp, vp, i, vp, vp, vp, vp, vp, vp]),
         "tcfft_queue_check": (i, [vp, vp]),
         "tcfft_queue_destroy": (i, [vp]),
+        "tcfft_copy_inputs": (i, [i, vp, vp, vp, vp, vp]),
         "tcfft_batch_set_graph": (i, [vp, i]),
         "tcfft_batch_exec": (i, [vp, vp, vp, vp]),
         "tcfft_batch_info": (i, [vp, ctypes.POINTER(i), ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(i)]),
@@ -346,6 +347,21 @@ class Batch:
             self.destroy()
         except Exception:
             pass
+
+
+def copy_inputs(host, src_off, nbytes, dst, dst_off, stream=None):
+    """Request inputs to the device (tcfft_copy_inputs): bytes
+    [src_off[i], src_off[i] + nbytes[i]) of the page-locked host tensor
+    `host` to byte offset dst_off[i] of the device tensor `dst`, one
+    asynchronous copy per input on `stream`."""
+    import numpy as np
+    src = np.ascontiguousarray(np.asarray(src_off, dtype=np.uint64) + np.uint64(host.data_ptr()))
+    nb = np.ascontiguousarray(nbytes, dtype=np.uint64)
+    do = np.ascontiguousarray(dst_off, dtype=np.uint64)
+    if len(nb) == 0:
+        return
+    _check(lib().tcfft_copy_inputs(len(nb), src.ctypes.data, nb.ctypes.data, dst.data_ptr(), do.ctypes.data,
+                                   _stream_ptr(stream)), "copy_inputs")
 
 
 class QueueConvDesc(ctypes.Structure):

@@ -68,6 +68,7 @@ struct IoRealRowIn {
   int sy, sx, P;
   long long in_image_stride;  // elements between images of `in`
   int flip;                   // 1: read w[sy-1-row][sx-1-l] (correlation filters)
+  int ld;                     // elements between rows of an image (0: sx)
   int pair;
   long long n_images;
   float scale;
@@ -75,7 +76,7 @@ struct IoRealRowIn {
   long long contig_len;
 
   __device__ __forceinline__ void load4(long long img, int row, int l0, float (&v)[4]) const {
-    const R* p = in + img * in_image_stride + static_cast<long long>(row) * sx;
+    const R* p = in + img * in_image_stride + static_cast<long long>(row) * (ld ? ld : sx);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int l = l0 + q;

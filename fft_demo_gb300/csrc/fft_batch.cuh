@@ -85,7 +85,10 @@ struct BatchConv {
   long long x_off, y_off;      // elements in the workspace
   void* kspec;                 // P x P filter spectrum (E)
   const float* filt;           // fy x fx float filter (spectrum items)
-  int sy, sx, oy, ox, r0, c0, logP, flip, fy, fx, pad0, pad1;
+  int sy, sx, oy, ox, r0, c0, logP, flip, fy, fx;
+  int ld;          // elements between image rows in conv_in (0: sx)
+  int pad0;
+  void* out_base;  // real output buffer (nullptr: the launch's conv_out)
 };
 
 struct BatchArgs {
@@ -320,6 +323,7 @@ __device__ __noinline__ bool batch_conv_item(typename BatchPrec<SPLIT>::State& s
     io.sx = cv.sx;
     io.P = L;
     io.in_image_stride = static_cast<long long>(cv.sy) * cv.sx;
+    io.ld = cv.ld;
     io.flip = 0;  // images are never flipped; correlation flips the filter
     io.scale = it.scale;
     return P::template tile<L, false, -1>(st, io, core, line0);
@@ -379,7 +383,7 @@ __device__ __noinline__ bool batch_conv_item(typename BatchPrec<SPLIT>::State& s
   }
   auto io = zeroed<IoRowCropReal<E, R>>();
   io.in = ws + cv.x_off;
-  io.out = static_cast<R*>(a.conv_out) + cv.out_off;
+  io.out = static_cast<R*>(cv.out_base ? cv.out_base : a.conv_out) + cv.out_off;
   io.total_lines = cv.oy;
   io.P = L;
   io.c0 = cv.c0;

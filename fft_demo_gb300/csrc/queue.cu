@@ -12,11 +12,21 @@
 // the GPU work of submit i. All submits of a queue share its workspace and
 // counters: use one stream per queue.
 //
+// Convolutions whose padded transform would exceed the persistent kernel's
+// largest (P > 2^kBatchMaxConvLog, e.g. a 2048 x 2048 image) run as
+// overlap-add: the image is cut into blocks of at most kBlockSide^2, each
+// block's full linear convolution (the filter rotated for a correlation) is an
+// ordinary convolution of the same launch, written to a scratch region of the
+// workspace, and one more launch sums the block outputs into the requested
+// output window (assemble_kernel).
+//
 // No counterpart in the reference, whose entry points run one plan's size
 // per call (tcfftExec, tcfft_half.cu:1177; fft_conv2d_half::conv2d_forward,
 // tensorcore_fft_conv2d.cpp:283).
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <map>
 #include <new>
@@ -29,6 +39,71 @@
 
 using namespace tcfft;
 using namespace tcfft::bh;
+
+namespace {
+
+constexpr int kBlockSide = 1024;
+
+// One overlap-add output: the window [r0, r0 + oy) x [c0, c0 + ox) of the
+// full convolution, assembled from blocks [blk0, blk0 + nblk).
+struct AsmJob {
+  long long out_off;  // real elements in conv_out
+  long long row0;     // first row of this job in the flattened row space
+  int oy, ox, r0, c0, blk0, nblk;
+};
+// One block's full convolution in the scratch region: h x w real values at
+// `off`, whose element (0, 0) is element (y0, x0) of the full convolution.
+struct AsmBlock {
+  long long off;
+  int y0, x0, h, w;
+};
+
+template <class R>
+__device__ __forceinline__ float asm_load(const R* p);
+template <>
+__device__ __forceinline__ float asm_load<__half>(const __half* p) {
+  return __half2float(*p);
+}
+template <>
+__device__ __forceinline__ float asm_load<float>(const float* p) {
+  return *p;
+}
+
+// Sum of the block outputs covering each output element (FP32), one output
+// row per CTA iteration over the rows of all jobs.
+template <class R>
+__global__ void assemble_kernel(const AsmJob* __restrict__ jobs, int njobs, const AsmBlock* __restrict__ blocks,
+                                const R* __restrict__ scratch, R* __restrict__ out, long long total_rows) {
+  for (long long row = blockIdx.x; row < total_rows; row += gridDim.x) {
+    int lo = 0, hi = njobs - 1;  // last job with row0 <= row
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) / 2;
+      if (jobs[mid].row0 <= row) lo = mid;
+      else hi = mid - 1;
+    }
+    const AsmJob jb = jobs[lo];
+    const int y = static_cast<int>(row - jb.row0);
+    const int Y = y + jb.r0;
+    R* dst = out + jb.out_off + static_cast<long long>(y) * jb.ox;
+    for (int x = threadIdx.x; x < jb.ox; x += blockDim.x) {
+      const int X = x + jb.c0;
+      float acc = 0.f;
+      for (int k = 0; k < jb.nblk; ++k) {
+        const AsmBlock b = blocks[jb.blk0 + k];
+        const int ly = Y - b.y0, lx = X - b.x0;
+        if (ly >= 0 && ly < b.h && lx >= 0 && lx < b.w)
+          acc += asm_load<R>(scratch + b.off + static_cast<long long>(ly) * b.w + lx);
+      }
+      if constexpr (sizeof(R) == 2) {
+        dst[x] = __float2half_rn(acc);
+      } else {
+        dst[x] = acc;
+      }
+    }
+  }
+}
+
+}  // namespace
 
 struct tcfftQueueImpl {
   int precision = TCFFT_FP16;
@@ -207,29 +282,78 @@ tcfftStatus tcfft_queue_submit(tcfftQueue q, int count, const long long* n, cons
   spec.scale = scale;
   // convolutions: geometry and spectra (a new (filter, P) spectrum is made
   // by this submit's first launch)
-  for (int c = 0; c < nconv; ++c) {
-    const tcfftQueueConv& r = convs[c];
-    auto fit = q->filters.find(r.filter_id);
-    if (fit == q->filters.end()) return record_status(TCFFT_INVALID_VALUE, 0);
-    tcfftBatchConv d{r.sy, r.sx, fit->second.fy, fit->second.fx, r.mode, r.img_off, r.out_off, 0};
-    BatchConv cv{};
-    if (r.sy < 1 || r.sx < 1 || !conv_geometry(d, cv)) return record_status(TCFFT_INVALID_SIZE, 0);
-    if (r.img_off < 0 || r.out_off < 0) return record_status(TCFFT_INVALID_VALUE, 0);
-    cv.img_off = r.img_off;
-    cv.out_off = r.out_off;
-    cv.filt = fit->second.dev;
+  // the spectrum of a filter for a padded size and orientation, made by this
+  // submit's first launch when it is new
+  auto add_conv = [&](BatchConv cv, tcfftQueueImpl::Filter& flt) -> tcfftStatus {
+    cv.filt = flt.dev;
     const auto key = std::make_pair(cv.logP, cv.flip);
     char prep = 0;
-    auto sit = fit->second.spec.find(key);
-    if (sit == fit->second.spec.end()) {
+    auto sit = flt.spec.find(key);
+    if (sit == flt.spec.end()) {
       void* k = nullptr;
-      if (cudaMalloc(&k, q->eb << (2 * cv.logP)) != cudaSuccess) return record_status(TCFFT_ALLOC_FAILED, 0);
-      sit = fit->second.spec.emplace(key, k).first;
+      if (cudaMalloc(&k, q->eb << (2 * cv.logP)) != cudaSuccess) return TCFFT_ALLOC_FAILED;
+      sit = flt.spec.emplace(key, k).first;
       prep = 1;
     }
     cv.kspec = sit->second;
     spec.convs.push_back(cv);
     spec.conv_prep.push_back(prep);
+    return TCFFT_OK;
+  };
+  std::vector<AsmJob> jobs;
+  std::vector<AsmBlock> blocks;
+  std::vector<size_t> block_conv;  // index in spec.convs of each block
+  long long scratch_elems = 0, asm_rows = 0;
+  for (int c = 0; c < nconv; ++c) {
+    const tcfftQueueConv& r = convs[c];
+    auto fit = q->filters.find(r.filter_id);
+    if (fit == q->filters.end()) return record_status(TCFFT_INVALID_VALUE, 0);
+    if (r.img_off < 0 || r.out_off < 0 || r.sy < 1 || r.sx < 1) return record_status(TCFFT_INVALID_VALUE, 0);
+    const int fy = fit->second.fy, fx = fit->second.fx;
+    tcfftBatchConv d{r.sy, r.sx, fy, fx, r.mode, r.img_off, r.out_off, 0};
+    BatchConv cv{};
+    if (conv_geometry(d, cv)) {
+      cv.img_off = r.img_off;
+      cv.out_off = r.out_off;
+      const tcfftStatus s = add_conv(cv, fit->second);
+      if (s != TCFFT_OK) return record_status(s, 0);
+      continue;
+    }
+    // too large for one transform (or an invalid request, rejected below):
+    // overlap-add of blocks, the window of the requested mode inside the
+    // full convolution
+    int oy, ox, r0, c0;
+    if (r.mode == TCFFT_CONV_VALID_CORR) {
+      if (fy > r.sy || fx > r.sx) return record_status(TCFFT_INVALID_SIZE, 0);
+      oy = r.sy - fy + 1, ox = r.sx - fx + 1, r0 = fy - 1, c0 = fx - 1;
+    } else if (r.mode == TCFFT_CONV_SAME) {
+      if (fy % 2 == 0 || fx % 2 == 0) return record_status(TCFFT_INVALID_SIZE, 0);
+      oy = r.sy, ox = r.sx, r0 = (fy - 1) / 2, c0 = (fx - 1) / 2;
+    } else if (r.mode == TCFFT_CONV_FULL) {
+      oy = r.sy + fy - 1, ox = r.sx + fx - 1, r0 = 0, c0 = 0;
+    } else {
+      return record_status(TCFFT_INVALID_VALUE, 0);
+    }
+    AsmJob jb{r.out_off, asm_rows, oy, ox, r0, c0, static_cast<int>(blocks.size()), 0};
+    for (int by0 = 0; by0 < r.sy; by0 += kBlockSide)
+      for (int bx0 = 0; bx0 < r.sx; bx0 += kBlockSide) {
+        const int bh = std::min(kBlockSide, r.sy - by0), bw = std::min(kBlockSide, r.sx - bx0);
+        BatchConv b{};
+        if (!conv_geometry(tcfftBatchConv{bh, bw, fy, fx, TCFFT_CONV_FULL, 0, 0, 0}, b))
+          return record_status(TCFFT_INVALID_SIZE, 0);
+        b.flip = r.mode == TCFFT_CONV_VALID_CORR ? 1 : 0;  // correlation: the rotated filter
+        b.img_off = r.img_off + static_cast<long long>(by0) * r.sx + bx0;
+        b.ld = r.sx;
+        b.out_off = scratch_elems;  // relative to the scratch region, set below
+        blocks.push_back(AsmBlock{scratch_elems, by0, bx0, b.oy, b.ox});
+        block_conv.push_back(spec.convs.size());
+        scratch_elems += static_cast<long long>(b.oy) * b.ox;
+        const tcfftStatus s = add_conv(b, fit->second);
+        if (s != TCFFT_OK) return record_status(s, 0);
+        ++jb.nblk;
+      }
+    jobs.push_back(jb);
+    asm_rows += oy;
   }
   // one prep pass per new spectrum, even if several requests share it
   for (size_t j = 0; j < spec.convs.size(); ++j)
@@ -237,8 +361,14 @@ tcfftStatus tcfft_queue_submit(tcfftQueue q, int count, const long long* n, cons
       if (spec.conv_prep[i] && spec.convs[i].kspec == spec.convs[j].kspec) spec.conv_prep[j] = 0;
   const int ctas = batch_ctas(q->pr, 0);
   Built bl = build_items(spec, 2 * ctas);
-  if (bl.ws_elems > q->ws_elems || static_cast<size_t>(bl.nctrs) > q->ctr_cap)
+  // scratch for the overlap-add blocks after the items' workspace (real
+  // elements, half the size of a complex one)
+  const size_t scratch_at = align_up(bl.ws_elems * q->eb, 256);
+  const size_t scratch_bytes = static_cast<size_t>(scratch_elems) * (q->eb / 2);
+  if (scratch_at + scratch_bytes > q->ws_elems * q->eb || static_cast<size_t>(bl.nctrs) > q->ctr_cap)
     return record_status(TCFFT_CAPACITY, 0);
+  unsigned char* scratch = static_cast<unsigned char*>(q->ws) + scratch_at;
+  for (size_t k = 0; k < block_conv.size(); ++k) bl.convs[block_conv[k]].out_base = scratch;
   // work lists -> staging slot
   size_t at = 0;
   auto place = [&](size_t bytes) {
@@ -252,6 +382,8 @@ tcfftStatus tcfft_queue_submit(tcfftQueue q, int count, const long long* n, cons
   const size_t o_prep = place(sizeof(BatchItem) * bl.prep_items.size());
   const size_t o_xf = place(sizeof(BatchXform) * bl.xforms.size());
   const size_t o_cv = place(sizeof(BatchConv) * bl.convs.size());
+  const size_t o_jobs = place(sizeof(AsmJob) * jobs.size());
+  const size_t o_blocks = place(sizeof(AsmBlock) * blocks.size());
   if (at > q->slot_bytes) return record_status(TCFFT_CAPACITY, 0);
   tcfftQueueImpl::Slot& sl = q->slot[q->cur];
   if (sl.pending && cudaEventSynchronize(sl.ev) != cudaSuccess) return record_status(TCFFT_LAUNCH_FAILED, 0);
@@ -265,6 +397,8 @@ tcfftStatus tcfft_queue_submit(tcfftQueue q, int count, const long long* n, cons
   put(o_prep, bl.prep_items.data(), sizeof(BatchItem) * bl.prep_items.size());
   put(o_xf, bl.xforms.data(), sizeof(BatchXform) * bl.xforms.size());
   put(o_cv, bl.convs.data(), sizeof(BatchConv) * bl.convs.size());
+  put(o_jobs, jobs.data(), sizeof(AsmJob) * jobs.size());
+  put(o_blocks, blocks.data(), sizeof(AsmBlock) * blocks.size());
   if (cudaMemcpyAsync(sl.dev, sl.host, at, cudaMemcpyHostToDevice, st) != cudaSuccess)
     return record_status(TCFFT_LAUNCH_FAILED, 0);
   BatchArgs a = q->base;
@@ -294,6 +428,21 @@ tcfftStatus tcfft_queue_submit(tcfftQueue q, int count, const long long* n, cons
   };
   if (!bl.prep_items.empty() && !launch(o_prep, bl.prep_items.size())) return record_status(TCFFT_LAUNCH_FAILED, 0);
   if (!bl.items.empty() && !launch(o_items, bl.items.size())) return record_status(TCFFT_LAUNCH_FAILED, launches);
+  if (!jobs.empty()) {
+    const unsigned grid = static_cast<unsigned>(std::min<long long>(asm_rows, 8192));
+    const AsmJob* dj = reinterpret_cast<const AsmJob*>(sl.dev + o_jobs);
+    const AsmBlock* db = reinterpret_cast<const AsmBlock*>(sl.dev + o_blocks);
+    if (q->precision == TCFFT_FP16)
+      assemble_kernel<__half><<<grid, 256, 0, st>>>(dj, static_cast<int>(jobs.size()), db,
+                                                    reinterpret_cast<const __half*>(scratch),
+                                                    static_cast<__half*>(conv_out), asm_rows);
+    else
+      assemble_kernel<float><<<grid, 256, 0, st>>>(dj, static_cast<int>(jobs.size()), db,
+                                                   reinterpret_cast<const float*>(scratch),
+                                                   static_cast<float*>(conv_out), asm_rows);
+    if (cudaGetLastError() != cudaSuccess) return record_status(TCFFT_LAUNCH_FAILED, launches);
+    ++launches;
+  }
   if (cudaEventRecord(sl.ev, st) != cudaSuccess) return record_status(TCFFT_LAUNCH_FAILED, launches);
   sl.pending = true;
   q->cur ^= 1;
@@ -315,6 +464,18 @@ tcfftStatus tcfft_queue_check(tcfftQueue q, void* stream) {
 tcfftStatus tcfft_queue_destroy(tcfftQueue q) {
   if (!q) return record_status(TCFFT_INVALID_VALUE, 0);
   free_queue(q);
+  return record_status(TCFFT_OK, 0);
+}
+
+tcfftStatus tcfft_copy_inputs(int count, const void* const* src, const size_t* bytes, void* dst_base,
+                              const size_t* dst_off, void* stream) {
+  if (count < 0 || (count > 0 && (!src || !bytes || !dst_base || !dst_off)))
+    return record_status(TCFFT_INVALID_VALUE, 0);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned char* dst = static_cast<unsigned char*>(dst_base);
+  for (int i = 0; i < count; ++i)
+    if (bytes[i] && cudaMemcpyAsync(dst + dst_off[i], src[i], bytes[i], cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return record_status(TCFFT_LAUNCH_FAILED, 0);
   return record_status(TCFFT_OK, 0);
 }
 

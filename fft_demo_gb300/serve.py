@@ -2,11 +2,15 @@
 
 Requests arrive as a Poisson stream and mix forward 1D FFTs (n = 2^k, k
 uniform on [6, 20]) and 'same'-mode 2D convolutions (square images, sides
-log-uniform over 64 .. 1024, filters from a resident pool of 64 with odd
-sides 3 .. 63), FP16 and split precision interleaved at random. Request
-inputs are resident in HBM (a pool of seeded payloads per size, as if an
-upstream GPU stage produced them); every batch's outputs are copied to
-pinned host memory, and a request completes when that copy has.
+log-uniform over the powers of two 64 .. 2048, filters from a resident pool
+of 64 with odd sides 3 .. 63), FP16 and split precision interleaved at
+random. Request inputs come from page-locked host memory (a pool of seeded
+payloads per size): every batch first copies its requests' inputs to the
+device (one asynchronous copy per request, tcfft_copy_inputs), and its
+outputs are copied back to page-locked host memory; a request completes when
+that copy has, so both copies are inside the latency. 2048-side images need
+a padded size of 4096, beyond the persistent kernel's largest; the queue
+runs them as overlap-add of four 1024-side blocks (one more launch).
 
 Each loop turn, per precision, the requests that have arrived are admitted
 in arrival order while they fit the device budget (an output ring and the
@@ -37,26 +41,49 @@ import numpy as np
 import fft_demo_gb300 as tc
 
 KMIN, KMAX = 6, 20
-IMAGE_SIDES = (64, 128, 256, 512, 1024)
+IMAGE_SIDES = (64, 128, 256, 512, 1024, 2048)
 N_FILTERS = 64
+MAX_P = 2048      # largest padded size of the persistent kernel
+BLOCK_SIDE = 1024  # overlap-add block side of the queue for larger images
 
 
-def conv_padded(s, f):
-    need = s + (f - 1) // 2
-    p = 64
-    while p < need:
+def _pow2_at_least(v, lo=64):
+    p = lo
+    while p < v:
         p *= 2
     return p
 
 
-def make_workload(seed, rate, seconds, conv_fraction=0.5):
+def conv_padded(s, f):
+    return _pow2_at_least(s + (f - 1) // 2)
+
+
+def conv_parts(s, f):
+    """The transforms the queue runs for an s x s 'same' convolution with an
+    f x f filter: [(rows, P)] per part, rows = the larger of the part's input
+    and output rows -- one part, or overlap-add blocks of at most BLOCK_SIDE
+    (full convolutions) when P would exceed MAX_P."""
+    p = conv_padded(s, f)
+    if p <= MAX_P:
+        return [(max(s, f), p)]
+    nb = -(-s // BLOCK_SIDE)
+    out = []
+    for by in range(nb):
+        for bx in range(nb):
+            h = min(BLOCK_SIDE, s - by * BLOCK_SIDE)
+            w = min(BLOCK_SIDE, s - bx * BLOCK_SIDE)
+            out.append((h + f - 1, _pow2_at_least(max(h, w) + f - 1)))
+    return out
+
+
+def make_workload(seed, rate, seconds, conv_fraction=0.5, sides=IMAGE_SIDES):
     rng = np.random.default_rng(seed)
     count = int(rate * seconds)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, count))
     is_conv = rng.random(count) < conv_fraction
     prec = np.where(rng.random(count) < 0.5, tc.FP16, tc.SPLIT_FP32)
     k = rng.integers(KMIN, KMAX + 1, count)
-    side = rng.choice(IMAGE_SIDES, count)
+    side = rng.choice(sides, count)
     fid = rng.integers(0, N_FILTERS, count)
     return {"arrival": arrivals, "conv": is_conv, "prec": prec, "k": k, "side": side, "fid": fid}
 
@@ -73,8 +100,8 @@ def make_filters(seed):
 
 def request_flops(wl, i, filters):
     if wl["conv"][i]:
-        p = conv_padded(int(wl["side"][i]), filters[wl["fid"][i]].shape[0])
-        return 2 * 5 * p * p * math.log2(p * p) + 6 * p * p
+        return sum(2 * 5 * p * p * math.log2(p * p) + 6 * p * p
+                   for _, p in conv_parts(int(wl["side"][i]), filters[wl["fid"][i]].shape[0]))
     n = 1 << int(wl["k"][i])
     return 5 * n * math.log2(n)
 
@@ -103,7 +130,7 @@ def lane_limit(lane, first_need):
 class Lane:
     """One precision: its queue, input pools, output ring and in-flight batches."""
 
-    def __init__(self, prec, filters, seed, ring_bytes, ws_bytes, staging_bytes, pool_per_size):
+    def __init__(self, prec, filters, seed, ring_bytes, ws_bytes, staging_bytes, pool_per_size, sides=IMAGE_SIDES):
         import torch
         self.prec = prec
         self.eb = 4 if prec == tc.FP16 else 8  # complex element bytes
@@ -113,7 +140,8 @@ class Lane:
             self.q.set_filter(i, w)
         self.ws_bytes = ws_bytes
         rng = np.random.default_rng(seed)
-        # input pools, one device arena: 1D complex payloads and real images
+        # input pools in one page-locked host arena: 1D complex payloads and
+        # real images
         self.pool = {}
         chunks, at = [], 0
         for kk in range(KMIN, KMAX + 1):
@@ -123,18 +151,20 @@ class Lane:
                 self.pool[("fft", kk, j)] = (at, a)
                 chunks.append(a.ravel())
                 at += a.size
-        for s in IMAGE_SIDES:
+        for s in sides:
             for j in range(pool_per_size):
                 a = rng.uniform(0, 1, (s, s)).astype(np.float32)
                 self.pool[("img", s, j)] = (at, a)
                 chunks.append(a.ravel())
                 at += a.size
-        self.arena = torch.from_numpy(np.concatenate(chunks)).to(self.dt).cuda()
-        # host copies of the payloads as rounded to the storage type (oracle input)
-        host = self.arena.float().cpu().numpy()
+        self.host_in = torch.from_numpy(np.concatenate(chunks)).to(self.dt).pin_memory()
+        # the payloads as rounded to the storage type (reference input)
+        host = self.host_in.float().numpy()
         self.pool = {key: (off, host[off:off + a.size].reshape(a.shape)) for key, (off, a) in self.pool.items()}
         self.ring_elems = ring_bytes // (self.eb // 2)  # in real elements of the storage type
         self.ring = torch.empty(self.ring_elems, dtype=self.dt, device="cuda")
+        # device inputs: request i's input sits at the offset its output has in `ring`
+        self.in_ring = torch.empty(self.ring_elems, dtype=self.dt, device="cuda")
         self.host_out = torch.empty(self.ring_elems, dtype=self.dt, pin_memory=True)
         self.head = 0       # next free real element of the ring
         self.inflight = collections.deque()  # (event, ring_start, ring_end, requests)
@@ -142,21 +172,24 @@ class Lane:
 
 
 def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, sample_every=97,
-        pool_per_size=2, max_batch=1024, verbose=False):
+        pool_per_size=2, max_batch=1024, verbose=False, max_side=IMAGE_SIDES[-1]):
+    """One Poisson stream; max_side limits the image sides drawn (the stated
+    mix is 64 .. 2048)."""
     import torch
     filters = make_filters(seed)
-    wl = make_workload(seed, rate, seconds, conv_fraction)
+    sides = tuple(x for x in IMAGE_SIDES if x <= max_side)
+    wl = make_workload(seed, rate, seconds, conv_fraction, sides)
     nreq = len(wl["arrival"])
     cap = int(hbm_cap_gb * (1 << 30))
     # HBM budget inside the cap: per precision an output ring and a workspace;
     # the input pools and filter spectra are counted against it too
     ws_bytes = min(6 << 30, cap // 8)
     ring_bytes = min(6 << 30, cap // 8)
-    lanes = {p: Lane(p, filters, seed + 10 * p, ring_bytes, ws_bytes, 16 << 20, pool_per_size)
+    lanes = {p: Lane(p, filters, seed + 10 * p, ring_bytes, ws_bytes, 16 << 20, pool_per_size, sides)
              for p in (tc.FP16, tc.SPLIT_FP32)}
-    spectra = sum(N_FILTERS * sum(conv_padded(s, 63) ** 2 for s in IMAGE_SIDES) * l.eb for l in lanes.values())
-    resident = spectra + sum(l.arena.numel() * l.arena.element_size() + ring_bytes + ws_bytes
-                             for l in lanes.values())
+    spectra = sum(N_FILTERS * sum(max(p for _, p in conv_parts(s, 63)) ** 2 for s in sides) * l.eb
+                  for l in lanes.values())
+    resident = spectra + sum(2 * ring_bytes + ws_bytes for _ in lanes.values())
     if resident > cap:
         raise RuntimeError("device budget %.1f GB exceeds the %.1f GB cap" % (resident / 1e9, cap / 1e9))
     # per-request device footprint: output + workspace
@@ -166,37 +199,42 @@ def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, s
         if wl["conv"][i]:
             s = int(wl["side"][i])
             f = filters[wl["fid"][i]].shape[0]
-            p = conv_padded(s, f)
+            parts = conv_parts(s, f)
             out_elems[i] = s * s
-            ws_elems[i] = (max(s, f) + p) * p
+            # per part: rows x P and P x P complex; overlap-add blocks add
+            # their real full outputs as scratch
+            ws_elems[i] = sum((rows + p) * p for rows, p in parts)
+            if len(parts) > 1:
+                ws_elems[i] += sum(rows * rows for rows, _ in parts) // 2 + 64 * len(parts)
         else:
             n = 1 << int(wl["k"][i])
             out_elems[i] = 2 * n
             ws_elems[i] = n if n > 8192 else 0
+    out_elems_raw = out_elems.copy()  # the request's own size, copied in
     out_elems = (out_elems + 63) // 64 * 64  # 128-byte alignment for FP16, 256 for split
     # work items of the persistent launch per request (tiles of 8192 points)
     items_est = np.zeros(nreq, np.int64)
     for i in range(nreq):
         if wl["conv"][i]:
             s_ = int(wl["side"][i])
-            p_ = conv_padded(s_, filters[wl["fid"][i]].shape[0])
-            items_est[i] = (2 * s_ + 2 * p_) * p_ // 8192 + 8
+            items_est[i] = sum((2 * rows + 2 * p_) * p_ // 8192 + 8
+                               for rows, p_ in conv_parts(s_, filters[wl["fid"][i]].shape[0]))
         else:
             items_est[i] = 2 * (1 << int(wl["k"][i])) // 8192 + 1
     # warm-up: every filter spectrum per padded size, and the kernel
     for lane in lanes.values():
-        convs = []
-        at = 0
+        es = lane.eb // 2
         for fidx, w in enumerate(filters):
-            for s in IMAGE_SIDES:
-                convs.append((s, s, fidx, tc.CONV_SAME, lane.pool[("img", s, 0)][0], at))
+            # one submit per filter (workspace limit): every image side, the
+            # inputs copied from the host pool like a request's
+            convs, src, nb, at = [], [], [], 0
+            for s in sides:
+                convs.append((s, s, fidx, tc.CONV_SAME, at, at))
+                src.append(lane.pool[("img", s, 0)][0] * es)
+                nb.append(s * s * es)
                 at += s * s
-        # in several submits (workspace limit)
-        for j in range(0, len(convs), 16):
-            part = convs[j:j + 16]
-            base = part[0][5]
-            part = [(a, b, c, d, e, f - base) for (a, b, c, d, e, f) in part]
-            lane.q.submit(convs=part, conv_in=lane.arena, conv_out=lane.ring, stream=lane.stream)
+            tc.copy_inputs(lane.host_in, src, nb, lane.in_ring, [c[4] * es for c in convs], stream=lane.stream)
+            lane.q.submit(convs=convs, conv_in=lane.in_ring, conv_out=lane.ring, stream=lane.stream)
         lane.q.check(lane.stream)
     torch.cuda.synchronize()
 
@@ -257,12 +295,17 @@ def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, s
                 continue
             ffts = [(i, off) for (i, off) in reqs if not wl["conv"][i]]
             cvs = [(i, off) for (i, off) in reqs if wl["conv"][i]]
+            # inputs host -> device, each to the offset of its output
+            es = lane.eb // 2
+            src = [lane.pool[("fft", int(wl["k"][i]), i % pool_per_size)][0] * es if not wl["conv"][i] else
+                   lane.pool[("img", int(wl["side"][i]), i % pool_per_size)][0] * es for i, _ in reqs]
+            tc.copy_inputs(lane.host_in, src, [int(out_elems_raw[i]) * es for i, _ in reqs], lane.in_ring,
+                           [off * es for _, off in reqs], stream=lane.stream)
             n = [1 << int(wl["k"][i]) for i, _ in ffts]
-            in_off = [lane.pool[("fft", int(wl["k"][i]), i % pool_per_size)][0] // 2 for i, _ in ffts]
-            out_off = [off // 2 for _, off in ffts]
-            convs = [(int(wl["side"][i]), int(wl["side"][i]), int(wl["fid"][i]), tc.CONV_SAME,
-                      lane.pool[("img", int(wl["side"][i]), i % pool_per_size)][0], off) for i, off in cvs]
-            lane.q.submit(n, in_off, out_off, convs, lane.arena, lane.ring, lane.arena, lane.ring,
+            io_off = [off // 2 for _, off in ffts]
+            convs = [(int(wl["side"][i]), int(wl["side"][i]), int(wl["fid"][i]), tc.CONV_SAME, off, off)
+                     for i, off in cvs]
+            lane.q.submit(n, io_off, io_off, convs, lane.in_ring, lane.ring, lane.in_ring, lane.ring,
                           stream=lane.stream)
             launches += tc.last_launch_count()
             with torch.cuda.stream(lane.stream):
@@ -349,8 +392,9 @@ def main():
     ap.add_argument("--seed", type=int, default=5)
     ap.add_argument("--conv-fraction", type=float, default=0.5)
     ap.add_argument("--hbm-cap-gb", type=float, default=60.0)
+    ap.add_argument("--max-side", type=int, default=IMAGE_SIDES[-1])
     args = ap.parse_args()
-    res = run(args.rate, args.seconds, args.seed, args.conv_fraction, args.hbm_cap_gb)
+    res = run(args.rate, args.seconds, args.seed, args.conv_fraction, args.hbm_cap_gb, max_side=args.max_side)
     out = summarize(res, errors(res))
     out.update({"rate": args.rate, "seconds": args.seconds, "conv_fraction": args.conv_fraction,
                 "hbm_cap_gb": args.hbm_cap_gb})

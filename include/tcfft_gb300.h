@@ -236,12 +236,17 @@ tcfftStatus tcfft_batch_destroy(tcfftBatch batch);
 /* ------------------------------------------------------------------------
  * Serving queue (no counterpart in the reference): continuous batching of
  * forward 1D FFTs (64 <= n <= 2^20) and 2D convolutions (filters from a
- * resident pool, padded size <= 2048) into the persistent batch kernel.
+ * resident pool) into the persistent batch kernel.
  * Tables, the filter pool and its spectra (made per padded size on first
  * use), a workspace arena of workspace_bytes and two staging slots of
  * staging_bytes stay resident; a submit builds the work list on the host,
  * copies it with one async copy and launches once (twice when a filter
- * spectrum is new). Submits share the workspace: one stream per queue.
+ * spectrum is new). A convolution whose padded size would exceed 2048 (an
+ * image side above ~2000) runs as overlap-add: its image is cut into blocks
+ * of at most 1024 x 1024 whose full convolutions are items of the same
+ * launch (padded size 2048 for filters up to 1025), written to workspace
+ * scratch, and one more launch sums them into the requested window.
+ * Submits share the workspace: one stream per queue.
  * TCFFT_CAPACITY: the submit needs more workspace or staging; split it.
  * ------------------------------------------------------------------------ */
 typedef struct tcfftQueueImpl *tcfftQueue;
@@ -258,6 +263,12 @@ tcfftStatus tcfft_queue_submit(tcfftQueue queue, int count, const long long *n, 
                                void *conv_out, void *stream);
 tcfftStatus tcfft_queue_check(tcfftQueue queue, void *stream);
 tcfftStatus tcfft_queue_destroy(tcfftQueue queue);
+/* Request inputs from the host: copies src[i] (bytes[i] bytes of host
+ * memory, page-locked for the copy to be asynchronous) to
+ * dst_base + dst_off[i] (bytes) on the device, one cudaMemcpyAsync per input
+ * on `stream`, so a submit on the same stream reads them. */
+tcfftStatus tcfft_copy_inputs(int count, const void *const *src, const size_t *bytes, void *dst_base,
+                              const size_t *dst_off, void *stream);
 
 /* Bound of the dependency waits inside the persistent kernels (the fused
  * four-step launch, tcfft_exec_static, the uneven-batch and serving

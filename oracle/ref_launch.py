@@ -250,3 +250,128 @@ def run_conv_valid(signal, filters, rev_tables):
              [ptr(padded), ptr(out), I(P), I(P), I(ox), I(oy), I(fx), ctypes.c_double(scale)])
     torch.cuda.synchronize()
     return out.cpu().numpy().reshape(F, oy, ox)
+
+
+# ---------------------------------------------------------------------------
+# Timing of the reference's own GPU kernels (the bench's reference arm)
+# ---------------------------------------------------------------------------
+def _events_ms(fn, reps=20, warm=3):
+    import torch
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def time_1d(n, batch, reps=20):
+    """ms per tcfftExec (tcfft_half.cu:1177) of the _A100 wiring for the one-
+    launch sizes (256, 512, 1024), batch sequences."""
+    import torch
+    d = driver()
+    cubin = os.path.join(REF_DIR, "ref_tcfft1d.cubin")
+    m0 = {256: 0, 512: 1, 1024: 2}[n]
+    data = (torch.rand(batch * n * 2, device="cuda") * 2 - 1).half()
+    fr, fi = dft16_tables()
+    f_re = torch.from_numpy(fr.ravel().copy()).cuda()
+    f_im = torch.from_numpy(fi.ravel().copy()).cuda()
+    args = [ctypes.c_void_p(data.data_ptr()), ctypes.c_void_p(f_re.data_ptr()), ctypes.c_void_p(f_im.data_ptr())]
+    fn = d.function(cubin, mangled(L0[m0], "A100", N_CONT[m0], False))
+    cont = N_CONT[m0]
+    return _events_ms(lambda: d.launch(fn, (n * batch // cont // RADIX[m0], 1), (32, 8), RADIX[m0] * 4 * cont, args),
+                      reps)
+
+
+def time_2d(n, batch, reps=20):
+    """ms per tcfftExec_2d (tcfft_half_2d.cu:1128) of an n x n plan (256 or 512)."""
+    import torch
+    d = driver()
+    cubin = os.path.join(REF_DIR, "ref_tcfft2d.cubin")
+    m = {256: 0, 512: 1}[n]
+    data = (torch.rand(batch * n * n * 2, device="cuda") * 2 - 1).half()
+    fr, fi = dft16_tables()
+    f_re = torch.from_numpy(fr.ravel().copy()).cuda()
+    f_im = torch.from_numpy(fi.ravel().copy()).cuda()
+    p = [ctypes.c_void_p(data.data_ptr()), ctypes.c_void_p(f_re.data_ptr()), ctypes.c_void_p(f_im.data_ptr())]
+    f0 = d.function(cubin, mangled(L0[m], "A100", N_CONT[m], False))
+    f1 = d.function(cubin, mangled(L1[m], "A100", N_CONT[m], True))
+    cont = N_CONT[m]
+
+    def run():
+        d.launch(f0, (n * n * batch // cont // n, 1), (32, 8), n * 4 * cont, p)
+        d.launch(f1, (n // cont, n * n * batch // n // n), (32, 8), n * 4 * cont, [ctypes.c_int(n)] + p)
+
+    return _events_ms(run, reps)
+
+
+def time_conv_valid(S, F, side, f, rev_tables, reps=10):
+    """ms per fft_conv2d_half(signal, filter, ...) + conv2d_forward(output)
+    on the device: the constructor's flip, pad and two forward transforms
+    (the reference transforms its filters on every construction), the
+    pointwise product, quantisation, inverse transform, dequantisation and
+    read-out -- the launch sequence of run_conv_valid, without its host
+    allocations, copies and synchronisations."""
+    import torch
+    d = driver()
+    cubin = os.path.join(REF_DIR, CONV_CUBIN)
+    P = 256 if side + f - 1 <= 256 else 512
+    oy = side - f + 1
+    dev = torch.device("cuda")
+    cu_signal = torch.rand(S * side * side, dtype=torch.float64, device=dev)
+    cu_filter = torch.rand(F * S * f * f, dtype=torch.float64, device=dev)
+    sig_pad = torch.zeros(S * P * P * 2, dtype=torch.float16, device=dev)
+    filt_pad = torch.zeros(F * S * P * P * 2, dtype=torch.float16, device=dev)
+    rev = torch.zeros(1024, dtype=torch.int32, device=dev)
+    rev[:P] = torch.from_numpy(np.asarray(rev_tables[P], dtype=np.int32))
+    pw_f = torch.zeros(F * P * P * 2, dtype=torch.float32, device=dev)
+    pw_h = torch.zeros(F * P * P * 2, dtype=torch.float16, device=dev)
+    max_line = torch.zeros(F * P, dtype=torch.float32, device=dev)
+    max_tile = torch.zeros(F, dtype=torch.float32, device=dev)
+    padded = torch.zeros(F * P * P * 2, dtype=torch.float64, device=dev)
+    out = torch.zeros(F * oy * oy, dtype=torch.float64, device=dev)
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    I = ctypes.c_int  # noqa: E741
+    k = {name: d.function(cubin, sym) for name, sym in _CONV_K.items()}
+    m = {256: 0, 512: 1}[P]
+    cont = N_CONT[m]
+    stage = {}
+    tables = {}
+    for fft in (1, -1):
+        fr, fi = dft16_tables(sign=-1 if fft == 1 else 1)
+        tables[fft] = (torch.from_numpy(fr.ravel().copy()).cuda(), torch.from_numpy(fi.ravel().copy()).cuda())
+        stage[fft] = (d.function(cubin, _conv_stage(L0[m], m, False)), d.function(cubin, _conv_stage(L1[m], m, True)))
+
+    def exec2d(t, batch, fft):
+        f0, f1 = stage[fft]
+        fr, fi = tables[fft]
+        p = [ptr(t), ptr(fr), ptr(fi)]
+        d.launch(f0, (P * P * batch // cont // P, 1), (32, 8), P * 4 * cont, p + [I(fft)])
+        d.launch(f1, (P // cont, batch), (32, 8), P * 4 * cont, [I(P)] + p + [I(fft)])
+
+    scale = float(np.float32(1.0) / np.float32(P * P))
+
+    def run():
+        d.launch(k["inv"], (F * S, f // 2), (f, 1), 0, [ptr(cu_filter), I(f), I(f)])
+        if f & 1 and f // 2 > 0:
+            d.launch(k["inv_odd"], (F * S, 1), (f // 2, 1), 0, [ptr(cu_filter), I(f), I(f)])
+        d.launch(k["pad"], (S, P), (P, 1), 0, [ptr(cu_signal), ptr(sig_pad), ptr(rev), ptr(rev), I(P), I(P), I(side),
+                                                I(side)])
+        d.launch(k["pad"], (F * S, P), (P, 1), 0, [ptr(cu_filter), ptr(filt_pad), ptr(rev), ptr(rev), I(P), I(P),
+                                                    I(f), I(f)])
+        exec2d(sig_pad, S, 1)
+        exec2d(filt_pad, F * S, 1)
+        d.launch(k["mul_add"], (F, P), (P, 1), 0, [ptr(sig_pad), ptr(filt_pad), ptr(pw_f), I(S), I(F), I(P), I(P)])
+        d.launch(k["q1"], (F, 1), (P, 1), 0, [ptr(pw_f), ptr(max_line), I(P), I(P)])
+        d.launch(k["q2"], (1, 1), (F, 1), 0, [ptr(max_line), ptr(max_tile), I(P), I(P)])
+        d.launch(k["q3"], (F, P), (P, 1), 0, [ptr(pw_f), ptr(pw_h), ptr(max_tile), ptr(rev), ptr(rev), I(P), I(P)])
+        exec2d(pw_h, F, -1)
+        d.launch(k["deq"], (F, P), (P, 1), 0, [ptr(pw_h), ptr(padded), ptr(max_tile), I(P), I(P)])
+        d.launch(k["read"], (F, oy), (oy, 1), 0, [ptr(padded), ptr(out), I(P), I(P), I(oy), I(oy), I(f),
+                                                   ctypes.c_double(scale)])
+
+    return _events_ms(run, reps)

@@ -73,7 +73,7 @@ def test_queue_rejects_unknown_filter_and_oversize(tc):
 
 def test_serving_loop_short_stream(tc):
     from fft_demo_gb300 import serve
-    res = serve.run(rate=2000.0, seconds=0.25, seed=3, hbm_cap_gb=24.0, sample_every=7)
+    res = serve.run(rate=2000.0, seconds=0.25, seed=3, hbm_cap_gb=32.0, sample_every=7)
     errs = serve.errors(res, max_samples=30)
     out = serve.summarize(res, errs)
     assert out["requests"] == 500
@@ -133,3 +133,78 @@ def test_queue_result_same_alone_and_in_mix(tc, precision, tol):
         a = alone.double().cpu().numpy()
         assert rel(a[o:o + s * s], m[o:o + s * s]) < tol, s
     q.destroy()
+
+
+@pytest.mark.parametrize("precision,tol", [(tcm.FP16, CONV_SCALED_FP16), (tcm.SPLIT_FP32, 1e-5)])
+def test_queue_large_images_by_overlap_add(tc, orc, precision, tol):
+    """Images whose padded transform would exceed 2048 (2048-side 'same' with
+    a 31 x 31 filter needs P = 4096) run as overlap-add of 1024-side blocks in
+    the same launch plus one assembly launch; the three modes, non-square
+    images, and a 1D transform and a small convolution in the same submit."""
+    import torch
+    rng = np.random.default_rng(40 + precision)
+    q = tc.Queue(precision, workspace_bytes=3 << 30, staging_bytes=4 << 20)
+    w31 = rng.standard_normal((31, 31))
+    w31 /= np.abs(w31).sum()
+    w13 = rng.standard_normal((13, 13))
+    w13 /= np.abs(w13).sum()
+    q.set_filter(0, w31.astype(np.float32))
+    q.set_filter(1, w13.astype(np.float32))
+    wf = {0: w31.astype(np.float32).astype(np.float64), 1: w13.astype(np.float32).astype(np.float64)}
+    reqs = [(2048, 2048, 0, tcm.CONV_SAME), (2100, 1900, 1, tcm.CONV_VALID_CORR),
+            (1200, 2060, 1, tcm.CONV_FULL), (300, 200, 0, tcm.CONV_SAME)]
+    dt = torch.float16 if precision == tcm.FP16 else torch.float32
+    img_off, out_off, shapes, at_i, at_o = [], [], [], 0, 0
+    for sy, sx, fid, mode in reqs:
+        f = wf[fid].shape[0]
+        oy, ox = {tcm.CONV_SAME: (sy, sx), tcm.CONV_VALID_CORR: (sy - f + 1, sx - f + 1),
+                  tcm.CONV_FULL: (sy + f - 1, sx + f - 1)}[mode]
+        img_off.append(at_i)
+        out_off.append(at_o)
+        shapes.append((oy, ox))
+        at_i += sy * sx + (-(sy * sx)) % 8
+        at_o += oy * ox + (-(oy * ox)) % 8
+    cin = torch.from_numpy(rng.uniform(0, 1, at_i).astype(np.float32)).to(dt).cuda()
+    cout = torch.zeros(at_o, dtype=dt, device="cuda")
+    x = torch.from_numpy(rng.uniform(-1, 1, (4096, 2)).astype(np.float32)).to(dt).cuda()
+    y = torch.zeros_like(x)
+    convs = [(sy, sx, fid, mode, io, oo) for (sy, sx, fid, mode), io, oo in zip(reqs, img_off, out_off)]
+    q.submit([4096], [0], [0], convs, x, y, cin, cout)
+    assert tc.last_launch_count() >= 3  # filter spectra, the persistent launch, the assembly
+    q.check()
+    a = cin.double().cpu().numpy()
+    o = cout.double().cpu().numpy()
+    for (sy, sx, fid, mode), io, oo, (oy, ox) in zip(reqs, img_off, out_off, shapes):
+        img = a[io:io + sy * sx].reshape(sy, sx)
+        w = wf[fid]
+        if mode == tcm.CONV_SAME:
+            ref = orc.conv2d_same(img, w)
+        elif mode == tcm.CONV_VALID_CORR:
+            ref = orc.corr2d_valid(img[None], w[None, None])[0]
+        else:
+            ref = orc.conv2d_full(img, w[None])[0]
+        got = o[oo:oo + oy * ox].reshape(oy, ox)
+        err = orc.conv_scaled_err(got[None, None], ref[None, None], img[None, None], w[None, None])
+        assert err < tol, (sy, sx, mode, err)
+    xh = x.double().cpu().numpy()
+    yh = y.double().cpu().numpy()
+    rel = orc.rel_l2(yh[:, 0] + 1j * yh[:, 1], orc.fft1d(xh[:, 0] + 1j * xh[:, 1]))
+    assert rel < (2e-3 if precision == tcm.FP16 else 1e-5)
+    # the same 2048-side request alone gives the same result
+    alone = torch.zeros_like(cout)
+    q.submit(convs=[convs[0]], conv_in=cin, conv_out=alone)
+    q.check()
+    s = slice(out_off[0], out_off[0] + 2048 * 2048)
+    assert torch.equal(alone[s], cout[s])
+    q.destroy()
+
+
+def test_copy_inputs_to_device(tc):
+    import torch
+    host = torch.arange(1000, dtype=torch.float32).pin_memory()
+    dev = torch.zeros(1000, dtype=torch.float32, device="cuda")
+    tc.copy_inputs(host, [0, 400], [40, 80], dev, [800, 0])
+    torch.cuda.synchronize()
+    d = dev.cpu()
+    assert torch.equal(d[200:210], torch.arange(10, dtype=torch.float32))
+    assert torch.equal(d[0:20], torch.arange(100, 120, dtype=torch.float32))
