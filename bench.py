@@ -291,11 +291,30 @@ def load_tuning():
 
 
 def run_case(spec):
-    """A small, fixed workload for ncu: REPS execs of one plan on seeded data."""
+    """A small, fixed workload for ncu: REPS execs of one plan on seeded data.
+    N,BATCH[,REPS[,PREC]] for a 1D plan; conv,SIDE,F[,REPS] for the FP16
+    'same' convolution of one SIDE x SIDE image with an F x F filter."""
     import torch
     import fft_demo_gb300 as tc
     load_tuning()
     parts = spec.split(",")
+    if parts[0] == "conv":
+        side, f = int(parts[1]), int(parts[2])
+        reps = int(parts[3]) if len(parts) > 3 else 3
+        g = torch.Generator(device="cuda")
+        g.manual_seed(1)
+        img = torch.rand((1, 1, side, side), device="cuda", generator=g).half()
+        w = torch.randn((1, 1, f, f), device="cuda", generator=g)
+        conv = tc.Conv2d(1, 1, side, side, f, f, mode=tc.CONV_SAME, precision=tc.FP16)
+        conv.set_filters(w / w.abs().sum())
+        out = conv.exec(img)
+        for _ in range(reps):
+            conv.exec(img, out)
+        launches = tc.last_launch_count()
+        conv.check()
+        torch.cuda.synchronize()
+        print(json.dumps({"case": spec, "launches_per_exec": launches, "padded": conv.padded}))
+        return 0
     n, batch = int(parts[0]), int(parts[1])
     reps = int(parts[2]) if len(parts) > 2 else 3
     prec = tc.SPLIT_FP32 if len(parts) > 3 and parts[3] == "split" else tc.FP16
