@@ -908,6 +908,90 @@ __device__ __forceinline__ bool wait_prefetch(PassState& st, const IO& io, const
   return true;
 }
 
+// Which item of permute_raw's loop a thread starts at. In a line-minor tile
+// the 16-byte chunks of a K row are XOR-swizzled by the row, so an 8-byte
+// plane store from lanes whose butterflies share a K row lands in a few banks
+// (up to 8 wavefronts per half-warp where 1 would do); lanes whose butterflies
+// lie in different K rows spread over all 32. The five lane bits of the
+// thread index are therefore sent to other bits of the item index (the
+// remaining bits keep their order), which leaves the item set of each sweep of
+// the NT threads unchanged. The destinations per (input kind, L, butterflies
+// per tile) were chosen by counting shared-memory wavefronts -- per phase
+// (32, 16 or 8 lanes for 4-, 8- or 16-byte accesses) the largest number of
+// distinct words in one bank -- of the staged-tile loads plus the plane
+// stores over every assignment of the lane bits; e.g. L = 1024, 512
+// butterflies: 2304 -> 1024 wavefronts per tile for row input, 1280 -> 768
+// for column input. Identity where nothing is gained.
+struct LaneBits {
+  int b[5];
+};
+template <int L, int Mt, bool IN_VEC_L, bool LINE_MINOR>
+constexpr LaneBits permute_lane_bits() {
+  constexpr int G = Mt * 16 / L;  // lines per tile; the table covers G % 4 == 0
+  if constexpr (G % 4 != 0) {
+    return {{0, 1, 2, 3, 4}};
+  } else if constexpr (LINE_MINOR && !IN_VEC_L) {
+    if constexpr (Mt == 512) {
+      if constexpr (L == 512) return {{0, 1, 2, 7, 3}};
+      if constexpr (L == 1024) return {{0, 1, 2, 5, 3}};
+      if constexpr (L == 2048) return {{0, 1, 4, 5, 2}};
+    } else if constexpr (Mt == 256) {
+      if constexpr (L == 128 || L == 512) return {{0, 1, 2, 5, 3}};
+      if constexpr (L == 1024) return {{0, 1, 2, 4, 3}};
+    }
+  } else if constexpr (LINE_MINOR && IN_VEC_L) {
+    if constexpr (Mt == 512) {
+      if constexpr (L <= 64) return {{0, 1, 2, 4, 3}};
+      if constexpr (L >= 256 && L <= 1024) return {{0, 1, 4, 5, 2}};
+      if constexpr (L == 2048) return {{0, 1, 2, 4, 5}};
+    } else if constexpr (Mt == 256) {
+      if constexpr (L != 128) return {{0, 1, 2, 4, 3}};
+    }
+  }
+  return {{0, 1, 2, 3, 4}};
+}
+
+struct BitPerm {
+  int d[8];
+};
+template <int L, int Mt, bool IN_VEC_L, bool LINE_MINOR, int K>
+constexpr BitPerm permute_item_bits() {
+  constexpr LaneBits lb = permute_lane_bits<L, Mt, IN_VEC_L, LINE_MINOR>();
+  BitPerm p{};
+  bool used[8] = {};
+  for (int i = 0; i < 5; ++i) {
+    p.d[i] = lb.b[i];
+    used[lb.b[i]] = true;
+  }
+  int n = 5;
+  for (int k = 0; k < K; ++k)
+    if (!used[k]) p.d[n++] = k;
+  return p;
+}
+
+constexpr bool is_bit_permutation(const BitPerm& p, int K) {
+  int seen = 0;
+  for (int i = 0; i < K; ++i) {
+    if (p.d[i] < 0 || p.d[i] >= K || ((seen >> p.d[i]) & 1)) return false;
+    seen |= 1 << p.d[i];
+  }
+  return true;
+}
+
+template <int L, int Mt, bool IN_VEC_L, bool LINE_MINOR, int NT>
+__device__ __forceinline__ int permute_first_item(int tid) {
+  constexpr int K = ilog2c(NT);
+  static_assert((1 << K) == NT && K >= 5 && K <= 8, "threads per CTA");
+  constexpr LaneBits lb = permute_lane_bits<L, Mt, IN_VEC_L, LINE_MINOR>();
+  static_assert(lb.b[0] < K && lb.b[1] < K && lb.b[2] < K && lb.b[3] < K && lb.b[4] < K, "lane bit in range");
+  constexpr BitPerm p = permute_item_bits<L, Mt, IN_VEC_L, LINE_MINOR, K>();
+  static_assert(is_bit_permutation(p, K), "a permutation of the thread index bits");
+  int r = 0;
+#pragma unroll
+  for (int i = 0; i < K; ++i) r |= ((tid >> i) & 1) << p.d[i];
+  return r;
+}
+
 // raw (staged input) -> planes, with the radix-T first stage and the first
 // radix-16 stage's twiddle. Lines >= nval read as zero.
 template <int L, int G, bool LINE_MINOR, int SIGN, class IO, int NT = kPassThreads>
@@ -917,7 +1001,7 @@ __device__ __forceinline__ void permute_raw(const uint8_t* raw, uint8_t* re, uin
   using Tl = Tile<L, G, LINE_MINOR>;
   constexpr int T = Sh::T;
   constexpr int J = Sh::J;
-  const int tid = threadIdx.x;
+  const int tid = permute_first_item<L, Tl::Mt, IO::IN_VEC_L, LINE_MINOR, NT>(threadIdx.x);
   const uint4 zero = make_uint4(0, 0, 0, 0);
   if constexpr (IO::IN_VEC_L && LINE_MINOR && G % 4 == 0) {
     // Line-minor tile from line-major raw input: item = LPI adjacent lines
