@@ -951,45 +951,41 @@ constexpr LaneBits permute_lane_bits() {
   return {{0, 1, 2, 3, 4}};
 }
 
-struct BitPerm {
-  int d[8];
-};
-template <int L, int Mt, bool IN_VEC_L, bool LINE_MINOR, int K>
-constexpr BitPerm permute_item_bits() {
-  constexpr LaneBits lb = permute_lane_bits<L, Mt, IN_VEC_L, LINE_MINOR>();
-  BitPerm p{};
-  bool used[8] = {};
-  for (int i = 0; i < 5; ++i) {
-    p.d[i] = lb.b[i];
-    used[lb.b[i]] = true;
+// Thread index with its five lane bits sent to bits B0..B4 (the other bits
+// of the index fill the remaining positions in order): a permutation of
+// [0, NT), so the items one sweep of NT threads covers stay the same.
+template <int NT, int B0, int B1, int B2, int B3, int B4>
+__device__ __forceinline__ int remap_lane_bits(int tid) {
+  constexpr int K = ilog2c(NT);
+  static_assert((1 << K) == NT && K >= 5 && K <= 8, "threads per CTA");
+  constexpr int B[5] = {B0, B1, B2, B3, B4};
+  if constexpr (B0 == 0 && B1 == 1 && B2 == 2 && B3 == 3 && B4 == 4) {
+    return tid;
+  } else {
+    static_assert(B0 < K && B1 < K && B2 < K && B3 < K && B4 < K, "lane bit in range");
+    static_assert(B0 != B1 && B0 != B2 && B0 != B3 && B0 != B4 && B1 != B2 && B1 != B3 && B1 != B4 &&
+                      B2 != B3 && B2 != B4 && B3 != B4,
+                  "distinct destinations");
+    int r = 0;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) r |= ((tid >> i) & 1) << B[i];
+    // the higher thread-index bits, in order, into the positions left free
+    int src = 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      if (k != B0 && k != B1 && k != B2 && k != B3 && k != B4) {
+        r |= ((tid >> src) & 1) << k;
+        ++src;
+      }
+    }
+    return r;
   }
-  int n = 5;
-  for (int k = 0; k < K; ++k)
-    if (!used[k]) p.d[n++] = k;
-  return p;
-}
-
-constexpr bool is_bit_permutation(const BitPerm& p, int K) {
-  int seen = 0;
-  for (int i = 0; i < K; ++i) {
-    if (p.d[i] < 0 || p.d[i] >= K || ((seen >> p.d[i]) & 1)) return false;
-    seen |= 1 << p.d[i];
-  }
-  return true;
 }
 
 template <int L, int Mt, bool IN_VEC_L, bool LINE_MINOR, int NT>
 __device__ __forceinline__ int permute_first_item(int tid) {
-  constexpr int K = ilog2c(NT);
-  static_assert((1 << K) == NT && K >= 5 && K <= 8, "threads per CTA");
   constexpr LaneBits lb = permute_lane_bits<L, Mt, IN_VEC_L, LINE_MINOR>();
-  static_assert(lb.b[0] < K && lb.b[1] < K && lb.b[2] < K && lb.b[3] < K && lb.b[4] < K, "lane bit in range");
-  constexpr BitPerm p = permute_item_bits<L, Mt, IN_VEC_L, LINE_MINOR, K>();
-  static_assert(is_bit_permutation(p, K), "a permutation of the thread index bits");
-  int r = 0;
-#pragma unroll
-  for (int i = 0; i < K; ++i) r |= ((tid >> i) & 1) << p.d[i];
-  return r;
+  return remap_lane_bits<NT, lb.b[0], lb.b[1], lb.b[2], lb.b[3], lb.b[4]>(tid);
 }
 
 // raw (staged input) -> planes, with the radix-T first stage and the first
