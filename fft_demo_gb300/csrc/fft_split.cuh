@@ -30,6 +30,16 @@ __device__ __forceinline__ void split_f(float v, __half& hi, __half& lo) {
   lo = __float2half_rn(v - __half2float(hi));
 }
 
+// hi / lo halves of two values at once (packed instructions): hi = rn16(y),
+// lo = rn16(y - hi), the difference exact in FP32
+__device__ __forceinline__ void split_pair(float2 y, uint32_t& hi, uint32_t& lo) {
+  const __half2 h = __float22half2_rn(y);
+  const float2 f = __half22float2(h);
+  const __half2 l = __float22half2_rn(f2fma(f, f2bcast(-1.f), y));
+  hi = *reinterpret_cast<const uint32_t*>(&h);
+  lo = *reinterpret_cast<const uint32_t*>(&l);
+}
+
 __device__ __forceinline__ void st_pair_split(const SplitPlanes& P, uint32_t off, float2 v) {
   __half a, b, c, d;
   split_f(v.x, a, b);
@@ -40,20 +50,6 @@ __device__ __forceinline__ void st_pair_split(const SplitPlanes& P, uint32_t off
   *reinterpret_cast<__half*>(P.il + off) = d;
 }
 
-// four consecutive m in one K row (8-byte aligned)
-__device__ __forceinline__ void st_quad_split(const SplitPlanes& P, uint32_t off, const float2 (&x)[4]) {
-  __half rh[4], rl[4], ih[4], il[4];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    split_f(x[q].x, rh[q], rl[q]);
-    split_f(x[q].y, ih[q], il[q]);
-  }
-  *reinterpret_cast<uint2*>(P.rh + off) = *reinterpret_cast<uint2*>(rh);
-  *reinterpret_cast<uint2*>(P.rl + off) = *reinterpret_cast<uint2*>(rl);
-  *reinterpret_cast<uint2*>(P.ih + off) = *reinterpret_cast<uint2*>(ih);
-  *reinterpret_cast<uint2*>(P.il + off) = *reinterpret_cast<uint2*>(il);
-}
-
 // N consecutive m in one K row (N = 2, 4, 8; offset 2N-byte aligned, inside
 // one 16-byte chunk): one 2N-byte store per plane.
 template <int N>
@@ -62,15 +58,8 @@ __device__ __forceinline__ void st_run_split(const SplitPlanes& P, uint32_t off,
   uint32_t rh[N / 2], rl[N / 2], ih[N / 2], il[N / 2];
 #pragma unroll
   for (int k = 0; k < N / 2; ++k) {
-    const __half2 hr = __floats2half2_rn(x[2 * k].x, x[2 * k + 1].x);
-    const __half2 hi = __floats2half2_rn(x[2 * k].y, x[2 * k + 1].y);
-    const float2 fr = __half22float2(hr), fi = __half22float2(hi);
-    const __half2 lr = __floats2half2_rn(x[2 * k].x - fr.x, x[2 * k + 1].x - fr.y);
-    const __half2 li = __floats2half2_rn(x[2 * k].y - fi.x, x[2 * k + 1].y - fi.y);
-    rh[k] = *reinterpret_cast<const uint32_t*>(&hr);
-    ih[k] = *reinterpret_cast<const uint32_t*>(&hi);
-    rl[k] = *reinterpret_cast<const uint32_t*>(&lr);
-    il[k] = *reinterpret_cast<const uint32_t*>(&li);
+    split_pair(make_float2(x[2 * k].x, x[2 * k + 1].x), rh[k], rl[k]);
+    split_pair(make_float2(x[2 * k].y, x[2 * k + 1].y), ih[k], il[k]);
   }
   auto put = [&](uint8_t* plane, const uint32_t (&w)[N / 2]) {
     if constexpr (N == 2) {
@@ -80,6 +69,27 @@ __device__ __forceinline__ void st_run_split(const SplitPlanes& P, uint32_t off,
     } else {
       *reinterpret_cast<uint4*>(plane + off) = make_uint4(w[0], w[1], w[2], w[3]);
     }
+  };
+  put(P.rh, rh);
+  put(P.ih, ih);
+  put(P.rl, rl);
+  put(P.il, il);
+}
+
+// four consecutive m in one K row (8-byte aligned)
+__device__ __forceinline__ void st_quad_split(const SplitPlanes& P, uint32_t off, const float2 (&x)[4]) {
+  st_run_split<4>(P, off, x);
+}
+
+// Two outputs (real parts yr, imaginary parts yi, as pairs) split into the
+// four planes at two 2-byte positions o0 (first output) and o1 (second).
+__device__ __forceinline__ void st_two_split(const SplitPlanes& P, uint32_t o0, uint32_t o1, float2 yr, float2 yi) {
+  uint32_t rh, rl, ih, il;
+  split_pair(yr, rh, rl);
+  split_pair(yi, ih, il);
+  auto put = [&](uint8_t* plane, uint32_t w) {
+    *reinterpret_cast<uint16_t*>(plane + o0) = static_cast<uint16_t>(w & 0xffffu);
+    *reinterpret_cast<uint16_t*>(plane + o1) = static_cast<uint16_t>(w >> 16);
   };
   put(P.rh, rh);
   put(P.ih, ih);
@@ -130,13 +140,14 @@ __device__ __forceinline__ bool split_stage_epilogue(const SplitPlanes& P, const
     int g, j;
     Tl::unpos(m, g, j);
     // Twiddles of the next stage, W_L^(e0 + c*de) for outputs c = 0..15 (see
-    // below for e0, de), each times the stage's 2^-4 (exact). Line-minor
-    // tiles: the G lanes of a line group share the address, so each output's
-    // exact table value is one broadcast load. Line-major tiles (32 distinct
-    // addresses per load): exact table values at c = 0, 4, 8, 12 and the
-    // step W_L^de, read before the TMEM load so their latency overlaps it;
-    // the three values between two exact ones follow by multiplying with the
-    // step (at most three FP32 products from an exact value).
+    // below for e0, de); the stage's 2^-4 (exact) is applied to the products.
+    // Line-minor tiles: the G lanes of a line group share the address, so
+    // each output's exact table value is one broadcast load. Line-major tiles
+    // (32 distinct addresses per load): exact table values at c = 0, 4, 8, 12
+    // and the step W_L^de, read before the TMEM load so their latency
+    // overlaps it; the three values between two exact ones follow by
+    // multiplying with the step (at most three FP32 products from an exact
+    // value).
     int e0_ = 0, de_ = 0;
     float2 wq[4] = {}, wstep = make_float2(1.f, 0.f);
     if constexpr (!LAST) {
@@ -145,17 +156,13 @@ __device__ __forceinline__ bool split_stage_epilogue(const SplitPlanes& P, const
       de_ = rp_ * (L / 256);
       if constexpr (!LINE_MINOR) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const float2 t = __ldg(tw + e0_ + 4 * q * de_);
-          wq[q] = make_float2(t.x * 0.0625f, t.y * 0.0625f);
-        }
+        for (int q = 0; q < 4; ++q) wq[q] = __ldg(tw + e0_ + 4 * q * de_);
         wstep = __ldg(tw + de_);
       }
     }
     auto twiddle = [&](int c, float2& w) {
       if constexpr (LINE_MINOR) {
-        const float2 t = __ldg(tw + e0_ + c * de_);
-        w = make_float2(t.x * 0.0625f, t.y * 0.0625f);
+        w = __ldg(tw + e0_ + c * de_);
       } else {
         w = (c & 3) == 0 ? wq[c >> 2] : cmulf(w, wstep);
       }
@@ -171,11 +178,16 @@ __device__ __forceinline__ bool split_stage_epilogue(const SplitPlanes& P, const
     tmem_ld_x32(taddr, d);
     tmem_ld_x32(taddr + 32u, e);
     tmem_ld_wait();
-    float2 v[16];
+    // the two halves of the accumulator summed, outputs as pairs: vr[k] =
+    // real parts of outputs 2k, 2k + 1, vi[k] = their imaginary parts
+    float2 vr[8], vi[8];
 #pragma unroll
-    for (int c = 0; c < 16; ++c)
-      v[c] = make_float2(__uint_as_float(d[c]) + __uint_as_float(e[c]),
-                         __uint_as_float(d[16 + c]) + __uint_as_float(e[16 + c]));
+    for (int k = 0; k < 8; ++k) {
+      vr[k] = f2add(make_float2(__uint_as_float(d[2 * k]), __uint_as_float(d[2 * k + 1])),
+                    make_float2(__uint_as_float(e[2 * k]), __uint_as_float(e[2 * k + 1])));
+      vi[k] = f2add(make_float2(__uint_as_float(d[16 + 2 * k]), __uint_as_float(d[17 + 2 * k])),
+                    make_float2(__uint_as_float(e[16 + 2 * k]), __uint_as_float(e[17 + 2 * k])));
+    }
     if constexpr (LAST) {
       const long long line = line0 + g;
       if (line < io.total_lines) {
@@ -183,11 +195,18 @@ __device__ __forceinline__ bool split_stage_epilogue(const SplitPlanes& P, const
         // own scale (one multiply per value instead of two)
         constexpr bool FOLD = ScaledStoreIo<IO>;
         if constexpr (!FOLD) {
+          const float2 s2 = f2bcast(out_scale);
 #pragma unroll
-          for (int c = 0; c < 16; ++c) {
-            v[c].x *= out_scale;
-            v[c].y *= out_scale;
+          for (int k = 0; k < 8; ++k) {
+            vr[k] = f2mul(vr[k], s2);
+            vi[k] = f2mul(vi[k], s2);
           }
+        }
+        float2 v[16];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          v[2 * k] = make_float2(vr[k].x, vi[k].x);
+          v[2 * k + 1] = make_float2(vr[k].y, vi[k].y);
         }
         bool staged = false;
         if constexpr (TensorMapIo<IO> && LINE_MINOR) {
@@ -237,22 +256,25 @@ __device__ __forceinline__ bool split_stage_epilogue(const SplitPlanes& P, const
       // de = rp L / 256
       const uint32_t krow = (static_cast<uint32_t>(rp) >> 3) * Tl::KSTRIDE + (rp & 7) * 128u;
       constexpr uint32_t CSTEP = LINE_MINOR ? static_cast<uint32_t>(Ns * G) : static_cast<uint32_t>(Ns);
+      // outputs 2k, 2k + 1 times their twiddles and 2^-4, as pairs
+      const float2 sixteenth = f2bcast(0.0625f);
+      float2 w;
+      auto twiddled = [&](int k, float2& yr, float2& yi) {
+        const float2 w0 = twiddle(2 * k, w);
+        const float2 w1 = twiddle(2 * k + 1, w);
+        cmul_pair(vr[k], vi[k], twpair(w0, w1), yr, yi);
+        yr = f2mul(yr, sixteenth);
+        yi = f2mul(yi, sixteenth);
+      };
       if constexpr (Ns == 1 && !LINE_MINOR) {
         // 16 outputs -> 16 consecutive columns: per plane two 16-byte stores
         uint32_t prh[8], pih[8], prl[8], pil[8];
-        float2 w;
 #pragma unroll
-        for (int c = 0; c < 16; c += 2) {
-          float2 x0 = cmulf(v[c], twiddle(c, w));
-          float2 x1 = cmulf(v[c + 1], twiddle(c + 1, w));
-          const __half2 hr = __floats2half2_rn(x0.x, x1.x), hi = __floats2half2_rn(x0.y, x1.y);
-          const float2 fr = __half22float2(hr), fi = __half22float2(hi);
-          const __half2 lr = __floats2half2_rn(x0.x - fr.x, x1.x - fr.y);
-          const __half2 li = __floats2half2_rn(x0.y - fi.x, x1.y - fi.y);
-          prh[c / 2] = *reinterpret_cast<const uint32_t*>(&hr);
-          pih[c / 2] = *reinterpret_cast<const uint32_t*>(&hi);
-          prl[c / 2] = *reinterpret_cast<const uint32_t*>(&lr);
-          pil[c / 2] = *reinterpret_cast<const uint32_t*>(&li);
+        for (int k = 0; k < 8; ++k) {
+          float2 yr, yi;
+          twiddled(k, yr, yi);
+          split_pair(yr, prh[k], prl[k]);
+          split_pair(yi, pih[k], pil[k]);
         }
         const uint32_t mp = static_cast<uint32_t>(Tl::pos(g, jp0));  // multiple of 16
         // lanes with bit 2 set store the upper half first (bank spread)
@@ -279,20 +301,24 @@ __device__ __forceinline__ bool split_stage_epilogue(const SplitPlanes& P, const
           const uint32_t mp = mp0 + static_cast<uint32_t>(k) * CSTEP;
           offs[k] = krow + (mp >> 6) * 1024u + ((((mp & 63u) >> 3) ^ (rp & 7)) << 4) + (mp & 7u) * 2u;
         }
-        float2 w;
 #pragma unroll
-        for (int c = 0; c < 16; ++c) {
-          float2 x = cmulf(v[c], twiddle(c, w));
-          st_pair_split(P, offs[c % PER] + static_cast<uint32_t>(c / PER) * 1024u, x);
+        for (int k = 0; k < 8; ++k) {
+          float2 yr, yi;
+          twiddled(k, yr, yi);
+          const int c0 = 2 * k, c1 = 2 * k + 1;
+          st_two_split(P, offs[c0 % PER] + static_cast<uint32_t>(c0 / PER) * 1024u,
+                       offs[c1 % PER] + static_cast<uint32_t>(c1 / PER) * 1024u, yr, yi);
         }
       } else {
-        float2 w;
-#pragma unroll
-        for (int c = 0; c < 16; ++c) {
-          float2 x = cmulf(v[c], twiddle(c, w));
+        auto off_of = [&](int c) {
           const uint32_t mp = static_cast<uint32_t>(Tl::pos(g, jp0 + c * Ns));
-          const uint32_t off = krow + (mp >> 6) * 1024u + ((((mp & 63u) >> 3) ^ (rp & 7)) << 4) + (mp & 7u) * 2u;
-          st_pair_split(P, off, x);
+          return krow + (mp >> 6) * 1024u + ((((mp & 63u) >> 3) ^ (rp & 7)) << 4) + (mp & 7u) * 2u;
+        };
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          float2 yr, yi;
+          twiddled(k, yr, yi);
+          st_two_split(P, off_of(2 * k), off_of(2 * k + 1), yr, yi);
         }
       }
     }
@@ -516,22 +542,45 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
             for (int c = 1; c < T; ++c) wt[c] = __ldg(core.tw + rp * c * (L / (16 * T)));
           };
           if constexpr (SHARED_RP) load_tw((j0 * T) / J);
+          if constexpr (LINE_MINOR && SHARED_RP) {
+            // two butterflies at a time: output c of each goes to its own
+            // column, and the products and the hi / lo split run on pairs
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            float2 t[T];
+            for (int q = 0; q < 4; q += 2) {
+              float2 t0[T], t1[T];
 #pragma unroll
-            for (int r = 0; r < T; ++r) t[r] = v[u][r][q];
-            small_dft<T, SIGN>(t);
-            const int j = j0 + q;
-            if constexpr (!SHARED_RP) load_tw((j * T) / J);
+              for (int r = 0; r < T; ++r) {
+                t0[r] = v[u][r][q];
+                t1[r] = v[u][r][q + 1];
+              }
+              small_dft<T, SIGN>(t0);
+              small_dft<T, SIGN>(t1);
+              const int j = j0 + q;
 #pragma unroll
-            for (int c = 1; c < T; ++c) t[c] = cmulf(t[c], wt[c]);
-            if constexpr (!LINE_MINOR) {
-              // T consecutive columns of one K row: one store per plane
-              st_run_split<T>(P, Tl::off(g, j * T), t);
-            } else {
+              for (int c = 0; c < T; ++c) {
+                float2 yr = make_float2(t0[c].x, t1[c].x), yi = make_float2(t0[c].y, t1[c].y);
+                if (c > 0) cmul_pair(yr, yi, twpair(wt[c], wt[c]), yr, yi);
+                st_two_split(P, Tl::off(g, j * T + c), Tl::off(g, (j + 1) * T + c), yr, yi);
+              }
+            }
+          } else {
 #pragma unroll
-              for (int c = 0; c < T; ++c) st_pair_split(P, Tl::off(g, j * T + c), t[c]);
+            for (int q = 0; q < 4; ++q) {
+              float2 t[T];
+#pragma unroll
+              for (int r = 0; r < T; ++r) t[r] = v[u][r][q];
+              small_dft<T, SIGN>(t);
+              const int j = j0 + q;
+              if constexpr (!SHARED_RP) load_tw((j * T) / J);
+#pragma unroll
+              for (int c = 1; c < T; ++c) t[c] = cmulf(t[c], wt[c]);
+              if constexpr (!LINE_MINOR) {
+                // T consecutive columns of one K row: one store per plane
+                st_run_split<T>(P, Tl::off(g, j * T), t);
+              } else {
+#pragma unroll
+                for (int c = 0; c < T; ++c) st_pair_split(P, Tl::off(g, j * T + c), t[c]);
+              }
             }
           }
         }
