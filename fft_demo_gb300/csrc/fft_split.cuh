@@ -869,54 +869,64 @@ struct IoFloat {
   }
   __device__ __forceinline__ void decode_l(const Raw& r, long long, int, float2 (&v)[4]) const { unpack(r, v); }
   __device__ __forceinline__ void decode_g(const Raw& r, long long, int, float2 (&v)[4]) const { unpack(r, v); }
+  // v[c] *= W_N^{li (j + c J)} * k for c = 0..15 (the outer twiddle of line
+  // li and the store scale k). The twiddle is exact (two-level table) at
+  // c = 0, 4, 8, 12, each times k; the three values after an exact one follow
+  // from the exact step W_N^{li J} (c + 1 by one product, c + 2 and c + 3 as a
+  // pair times step^2), products on packed pairs.
+  __device__ __forceinline__ void twiddle_scale16(long long line, int j, int J, float2 (&v)[16], float k) const {
+    const long long li = line & ((1ll << lps_log2) - 1);
+    const float2 step = otw(li, J);
+    const float2 s2 = cmulf(step, step);
+    const TwPair s2p = twpair(s2, s2);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      float2 w0 = otw(li, j + 4 * q * J);
+      w0 = make_float2(w0.x * k, w0.y * k);
+      const float2 w1 = cmulf(w0, step);
+      const TwPair p01 = twpair(w0, w1);
+      float2 r23, i23;
+      cmul_pair(p01.re, p01.im, s2p, r23, i23);  // (w2, w3) = (w0, w1) * step^2
+      const TwPair p23 = TwPair{r23, i23, make_float2(-i23.x, -i23.y)};
+      const int c = 4 * q;
+      float2 yr, yi;
+      cmul_pair(make_float2(v[c].x, v[c + 1].x), make_float2(v[c].y, v[c + 1].y), p01, yr, yi);
+      v[c] = make_float2(yr.x, yi.x);
+      v[c + 1] = make_float2(yr.y, yi.y);
+      cmul_pair(make_float2(v[c + 2].x, v[c + 3].x), make_float2(v[c + 2].y, v[c + 3].y), p23, yr, yi);
+      v[c + 2] = make_float2(yr.x, yi.x);
+      v[c + 3] = make_float2(yr.y, yi.y);
+    }
+  }
+  __device__ __forceinline__ static void scale16(float2 (&v)[16], float k) {
+    const float2 k2 = f2bcast(k);
+#pragma unroll
+    for (int c = 0; c < 16; c += 2) {
+      const float2 r = f2mul(make_float2(v[c].x, v[c + 1].x), k2);
+      const float2 i = f2mul(make_float2(v[c].y, v[c + 1].y), k2);
+      v[c] = make_float2(r.x, i.x);
+      v[c + 1] = make_float2(r.y, i.y);
+    }
+  }
   // Outer twiddle and scale applied in place to outputs l = j + c*J of one
   // line (same values as store_row16 writes), for the staged tensor store.
   __device__ __forceinline__ void prepare_row16(long long line, int j, int J, float2 (&v)[16],
                                                 float s = 1.0f) const {
     const float k = scale * s;
     if (otw.hi) {
-      const long long li = line & ((1ll << lps_log2) - 1);
-      float2 wq[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) wq[q] = otw(li, j + 4 * q * J);
-      const float2 step = otw(li, J);
-      float2 w = wq[0];
-#pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        w = (c & 3) == 0 ? wq[c >> 2] : cmulf(w, step);
-        v[c] = cmulf(v[c], w);
-      }
+      twiddle_scale16(line, j, J, v, k);
+    } else {
+      scale16(v, k);
     }
-#pragma unroll
-    for (int c = 0; c < 16; ++c) v[c] = make_float2(v[c].x * k, v[c].y * k);
   }
-  // Outputs l = j + c*J (c = 0..15) of one line. The outer twiddle
-  // W_N^{li*l} is exact (two-level table) at c = 0, 4, 8, 12; in between it
-  // follows from the exact step W_N^{li*J} (at most three FP32 products from
-  // an exact value), so a row costs 5 table pairs instead of 16. The
-  // stored values are scaled by scale * s.
+  // Outputs l = j + c*J (c = 0..15) of one line, times the outer twiddle (if
+  // any) and scale * s.
   __device__ __forceinline__ void store_row16(long long line, int j, int J, float2 (&v)[16],
                                               float s = 1.0f) const {
-    const float k = scale * s;
+    prepare_row16(line, j, J, v, s);
     float2* p = out + out_base(line);
-    const long long li = line & ((1ll << lps_log2) - 1);
-    if (otw.hi) {
-      float2 wq[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) wq[q] = otw(li, j + 4 * q * J);
-      const float2 step = otw(li, J);
-      float2 w = wq[0];
-#pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        w = (c & 3) == 0 ? wq[c >> 2] : cmulf(w, step);
-        const float2 x = cmulf(v[c], w);
-        p[static_cast<long long>(j + c * J) * out_elem] = make_float2(x.x * k, x.y * k);
-      }
-    } else {
-#pragma unroll
-      for (int c = 0; c < 16; ++c)
-        p[static_cast<long long>(j + c * J) * out_elem] = make_float2(v[c].x * k, v[c].y * k);
-    }
+    for (int c = 0; c < 16; ++c) p[static_cast<long long>(j + c * J) * out_elem] = v[c];
   }
 };
 
