@@ -74,6 +74,7 @@ void init_registry() {
   register_split_rowt_kernels(g_tab[kPrecSplit][kPassRowT]);
   register_split_mid_kernels(g_tab[kPrecSplit][kPassRow], g_tab[kPrecSplit][kPassCol], g_tab[kPrecSplit][kPassRowT]);
   register_f16_narrow_kernels(g_tab[kPrecF16][kPassRow], g_tab[kPrecF16][kPassCol], g_tab[kPrecF16][kPassRowT]);
+  register_split_pf_kernels(g_tab[kPrecSplit][kPassRow], g_tab[kPrecSplit][kPassCol], g_tab[kPrecSplit][kPassRowT]);
   register_fused_kernels(g_fused);
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -327,7 +328,8 @@ int choose_tile(int prec, int kind, int logL, long long lines) {
   // FP16 narrow tiles (256 rows on 128 threads, 6 CTAs/SM) when they fill
   // the GPU and column-layout rows of the tile stay >= 32 bytes (G >= 8):
   // the tuner's choice at every such length on GB300
-  if (narrow.fn && (kind == kPassRow || narrow.G >= 8) && (lines + narrow.G - 1) / narrow.G >= 6ll * g_num_sms)
+  if (prec == kPrecF16 && narrow.fn && (kind == kPassRow || narrow.G >= 8) &&
+      (lines + narrow.G - 1) / narrow.G >= 6ll * g_num_sms)
     return kTileNarrow;
   // prefetching mid tiles (3 CTAs/SM) when they fill the GPU, measured fastest
   if (mid.fn && (lines + mid.G - 1) / mid.G >= 3ll * g_num_sms) return kTileMid;

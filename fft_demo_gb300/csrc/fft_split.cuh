@@ -345,6 +345,7 @@ struct SplitState {
   uint32_t tbase;
   uint32_t phase;
   uint32_t tma_phase;
+  bool pf_pending;  // prefetching kernel: a tile copy into the raw buffer is in flight
 };
 
 constexpr int kSplitMaxGroups = 4;  // Mt <= 512
@@ -375,6 +376,7 @@ __device__ __forceinline__ void split_setup(SplitState& st, const uint32_t* __re
   st.tbase = *st.tslot;
   st.phase = 0;
   st.tma_phase = 0;
+  st.pf_pending = false;
 }
 
 template <uint32_t TMEM_COLS>
@@ -397,14 +399,110 @@ __host__ __device__ constexpr uint32_t split_tmem_cols() {
 template <class IO>
 concept L2PrefetchIo = requires(const IO& io) { io.prefetch_tile_l2(0ll, 0, 0); };
 
+// ---------------------------------------------------------------------------
+// Prefetching split kernel: the next tile's input is copied into a raw
+// buffer beside the planes while the current tile runs. Raw layout: row
+// input [g][L], column input [l][G], 8-byte elements. Contiguous row tiles
+// move as one bulk copy and column tiles with an input map as tensor loads
+// (completion on the copy barrier); otherwise 16-byte asynchronous copies
+// (two lines of one column element, or two elements of one row), zero-filled
+// past the last line.
+// ---------------------------------------------------------------------------
+template <class IO>
+__device__ __forceinline__ bool split_pf_by_barrier(const IO& io) {
+  if constexpr (IO::IN_VEC_L) {
+    return io.in_contig;
+  } else if constexpr (TensorMapIo<IO>) {
+    return io.in_tma;
+  }
+  return false;
+}
+
+template <int L, int G, class IO, int NT>
+__device__ __forceinline__ void split_prefetch(SplitState& st, const IO& io, long long line0, uint8_t* raw) {
+  const int tid = threadIdx.x;
+  const long long rem = io.total_lines - line0;
+  const int nval = rem < G ? static_cast<int>(rem) : G;
+  st.pf_pending = true;
+  if constexpr (IO::IN_VEC_L) {
+    if (io.in_contig) {
+      if (tid == 0) {
+        const uint32_t bytes = static_cast<uint32_t>(nval) * L * 8u;
+        mbar_arrive_expect_tx(st.tma_bar, bytes);
+        bulk_g2s(raw, io.in + io.in_base(line0), bytes, st.tma_bar);
+      }
+      return;
+    }
+    constexpr int HPL = L / 2;  // 16-byte chunks per line
+#pragma unroll 4
+    for (int c = tid; c < G * HPL; c += NT) {
+      const int g = c / HPL, q = c % HPL;
+      const bool ok = g < nval;
+      const void* src = ok ? static_cast<const void*>(io.in + io.in_base(line0 + g) + 2 * q)
+                           : static_cast<const void*>(io.in);
+      cp_async16(raw + (static_cast<uint32_t>(g) * L + 2u * q) * 8u, src, ok ? 16u : 0u);
+    }
+    cp_async_commit();
+  } else {
+    if constexpr (TensorMapIo<IO>) {
+      if (io.in_tma) {
+        if (tid == 0) {
+          constexpr int BY = L < 256 ? L : 256;
+          mbar_arrive_expect_tx(st.tma_bar, static_cast<uint32_t>(G) * L * 8u);
+          const int seq = static_cast<int>(line0 >> io.lps_log2);
+          const int x0 = static_cast<int>(line0 & ((1ll << io.lps_log2) - 1));
+#pragma unroll
+          for (int r0 = 0; r0 < L; r0 += BY)
+            tma_load_3d(raw + static_cast<uint32_t>(r0) * G * 8u, &io.in_map, x0, r0, seq, st.tma_bar);
+        }
+        return;
+      }
+    }
+    // one 8-byte copy per element: lines need not be adjacent in memory
+#pragma unroll 4
+    for (int c = tid; c < L * G; c += NT) {
+      const int l = c / G, g = c % G;
+      const bool ok = g < nval;
+      const void* src = ok ? static_cast<const void*>(io.in + io.in_base(line0 + g) + static_cast<long long>(l) * io.in_elem)
+                           : static_cast<const void*>(io.in);
+      cp_async8(raw + (static_cast<uint32_t>(l) * G + g) * 8u, src, ok ? 8u : 0u);
+    }
+    cp_async_commit();
+  }
+}
+
+// Wait for the prefetched tile (whole CTA). False if the bounded wait gave up.
+template <class IO>
+__device__ __forceinline__ bool split_wait_prefetch(SplitState& st, const IO& io, const PassCore& core) {
+  st.pf_pending = false;
+  if (split_pf_by_barrier(io)) {
+    bool ok = true;
+    if (threadIdx.x == 0) {
+      ok = mbar_wait_bounded(st.tma_bar, st.tma_phase & 1u);
+      if (!ok) {
+        atomicOr(core.err, kErrMmaTimeout);
+        mbar_wait_bounded(st.tma_bar, st.tma_phase & 1u);  // let a late copy land before giving up
+      }
+    }
+    st.tma_phase++;
+    return !__syncthreads_or(!ok);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  return true;
+}
+
 // next_line0 >= 0: the tile this CTA processes next, whose input is
 // prefetched into L2 while this one runs.
 // TMA_IN: the tile arrives by tensor loads (column tiles whose IO carries an
 // input map); a template parameter so each load path is compiled on its own.
 // NT: threads per CTA (256, or 128 for 256-row tiles run 4 CTAs per SM).
-template <int L, int G, bool LINE_MINOR, int SIGN, class IO, bool TMA_IN = false, int NT = kPassThreads>
+// PF: prefetching kernel; the tile is in rawbuf (its copy is awaited here)
+// and the next one's copy is issued once the planes are written.
+template <int L, int G, bool LINE_MINOR, int SIGN, class IO, bool TMA_IN = false, int NT = kPassThreads,
+          bool PF = false>
 __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const PassCore& core, long long line0,
-                                           long long next_line0 = -1) {
+                                           long long next_line0 = -1, uint8_t* rawbuf = nullptr) {
   using Sh = LineShape<L>;
   using Tl = Tile<L, G, LINE_MINOR>;
   constexpr int T = Sh::T;
@@ -426,7 +524,13 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
   const int warp = tid >> 5;
   const int lane = tid & 31;
   bool timed_out = false;
-  if constexpr (L2PrefetchIo<IO>) {
+  static_assert(!(PF && TMA_IN), "the prefetching kernel moves column tiles into its raw buffer");
+  [[maybe_unused]] int nval = G;
+  if constexpr (PF) {
+    const long long rem = io.total_lines - line0;
+    nval = rem < G ? static_cast<int>(rem) : G;
+    if (!split_wait_prefetch(st, io, core)) return false;
+  } else if constexpr (L2PrefetchIo<IO>) {
     if (next_line0 >= 0) io.prefetch_tile_l2(next_line0, G, L);
   }
   // a tensor store of the previous tile reads the plane region: it must be
@@ -491,8 +595,19 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
       for (int u = 0; u < U; ++u) {
         const int it = tid + u * NT;
 #pragma unroll
-        for (int r = 0; r < T; ++r)
-          raw[u][r] = io.fetch_l(line0 + item_g(it), item_j0(it) + r * (L / T), it < ITEMS);
+        for (int r = 0; r < T; ++r) {
+          if constexpr (PF) {
+            const int g = item_g(it);
+            if ((ITEMS % (NT * U) == 0 || it < ITEMS) && g < nval) {
+              raw[u][r] = *reinterpret_cast<const typename IO::Raw*>(
+                  rawbuf + ((static_cast<uint32_t>(g) * L + item_j0(it) + r * (L / T)) << 3));
+            } else {
+              raw[u][r] = typename IO::Raw{make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
+            }
+          } else {
+            raw[u][r] = io.fetch_l(line0 + item_g(it), item_j0(it) + r * (L / T), it < ITEMS);
+          }
+        }
       }
       float2 v[U][T][4];
       float lmax = 0.f;
@@ -622,6 +737,21 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
           loaded = true;
         }
       }
+      if constexpr (PF) {
+        // the prefetched [L][G] tile (past the last line: zero-filled)
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int it = tid + u * NT;
+#pragma unroll
+          for (int r = 0; r < T; ++r) {
+            raw[u][r] = typename IO::Raw{make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
+            if (ITEMS % (NT * U) == 0 || it < ITEMS)
+              raw[u][r] = *reinterpret_cast<const typename IO::Raw*>(
+                  rawbuf + ((static_cast<uint32_t>(it / GQ + r * (L / T)) * G + (it % GQ) * 4u) << 3));
+          }
+        }
+        loaded = true;
+      }
       if (!loaded) {
 #pragma unroll
         for (int u = 0; u < U; ++u) {
@@ -689,6 +819,10 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
     fence_proxy_async_smem();
     tc_fence_before_sync();
     __syncthreads();
+    // the raw buffer is read: the next tile's copy can go in
+    if constexpr (PF) {
+      if (next_line0 >= 0) split_prefetch<L, G, IO, NT>(st, io, next_line0, rawbuf);
+    }
 
     auto run_stage = [&](auto s_const) {
       constexpr int s = decltype(s_const)::value;
@@ -773,6 +907,52 @@ __global__ void __launch_bounds__(NT, 512 / NT) fft_pass_split(const __grid_cons
 template <int L, int G>
 constexpr int split_smem_bytes() {
   return static_cast<int>(kSplitPlaneOffset) + 4 * (G * L / 16) * 32 + 1024;
+}
+
+// Prefetching split-precision pass kernel: the planes plus a raw buffer of
+// one tile's input (G * L * 8 bytes), whose copy for the next tile runs
+// while the current one goes through its stages.
+template <int L, int G, bool LINE_MINOR, int SIGN, class IO, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) fft_pass_split_pf(const __grid_constant__ IO io, const PassCore core) {
+  using Tl = Tile<L, G, LINE_MINOR>;
+  constexpr uint32_t TMEM_COLS = split_tmem_cols<L, G>();
+  static_assert(TMEM_COLS >= 32 && (TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM columns");
+  SplitState st;
+  split_setup<TMEM_COLS>(st, core.bmat);
+  uint8_t* raw = st.smem + kSplitPlaneOffset + 4 * Tl::PLANE;
+  const long long ntiles = (io.total_lines + G - 1) / G;
+  if (blockIdx.x < ntiles) split_prefetch<L, G, IO, NT>(st, io, static_cast<long long>(blockIdx.x) * G, raw);
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long long next = tile + gridDim.x < ntiles ? (tile + gridDim.x) * G : -1;
+    if (!split_tile<L, G, LINE_MINOR, SIGN, IO, false, NT, true>(st, io, core, tile * G, next, raw)) break;
+    if constexpr (TensorMapIo<IO> && LINE_MINOR) {
+      if (io.out_tma && threadIdx.x == 0) {
+        constexpr int BY = L < 256 ? L : 256;
+        const long long line0 = tile * G;
+        const int seq = static_cast<int>(line0 >> io.lps_log2);
+        const int x0 = static_cast<int>(line0 & ((1ll << io.lps_log2) - 1));
+        const uint8_t* stage = st.smem + kSplitPlaneOffset;
+#pragma unroll
+        for (int r0 = 0; r0 < L; r0 += BY)
+          tma_store_3d(&io.out_map, stage + static_cast<uint32_t>(r0) * G * 8u, x0, r0, seq);
+        bulk_commit();
+      }
+    }
+  }
+  // an early exit may leave a copy in flight: let it land before the CTA ends
+  if (st.pf_pending) {
+    if (split_pf_by_barrier(io)) {
+      if (threadIdx.x == 0) mbar_wait_bounded(st.tma_bar, st.tma_phase & 1u);
+    } else {
+      cp_async_wait_all();
+    }
+  }
+  split_teardown<TMEM_COLS>(st);
+}
+
+template <int L, int G>
+constexpr int split_pf_smem_bytes() {
+  return static_cast<int>(kSplitPlaneOffset) + 4 * (G * L / 16) * 32 + G * L * 8 + 1024;
 }
 
 // Interleaved complex float in and out, arbitrary strides (in elements).

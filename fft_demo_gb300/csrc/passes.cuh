@@ -20,7 +20,8 @@ enum PassKind : int {
 // Tile-size variants: Mt = butterflies per radix-16 stage in one tile
 // (FP16: small 128, big 1024, mid 512 prefetching at 3 CTAs/SM, narrow 256
 //  prefetching on 128 threads at 6 CTAs/SM;
-//  split: small 128, big 512, mid 256 on 128 threads at 4 CTAs/SM).
+//  split: small 128, big 512, mid 256 on 128 threads at 4 CTAs/SM, narrow
+//  256 prefetching on 128 threads at 3 CTAs/SM).
 enum TileSel : int { kTileSmall = 0, kTileBig = 1, kTileMid = 2, kTileNarrow = 3, kNumTileSel = 4 };
 
 enum PrecSel : int { kPrecF16 = 0, kPrecSplit = 1, kNumPrec = 2 };
@@ -47,6 +48,7 @@ void register_split_col_kernels(PassTable& tab);
 void register_split_rowt_kernels(PassTable& tab);
 void register_split_mid_kernels(PassTable& row, PassTable& col, PassTable& rowt);
 void register_f16_narrow_kernels(PassTable& row, PassTable& col, PassTable& rowt);
+void register_split_pf_kernels(PassTable& row, PassTable& col, PassTable& rowt);
 
 template <int L, int Mt>
 constexpr int tile_lines() {
@@ -96,6 +98,25 @@ void fill_split_entry(PassTable& tab, int tile) {
   using IO = IoFloat<IN_VEC_L, OUT_VEC_L>;
   f.fn = reinterpret_cast<const void*>(&fft_pass_split<L, G, LINE_MINOR, -1, IO, NT>);
   i.fn = reinterpret_cast<const void*>(&fft_pass_split<L, G, LINE_MINOR, +1, IO, NT>);
+  f.smem = i.smem = smem;
+  f.G = i.G = G;
+  f.Mt = i.Mt = Mt;
+  f.threads = i.threads = NT;
+  tab[LOG][tile][0] = f;
+  tab[LOG][tile][1] = i;
+}
+
+// Prefetching split-precision variant (raw input buffer beside the planes;
+// fft_pass_split_pf).
+template <int L, int Mt, bool LINE_MINOR, bool IN_VEC_L, bool OUT_VEC_L, int NT, int MINB>
+void fill_split_pf_entry(PassTable& tab, int tile) {
+  constexpr int G = tile_lines<L, Mt>();
+  constexpr int LOG = ilog2c(L);
+  const int smem = split_pf_smem_bytes<L, G>();
+  PassKernel f, i;
+  using IO = IoFloat<IN_VEC_L, OUT_VEC_L>;
+  f.fn = reinterpret_cast<const void*>(&fft_pass_split_pf<L, G, LINE_MINOR, -1, IO, NT, MINB>);
+  i.fn = reinterpret_cast<const void*>(&fft_pass_split_pf<L, G, LINE_MINOR, +1, IO, NT, MINB>);
   f.smem = i.smem = smem;
   f.G = i.G = G;
   f.Mt = i.Mt = Mt;

@@ -245,6 +245,13 @@ __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc, uin
                "r"(src_bytes)
                : "memory");
 }
+// 8-byte asynchronous global -> shared copy (both addresses 8-byte aligned);
+// src_bytes 0 writes zeros (src must still be a valid address).
+__device__ __forceinline__ void cp_async8(void* smem_dst, const void* gsrc, uint32_t src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(smem_u32(smem_dst)), "l"(gsrc),
+               "r"(src_bytes)
+               : "memory");
+}
 // L2 prefetch of one 3D tensor-map box (a hint: no data moves to the SM).
 __device__ __forceinline__ void tma_prefetch_3d(const void* map, int c0, int c1, int c2) {
   asm volatile("cp.async.bulk.prefetch.tensor.3d.L2.global.tile [%0, {%1, %2, %3}];" ::"l"(map), "r"(c0), "r"(c1),

@@ -1,10 +1,11 @@
 """Every split-precision tile variant gives the transform within the split
 bound (GPU).
 
-tcfft_tune_set forces a variant (small 128-row tiles, big 512-row tiles);
-results are compared with
-the FP64 oracle at REL_L2_SPLIT. Batches are ragged (not a multiple of the
-tile's lines) so the last tile is partly empty."""
+tcfft_tune_set forces a variant (small 128-row tiles, big 512-row tiles,
+mid 256-row tiles, narrow 256-row tiles whose next input is prefetched into
+shared memory); results are compared with the FP64 oracle at REL_L2_SPLIT.
+Batches are ragged (not a multiple of the tile's lines) so the last tile is
+partly empty."""
 import ctypes
 
 import numpy as np
@@ -72,7 +73,7 @@ def test_split_row_inverse_variants(tc, orc):
         tc.lib().tcfft_tune_set(SPLIT, PASS_ROW, 12, -1)
 
 
-@pytest.mark.parametrize("n,log_n1", [(1 << 16, 9), (1 << 16, 8), (1 << 20, 9), (1 << 20, 10)])
+@pytest.mark.parametrize("n,log_n1", [(1 << 16, 9), (1 << 16, 8), (1 << 16, 6), (1 << 20, 9), (1 << 20, 10)])
 def test_split_four_step_tile_variants(tc, orc, n, log_n1):
     """Both passes of the two-pass path with every combination of the column
     and transposing-row variants, under the given column/row split."""
