@@ -84,8 +84,11 @@ concept TensorMapIo = requires(const IO& io) {
 template <class IO>
 concept PlanesOutIo = requires { IO::TO_PLANES; };
 
+// Complex product with a fixed rounding sequence (one product rounded, then
+// one fused multiply-add per component), so every kernel that forms the same
+// product gets the same bits whatever the compiler would contract.
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
-  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+  return make_float2(__fmaf_rn(a.x, b.x, -__fmul_rn(a.y, b.y)), __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x)));
 }
 
 // Packed FP32 pairs: one sm_100-family instruction does the same operation on
@@ -558,6 +561,66 @@ __device__ __forceinline__ bool run_stages(PassState& st, const IO& io, const Pa
     return !timed_out;
 }
 
+// Five lane-bit destinations for remap_lane_bits.
+struct LaneBits {
+  int b[5];
+};
+
+// Thread index with its five lane bits sent to bits B0..B4 (the other bits
+// of the index fill the remaining positions in order): a permutation of
+// [0, NT), so the items one sweep of NT threads covers stay the same.
+template <int NT, int B0, int B1, int B2, int B3, int B4>
+__device__ __forceinline__ int remap_lane_bits(int tid) {
+  constexpr int K = ilog2c(NT);
+  static_assert((1 << K) == NT && K >= 5 && K <= 8, "threads per CTA");
+  constexpr int B[5] = {B0, B1, B2, B3, B4};
+  if constexpr (B0 == 0 && B1 == 1 && B2 == 2 && B3 == 3 && B4 == 4) {
+    return tid;
+  } else {
+    static_assert(B0 < K && B1 < K && B2 < K && B3 < K && B4 < K, "lane bit in range");
+    static_assert(B0 != B1 && B0 != B2 && B0 != B3 && B0 != B4 && B1 != B2 && B1 != B3 && B1 != B4 &&
+                      B2 != B3 && B2 != B4 && B3 != B4,
+                  "distinct destinations");
+    int r = 0;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) r |= ((tid >> i) & 1) << B[i];
+    // the higher thread-index bits, in order, into the positions left free
+    int src = 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      if (k != B0 && k != B1 && k != B2 && k != B3 && k != B4) {
+        r |= ((tid >> src) & 1) << k;
+        ++src;
+      }
+    }
+    return r;
+  }
+}
+
+// Lane-bit destinations (remap_lane_bits) of tile_load's column-input items
+// (four adjacent lines at one butterfly, one 8-byte store per plane and
+// output), per (L, butterflies per tile), from the same shared-memory bank
+// model as permute_lane_bits; lane bit 0 stays, so two lanes still read one
+// 32-byte element row. E.g. L = 1024 on 512-butterfly tiles: 1024 -> 256
+// store wavefronts per tile. Identity where nothing is gained.
+template <int L, int Mt, bool LINE_MINOR>
+constexpr LaneBits tile_load_lane_bits() {
+  if constexpr (LINE_MINOR) {
+    if constexpr (Mt == 128) {
+      if constexpr (L == 64) return {{0, 1, 2, 5, 3}};
+      if constexpr (L == 128) return {{0, 1, 3, 4, 2}};
+    } else if constexpr (Mt == 512) {
+      if constexpr (L == 512) return {{0, 1, 2, 7, 3}};
+      if constexpr (L == 1024) return {{0, 1, 5, 6, 2}};
+      if constexpr (L == 2048) return {{0, 1, 4, 5, 2}};
+    } else if constexpr (Mt == 1024) {
+      if constexpr (L == 1024) return {{0, 1, 2, 7, 3}};
+      if constexpr (L == 2048) return {{0, 5, 6, 7, 1}};
+    }
+  }
+  return {{0, 1, 2, 3, 4}};
+}
+
 // ---------------------------------------------------------------------------
 // Load phase of one tile: G lines of length L starting at line0 from global
 // memory into the planes re / im (the radix-T stage and the first radix-16
@@ -697,32 +760,49 @@ __device__ __forceinline__ bool tile_load(PassState& st, const IO& io, const Pas
               for (int q = 0; q < 4; ++q) st_pair(re, im, Tl::off(g, j0 + q), v[0][q]);
             }
           } else {
+            // output c of butterfly j -> l' = j*T + c: K row rp = j*T / J for
+            // every c, twiddle W_(16T)^(rp c) of the next stage (Ns = T); the
+            // four butterflies of an item share rp when J / T is a multiple of
+            // 4. Line-major tiles store a butterfly's T outputs as one run.
+            constexpr bool SHARED_RP = ((J / T) % 4) == 0;
+            float2 wt[T];
+            auto load_tw = [&](int rp) {
+              wt[0] = make_float2(1.f, 0.f);
+#pragma unroll
+              for (int c = 1; c < T; ++c) wt[c] = __ldg(core.tw + rp * c * (L / (16 * T)));
+            };
+            if constexpr (SHARED_RP) load_tw((j0 * T) / J);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
               float2 t[T];
 #pragma unroll
               for (int r = 0; r < T; ++r) t[r] = v[r][q];
               small_dft<T, SIGN>(t);
-              // output c of butterfly j -> l' = j*T + c; next stage (Ns = T) twiddle
               const int j = j0 + q;
+              if constexpr (!SHARED_RP) load_tw((j * T) / J);
 #pragma unroll
-              for (int c = 0; c < T; ++c) {
-                const int lp = j * T + c;
-                const int rp = lp / J, jp = lp % J;
-                const float2 w = __ldg(core.tw + rp * (jp % T) * (L / (16 * T)));
-                st_pair(re, im, Tl::off(g, lp), cmulf(t[c], w));
+              for (int c = 1; c < T; ++c) t[c] = cmulf(t[c], wt[c]);
+              if constexpr (!LINE_MINOR) {
+                st_run<T>(re, im, Tl::off(g, j * T), t);
+              } else {
+#pragma unroll
+                for (int c = 0; c < T; ++c) st_pair(re, im, Tl::off(g, j * T + c), t[c]);
               }
             }
           }
         }
       }
     } else {
-      // item = (4 adjacent lines g0..g0+3, butterfly j of the radix-T stage)
+      // item = (4 adjacent lines g0..g0+3, butterfly j of the radix-T stage);
+      // the lane bits of the first item are remapped so that one store
+      // instruction's 8-byte plane stores spread over the banks
       constexpr int GQ = G / 4;
       constexpr int ITEMS = GQ * (L / T);
       constexpr int U = T >= 8 ? 1 : 8 / T;
+      constexpr LaneBits lb = tile_load_lane_bits<L, Mt, LINE_MINOR>();
+      const int first = remap_lane_bits<kPassThreads, lb.b[0], lb.b[1], lb.b[2], lb.b[3], lb.b[4]>(tid);
 #pragma unroll 1
-      for (int base = tid; base < ITEMS; base += kPassThreads * U) {
+      for (int base = first; base < ITEMS; base += kPassThreads * U) {
         typename IO::Raw raw[U][T];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
@@ -922,9 +1002,6 @@ __device__ __forceinline__ bool wait_prefetch(PassState& st, const IO& io, const
 // stores over every assignment of the lane bits; e.g. L = 1024, 512
 // butterflies: 2304 -> 1024 wavefronts per tile for row input, 1280 -> 768
 // for column input. Identity where nothing is gained.
-struct LaneBits {
-  int b[5];
-};
 template <int L, int Mt, bool IN_VEC_L, bool LINE_MINOR>
 constexpr LaneBits permute_lane_bits() {
   constexpr int G = Mt * 16 / L;  // lines per tile; the table covers G % 4 == 0
@@ -949,37 +1026,6 @@ constexpr LaneBits permute_lane_bits() {
     }
   }
   return {{0, 1, 2, 3, 4}};
-}
-
-// Thread index with its five lane bits sent to bits B0..B4 (the other bits
-// of the index fill the remaining positions in order): a permutation of
-// [0, NT), so the items one sweep of NT threads covers stay the same.
-template <int NT, int B0, int B1, int B2, int B3, int B4>
-__device__ __forceinline__ int remap_lane_bits(int tid) {
-  constexpr int K = ilog2c(NT);
-  static_assert((1 << K) == NT && K >= 5 && K <= 8, "threads per CTA");
-  constexpr int B[5] = {B0, B1, B2, B3, B4};
-  if constexpr (B0 == 0 && B1 == 1 && B2 == 2 && B3 == 3 && B4 == 4) {
-    return tid;
-  } else {
-    static_assert(B0 < K && B1 < K && B2 < K && B3 < K && B4 < K, "lane bit in range");
-    static_assert(B0 != B1 && B0 != B2 && B0 != B3 && B0 != B4 && B1 != B2 && B1 != B3 && B1 != B4 &&
-                      B2 != B3 && B2 != B4 && B3 != B4,
-                  "distinct destinations");
-    int r = 0;
-#pragma unroll
-    for (int i = 0; i < 5; ++i) r |= ((tid >> i) & 1) << B[i];
-    // the higher thread-index bits, in order, into the positions left free
-    int src = 5;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      if (k != B0 && k != B1 && k != B2 && k != B3 && k != B4) {
-        r |= ((tid >> src) & 1) << k;
-        ++src;
-      }
-    }
-    return r;
-  }
 }
 
 template <int L, int Mt, bool IN_VEC_L, bool LINE_MINOR, int NT>
