@@ -429,6 +429,45 @@ __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const f
           }
 #pragma unroll
           for (int c = 0; c < 16; ++c) st_pair(re, im, offs[c % PER] + static_cast<uint32_t>(c / PER) * 1024u, y[c]);
+        } else if constexpr (LINE_MINOR && Ns == 1 && G == 4) {
+          // Four-line tiles, first stage: output c of butterfly (g, j) goes
+          // to column (jp0 + c) * 4 + g of K row rp, jp0 a multiple of 16.
+          // A warp's 8 butterflies j share rp, so one output of all of them
+          // falls in the same 16-byte chunk of 8 atoms: 8 wavefronts per
+          // store. Lane group k = (lane >> 2) & 7 stores its outputs in the
+          // order c ^ 2k instead (slot i holds output i ^ 2k, chunk
+          // (i >> 1) ^ k ^ rp), so one instruction's stores fill 8 chunks.
+          // The values move as packed (re, im) halves through three
+          // conditional swaps.
+          const uint32_t k = (static_cast<uint32_t>(lane) >> 2) & 7u;
+          uint32_t h[16];
+#pragma unroll
+          for (int c = 0; c < 16; ++c) {
+            const __half2 p = __floats2half2_rn(y[c].x, y[c].y);
+            h[c] = *reinterpret_cast<const uint32_t*>(&p);
+          }
+#pragma unroll
+          for (int lvl = 0; lvl < 3; ++lvl) {
+            const bool sw = (k >> lvl) & 1u;
+            const int stride = 2 << lvl;
+#pragma unroll
+            for (int c = 0; c < 16; ++c) {
+              if ((c & stride) == 0) {
+                const uint32_t a = h[c], b = h[c + stride];
+                h[c] = sw ? b : a;
+                h[c + stride] = sw ? a : b;
+              }
+            }
+          }
+          const uint32_t mp0 = static_cast<uint32_t>(Tl::pos(g, jp0));
+          const uint32_t base = krow + (mp0 >> 6) * 1024u + static_cast<uint32_t>(g) * 2u;
+          const uint32_t kx = k ^ static_cast<uint32_t>(rp & 7);
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const uint32_t off = base + (((static_cast<uint32_t>(i) >> 1) ^ kx) << 4) + static_cast<uint32_t>(i & 1) * 8u;
+            *reinterpret_cast<uint16_t*>(re + off) = static_cast<uint16_t>(h[i] & 0xffffu);
+            *reinterpret_cast<uint16_t*>(im + off) = static_cast<uint16_t>(h[i] >> 16);
+          }
         } else {
 #pragma unroll
           for (int c = 0; c < 16; ++c) {
