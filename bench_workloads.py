@@ -363,7 +363,7 @@ def uneven(peak_gbs, count=10000, nconv=512, seed=4, precisions=((tc.SPLIT_FP32,
     return {"workload": "uneven batch: 10000 1D FFTs 2^6..2^16 + 512 same convs", **out}
 
 
-def serving(peak_gbs, rate=20000.0, seconds=1.0, sweep=(8000.0, 12000.0, 16000.0, 24000.0), sweep_seconds=0.5,
+def serving(peak_gbs, rate=20000.0, seconds=1.0, sweep=(8000.0, 16000.0, 24000.0, 32000.0, 40000.0), sweep_seconds=0.5,
             p99_bound_ms=50.0, max_side=2048):
     """Config 5 at the offered 20k req/s (image sides 64 .. max_side), then a
     sweep of offered rates: the saturation rate is the largest achieved rate

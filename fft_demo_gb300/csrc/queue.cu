@@ -12,13 +12,18 @@
 // the GPU work of submit i. All submits of a queue share its workspace and
 // counters: use one stream per queue.
 //
-// Convolutions whose padded transform would exceed the persistent kernel's
-// largest (P > 2^kBatchMaxConvLog, e.g. a 2048 x 2048 image) run as
-// overlap-add: the image is cut into blocks of at most kBlockSide^2, each
-// block's full linear convolution (the filter rotated for a correlation) is an
-// ordinary convolution of the same launch, written to a scratch region of the
-// workspace, and one more launch sums the block outputs into the requested
-// output window (assemble_kernel).
+// Convolutions whose own padded transform would be 2048 or more (P >= 2^11:
+// images of side 1024 and up; the persistent kernel's largest is 2048) run as
+// overlap-add: the image is cut into square blocks of side B = P_b - (f - 1),
+// P_b = 512 (or the next power of two that keeps B >= 3/4 P_b for a large
+// filter side f), so each block's full linear convolution (the filter rotated
+// for a correlation) fits a P_b transform. Blocks are ordinary convolutions of
+// the same launch, written to a scratch region of the workspace, and one more
+// launch sums the block outputs into the requested output window
+// (assemble_kernel). The padded area falls from (2 s)^2 to about
+// (s P_b / B)^2: a 2048-side image with a 63-point filter runs 25 blocks of
+// 512^2 instead of one 4096^2 transform, and a 1024-side one 9 blocks instead
+// of one 2048^2 transform.
 //
 // No counterpart in the reference, whose entry points run one plan's size
 // per call (tcfftExec, tcfft_half.cu:1177; fft_conv2d_half::conv2d_forward,
@@ -42,7 +47,8 @@ using namespace tcfft::bh;
 
 namespace {
 
-constexpr int kBlockSide = 1024;
+constexpr int kOverlapMinLogP = 11;  // own transform of this size or more: overlap-add
+constexpr int kBlockLogP = 9;        // block transforms of 512 (or more for large filters)
 
 // One overlap-add output: the window [r0, r0 + oy) x [c0, c0 + ox) of the
 // full convolution, assembled from blocks [blk0, blk0 + nblk).
@@ -312,7 +318,7 @@ tcfftStatus tcfft_queue_submit(tcfftQueue q, int count, const long long* n, cons
     const int fy = fit->second.fy, fx = fit->second.fx;
     tcfftBatchConv d{r.sy, r.sx, fy, fx, r.mode, r.img_off, r.out_off, 0};
     BatchConv cv{};
-    if (conv_geometry(d, cv)) {
+    if (conv_geometry(d, cv) && cv.logP < kOverlapMinLogP) {
       cv.img_off = r.img_off;
       cv.out_off = r.out_off;
       const tcfftStatus s = add_conv(cv, fit->second);
@@ -334,10 +340,17 @@ tcfftStatus tcfft_queue_submit(tcfftQueue q, int count, const long long* n, cons
     } else {
       return record_status(TCFFT_INVALID_VALUE, 0);
     }
+    // block side: the block's full convolution (side B + f - 1) fills a
+    // 2^blog transform, with B >= 3/4 of it
+    const int fm1 = std::max(fy, fx) - 1;
+    int blog = kBlockLogP;
+    while (blog < kBatchMaxConvLog && 4 * ((1 << blog) - fm1) < 3 * (1 << blog)) ++blog;
+    const int bs = (1 << blog) - fm1;
+    if (bs < 1) return record_status(TCFFT_INVALID_SIZE, 0);
     AsmJob jb{r.out_off, asm_rows, oy, ox, r0, c0, static_cast<int>(blocks.size()), 0};
-    for (int by0 = 0; by0 < r.sy; by0 += kBlockSide)
-      for (int bx0 = 0; bx0 < r.sx; bx0 += kBlockSide) {
-        const int bh = std::min(kBlockSide, r.sy - by0), bw = std::min(kBlockSide, r.sx - bx0);
+    for (int by0 = 0; by0 < r.sy; by0 += bs)
+      for (int bx0 = 0; bx0 < r.sx; bx0 += bs) {
+        const int bh = std::min(bs, r.sy - by0), bw = std::min(bs, r.sx - bx0);
         BatchConv b{};
         if (!conv_geometry(tcfftBatchConv{bh, bw, fy, fx, TCFFT_CONV_FULL, 0, 0, 0}, b))
           return record_status(TCFFT_INVALID_SIZE, 0);

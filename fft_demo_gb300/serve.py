@@ -8,9 +8,11 @@ random. Request inputs come from page-locked host memory (a pool of seeded
 payloads per size): every batch first copies its requests' inputs to the
 device (one asynchronous copy per request, tcfft_copy_inputs), and its
 outputs are copied back to page-locked host memory; a request completes when
-that copy has, so both copies are inside the latency. 2048-side images need
-a padded size of 4096, beyond the persistent kernel's largest; the queue
-runs them as overlap-add of four 1024-side blocks (one more launch).
+that copy has, so both copies are inside the latency. Images of side 1024
+and 2048 (padded sizes 2048 and 4096; the persistent kernel's largest is
+2048) run in the queue as overlap-add of blocks whose full convolutions fill
+512-point transforms, plus one assembly launch: about 2.6 times less padded
+area than the images' own transforms.
 
 Each loop turn, per precision, the requests that have arrived are admitted
 in arrival order while they fit the device budget (an output ring and the
@@ -44,7 +46,9 @@ KMIN, KMAX = 6, 20
 IMAGE_SIDES = (64, 128, 256, 512, 1024, 2048)
 N_FILTERS = 64
 MAX_P = 2048      # largest padded size of the persistent kernel
-BLOCK_SIDE = 1024  # overlap-add block side of the queue for larger images
+OVERLAP_MIN_P = 2048  # the queue runs convolutions whose own P would be this or more as overlap-add
+BLOCK_P = 512     # ... of blocks whose full convolutions fill a P = 512 transform (or more for f > 129)
+SAMPLE_ELEMS = 48 << 20  # device buffer per lane for the outputs sampled for the error check
 
 
 def _pow2_at_least(v, lo=64):
@@ -58,20 +62,31 @@ def conv_padded(s, f):
     return _pow2_at_least(s + (f - 1) // 2)
 
 
+def overlap_block_side(f):
+    """Side of the queue's overlap-add blocks for an f x f filter: the block's
+    full convolution fills a BLOCK_P transform (the next power of two while
+    the block would be under 3/4 of it)."""
+    bp = BLOCK_P
+    while bp < MAX_P and 4 * (bp - (f - 1)) < 3 * bp:
+        bp *= 2
+    return bp - (f - 1)
+
+
 def conv_parts(s, f):
     """The transforms the queue runs for an s x s 'same' convolution with an
     f x f filter: [(rows, P)] per part, rows = the larger of the part's input
-    and output rows -- one part, or overlap-add blocks of at most BLOCK_SIDE
-    (full convolutions) when P would exceed MAX_P."""
+    and output rows -- one part, or overlap-add blocks (full convolutions)
+    when the image's own P would be OVERLAP_MIN_P or more."""
     p = conv_padded(s, f)
-    if p <= MAX_P:
+    if p < OVERLAP_MIN_P:
         return [(max(s, f), p)]
-    nb = -(-s // BLOCK_SIDE)
+    bs = overlap_block_side(f)
+    nb = -(-s // bs)
     out = []
     for by in range(nb):
         for bx in range(nb):
-            h = min(BLOCK_SIDE, s - by * BLOCK_SIDE)
-            w = min(BLOCK_SIDE, s - bx * BLOCK_SIDE)
+            h = min(bs, s - by * bs)
+            w = min(bs, s - bx * bs)
             out.append((h + f - 1, _pow2_at_least(max(h, w) + f - 1)))
     return out
 
@@ -189,7 +204,8 @@ def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, s
              for p in (tc.FP16, tc.SPLIT_FP32)}
     spectra = sum(N_FILTERS * sum(max(p for _, p in conv_parts(s, 63)) ** 2 for s in sides) * l.eb
                   for l in lanes.values())
-    resident = spectra + sum(2 * ring_bytes + ws_bytes for _ in lanes.values())
+    resident = spectra + sum(2 * ring_bytes + ws_bytes + (SAMPLE_ELEMS * l.eb // 2 if sample_every else 0)
+                             for l in lanes.values())
     if resident > cap:
         raise RuntimeError("device budget %.1f GB exceeds the %.1f GB cap" % (resident / 1e9, cap / 1e9))
     # per-request device footprint: output + workspace
@@ -239,7 +255,13 @@ def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, s
     torch.cuda.synchronize()
 
     lat = np.full(nreq, np.nan)
-    samples = []
+    # sampled outputs (for the error check) are copied on the device, on the
+    # lane's stream after their batch, into a per-lane buffer read after the
+    # run: no host copy inside the loop
+    sample_meta, sample_max = [], 60
+    for lane in lanes.values():
+        lane.sample_dev = torch.empty(SAMPLE_ELEMS if sample_every else 1, dtype=lane.dt, device="cuda")
+        lane.sample_head = 0
     e0 = torch.cuda.Event(enable_timing=True)
     pending = collections.deque(range(nreq))
     launches = 0
@@ -261,8 +283,6 @@ def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, s
                 t_done = lane.e0.elapsed_time(ev) * 1e-3
                 for (i, off) in reqs:
                     lat[i] = t_done - wl["arrival"][i]
-                    if sample_every and i % sample_every == 0:
-                        samples.append((i, lane.host_out[off:off + out_elems[i]].float().numpy().copy()))
                 done += len(reqs)
         # arrivals -> per-precision waiting lines
         while pending and wl["arrival"][pending[0]] <= now:
@@ -312,12 +332,23 @@ def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, s
                 lane.host_out[start:lane.head].copy_(lane.ring[start:lane.head], non_blocking=True)
                 ev = torch.cuda.Event(enable_timing=True)
                 ev.record(lane.stream)
+                if sample_every:
+                    for i, off in reqs:
+                        n_ = int(out_elems_raw[i])
+                        if i % sample_every == 0 and len(sample_meta) < sample_max and \
+                                lane.sample_head + n_ <= SAMPLE_ELEMS:
+                            h = lane.sample_head
+                            lane.sample_dev[h:h + n_].copy_(lane.ring[off:off + n_], non_blocking=True)
+                            sample_meta.append((i, p, h, n_))
+                            lane.sample_head += n_
             lane.inflight.append((ev, start, lane.head, reqs))
             busy_flops += sum(request_flops(wl, i, filters) for i, _ in reqs)
             if verbose:
                 print("t=%.4f p=%d batch=%d" % (now, p, len(reqs)), file=sys.stderr)
     t_end = max(lane.e0.elapsed_time(lane.inflight[-1][0]) * 1e-3 if lane.inflight else 0.0
                 for lane in lanes.values())
+    torch.cuda.synchronize()
+    samples = [(i, lanes[p].sample_dev[h:h + n_].float().cpu().numpy()) for i, p, h, n_ in sample_meta]
     for lane in lanes.values():
         lane.q.check(lane.stream)
     wall = np.nanmax(lat + wl["arrival"]) - wl["arrival"][0]

@@ -241,11 +241,12 @@ tcfftStatus tcfft_batch_destroy(tcfftBatch batch);
  * use), a workspace arena of workspace_bytes and two staging slots of
  * staging_bytes stay resident; a submit builds the work list on the host,
  * copies it with one async copy and launches once (twice when a filter
- * spectrum is new). A convolution whose padded size would exceed 2048 (an
- * image side above ~2000) runs as overlap-add: its image is cut into blocks
- * of at most 1024 x 1024 whose full convolutions are items of the same
- * launch (padded size 2048 for filters up to 1025), written to workspace
- * scratch, and one more launch sums them into the requested window.
+ * spectrum is new). A convolution whose own padded size would be 2048 or
+ * more (an image side above ~1000) runs as overlap-add: its image is cut
+ * into square blocks of side 512 - (f - 1) for an f x f filter (1024 or 2048
+ * minus f - 1 when f > 129 or > 257), whose full convolutions are items of the
+ * same launch padded to 512 (1024, 2048), written to workspace scratch, and
+ * one more launch sums them into the requested window.
  * Submits share the workspace: one stream per queue.
  * TCFFT_CAPACITY: the submit needs more workspace or staging; split it.
  * ------------------------------------------------------------------------ */

@@ -137,10 +137,11 @@ def test_queue_result_same_alone_and_in_mix(tc, precision, tol):
 
 @pytest.mark.parametrize("precision,tol", [(tcm.FP16, CONV_SCALED_FP16), (tcm.SPLIT_FP32, 1e-5)])
 def test_queue_large_images_by_overlap_add(tc, orc, precision, tol):
-    """Images whose padded transform would exceed 2048 (2048-side 'same' with
-    a 31 x 31 filter needs P = 4096) run as overlap-add of 1024-side blocks in
-    the same launch plus one assembly launch; the three modes, non-square
-    images, and a 1D transform and a small convolution in the same submit."""
+    """Images whose own padded transform would be 2048 or more (2048-side
+    'same' with a 31 x 31 filter needs P = 4096) run as overlap-add of blocks
+    whose full convolutions fill 512-point transforms, in the same launch plus
+    one assembly launch; the three modes, non-square images, and a 1D
+    transform and a small convolution in the same submit."""
     import torch
     rng = np.random.default_rng(40 + precision)
     q = tc.Queue(precision, workspace_bytes=3 << 30, staging_bytes=4 << 20)
