@@ -183,6 +183,34 @@ def conv_config3(reps=20, projections=False):
             "rel_l2": rel_l2(got, ref)}
 
 
+def conv_config3_queue(batch=8, reps=10):
+    """The same 2048^2 'same' convolution (31 x 31 zero-mean filter, FP16)
+    through the serving queue, `batch` images per submit: overlap-add of
+    blocks whose full convolutions fill 512-point transforms, plus the
+    assembly launch, instead of one P = 4096 transform."""
+    import torch
+    s, f = 2048, 31
+    rng = np.random.default_rng(3)
+    w = rng.standard_normal((f, f))
+    w /= np.abs(w).sum()
+    imgs = rng.uniform(0, 1, (batch, s, s)).astype(np.float32)
+    q = tc.Queue(tc.FP16, workspace_bytes=4 << 30, staging_bytes=8 << 20)
+    q.set_filter(0, w.astype(np.float32))
+    cin = torch.from_numpy(imgs).half().cuda().view(-1)
+    cout = torch.zeros_like(cin)
+    convs = [(s, s, 0, tc.CONV_SAME, k * s * s, k * s * s) for k in range(batch)]
+    ms = _timed(lambda: q.submit(convs=convs, conv_in=cin, conv_out=cout), reps)
+    launches = tc.last_launch_count()
+    q.check()
+    x = cin[:s * s].double().cpu().numpy().reshape(s, s)
+    ref = ref_conv_same(x, w)
+    got = cout[:s * s].double().cpu().numpy().reshape(s, s)
+    q.destroy()
+    return {"ms_per_conv": ms / batch, "conv_per_s": 1e3 * batch / ms, "batch": batch,
+            "launches_per_submit": launches, "scaled_err": conv_scaled_err(got, ref, x, w),
+            "rel_l2": rel_l2(got, ref)}
+
+
 def two_d_conv(peak_gbs):
     import torch
     out = {}
@@ -209,6 +237,7 @@ def two_d_conv(peak_gbs):
     plan.destroy()
     del x, y
     out["conv_same_2048_f31"] = conv_config3()
+    out["conv_same_2048_f31_queue"] = conv_config3_queue()
     # multi-image convolutions, where two real images share each complex
     # transform: 8 images of 1024^2 'same' with a 31 x 31 filter, and one
     # 512^2 input of 16 channels against 16 filters of 5 x 5 ('same')
@@ -469,6 +498,7 @@ def extras(peak_gbs, ref_cases=None):
             "rel_l2_vs_fp64": r["split"]["rel_l2_vs_fp64"], "split_hbm_frac": r["split"]["hbm_frac"],
             "cufft_fp32_ms": r["split"].get("cufft_ms")} for n, r in sp.items() if isinstance(r, dict)}
     out["config3_conv_same_2048_f31_fp16"] = conv_config3()
+    out["config3_via_queue_overlap_add"] = conv_config3_queue()
     un = uneven(peak_gbs, full=False)
     out["config4_uneven"] = {
         name: {"persistent_ms": r["persistent_eager"]["ms"], "persistent_graph_ms": r["persistent_graph"]["ms"],
