@@ -209,3 +209,43 @@ def test_copy_inputs_to_device(tc):
     d = dev.cpu()
     assert torch.equal(d[200:210], torch.arange(10, dtype=torch.float32))
     assert torch.equal(d[0:20], torch.arange(100, 120, dtype=torch.float32))
+
+
+@pytest.mark.parametrize("precision,tol", [(tcm.FP16, CONV_SCALED_FP16), (tcm.SPLIT_FP32, 1e-5)])
+def test_queue_overlap_add_block_sizes(tc, orc, precision, tol):
+    """The overlap-add block side follows the filter: 512 - (f - 1) for
+    small filters, 1024 - (f - 1) once the 512-point block would be under
+    3/4 of its transform (f = 151), with the last block row and column
+    narrower; 1024-side images (own P = 2048) take the block path too."""
+    import torch
+    rng = np.random.default_rng(70 + precision)
+    q = tc.Queue(precision, workspace_bytes=2 << 30, staging_bytes=4 << 20)
+    wbig = rng.standard_normal((151, 151))
+    wbig /= np.abs(wbig).sum()
+    wsmall = rng.standard_normal((5, 5))
+    wsmall /= np.abs(wsmall).sum()
+    q.set_filter(0, wbig.astype(np.float32))
+    q.set_filter(1, wsmall.astype(np.float32))
+    wf = {0: wbig.astype(np.float32).astype(np.float64), 1: wsmall.astype(np.float32).astype(np.float64)}
+    reqs = [(1100, 1030, 0), (1024, 1024, 1)]
+    dt = torch.float16 if precision == tcm.FP16 else torch.float32
+    offs, at = [], 0
+    for sy, sx, _ in reqs:
+        offs.append(at)
+        at += sy * sx + (-(sy * sx)) % 8
+    cin = torch.from_numpy(rng.uniform(0, 1, at).astype(np.float32)).to(dt).cuda()
+    cout = torch.zeros(at, dtype=dt, device="cuda")
+    convs = [(sy, sx, fid, tcm.CONV_SAME, o, o) for (sy, sx, fid), o in zip(reqs, offs)]
+    q.submit(convs=convs, conv_in=cin, conv_out=cout)
+    assert tc.last_launch_count() >= 2  # the persistent launch and the assembly
+    q.check()
+    a = cin.double().cpu().numpy()
+    o = cout.double().cpu().numpy()
+    for (sy, sx, fid), off in zip(reqs, offs):
+        img = a[off:off + sy * sx].reshape(sy, sx)
+        w = wf[fid]
+        ref = orc.conv2d_same(img, w)
+        got = o[off:off + sy * sx].reshape(sy, sx)
+        err = orc.conv_scaled_err(got[None, None], ref[None, None], img[None, None], w[None, None])
+        assert err < tol, (sy, sx, w.shape, err)
+    q.destroy()
