@@ -288,6 +288,7 @@ tcfftStatus conv_mid(tcfftConvImpl* c, const half2* X, half2* Z, long long plane
   fio.nr = c->P;
   fio.scale = 1.0f / static_cast<float>(c->P);
   fio.K = static_cast<const half2*>(c->K);
+  fio.tw_next = c->tw[1];
   auto iio = zero_io<IoColMaskCrop<half2>>();
   iio.out = Z;
   iio.total_lines = planes * c->P;

@@ -15,9 +15,11 @@
 // Method kept from the reference (tensorcore_fft_conv2d.cpp:250-289,
 // tensorcore_fft_conv2d_kernel.cu:1101-1150): pad, forward FFT, pointwise
 // product with the pre-transformed filter, inverse FFT, crop; the stage
-// boundaries are fused here. Lengths P = 16^k only (256, 4096): the inverse
-// transform starts with a radix-16 stage, so the hand-off needs no radix-T
-// butterfly across threads.
+// boundaries are fused here. For P = 16^k (256, 4096) the inverse starts with
+// a radix-16 stage and the hand-off writes the products as they are; other
+// lengths start the inverse with a radix-T stage (T = 2, 4, 8), whose
+// butterflies take inputs that one thread already holds, so the hand-off runs
+// that stage and its twiddle in registers (stage_epilogue).
 #pragma once
 #include "conv_io.cuh"
 #include "fft_tile.cuh"
@@ -28,7 +30,9 @@ namespace tcfft {
 template <class E>
 struct IoConvMidFwd : IoColMaskCrop<E> {
   static constexpr bool TO_PLANES = true;
+  static constexpr int NEXT_SIGN = +1;  // the transform that follows on chip: inverse
   const E* K;  // [P][P] filter spectrum (row ky, column kx), forward, unscaled
+  const float2* tw_next;  // W_P^e of the inverse direction (its radix-T stage's twiddles)
   // v[c] = X[ky = j + c J][kx] * K[ky][kx] * scale, kx = the line's column
   __device__ __forceinline__ void product16(long long line, int j, int J, float2 (&v)[16]) const {
     const int P = this->P;
@@ -91,7 +95,6 @@ __global__ void __launch_bounds__(kPassThreads, 2)
     conv_mid_f16(const IoConvMidFwd<E> fio, const IoColMaskCrop<E> iio, const PassCore cf, const PassCore ci) {
   using Tl = Tile<P, G, true>;
   constexpr uint32_t TMEM_COLS = pass_tmem_cols<P, G>();
-  static_assert(LineShape<P>::T == 1, "P must be a power of 16");
   PassState st;
   mid_setup<TMEM_COLS>(st, cf.bmat, ci.bmat);
   uint8_t* re = st.smem + kMidPlaneOffset;

@@ -71,7 +71,7 @@ ConvKernel conv_entry_mid_f16() {
 template <int P>
 void conv_fill_f16(ConvTable& t) {
   constexpr int LOG = ilog2c(P);
-  if constexpr (LineShape<P>::T == 1) t[kConvColMid][LOG] = conv_entry_mid_f16<P, 1024>();
+  t[kConvColMid][LOG] = conv_entry_mid_f16<P, 1024>();
   t[kConvRowFwdImg][LOG] = conv_entry_f16<P, 1024, false, -1, IoRealRowIn<__half, half2>>();
   t[kConvRowFwdFilt][LOG] = conv_entry_f16<P, 1024, false, -1, IoRealRowIn<float, half2>>();
   t[kConvColFwd][LOG] = conv_entry_f16<P, 1024, true, -1, IoColMaskCrop<half2>>();

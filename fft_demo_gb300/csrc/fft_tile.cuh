@@ -299,7 +299,6 @@ __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const f
     tmem_ld_x32(tbase + (static_cast<uint32_t>(32 * (warp & 3)) << 16) + grp * 32u, d);
     tmem_ld_wait();
     if constexpr (LAST && PlanesOutIo<IO>) {
-      static_assert(Sh::T == 1, "on-chip hand-off needs a power-of-16 length");
       const long long line = line0 + g;
       float2 v[16];
 #pragma unroll
@@ -310,8 +309,33 @@ __device__ __forceinline__ void stage_epilogue(uint8_t* re, uint8_t* im, const f
 #pragma unroll
         for (int c = 0; c < 16; ++c) v[c] = make_float2(0.f, 0.f);
       }
+      if constexpr (Sh::T == 1) {
 #pragma unroll
-      for (int c = 0; c < 16; ++c) st_pair(re, im, Tl::off(g, j + c * J), v[c]);
+        for (int c = 0; c < 16; ++c) st_pair(re, im, Tl::off(g, j + c * J), v[c]);
+      } else {
+        // The following transform starts with a radix-T stage over x[j'' +
+        // r L/T]; with L/T = (16/T) J, the inputs of its butterfly j'' = j +
+        // c0 J are this thread's outputs c = c0 + r 16/T. So the stage runs
+        // here, in registers, with the next transform's direction and first
+        // twiddle W_(16T)^(rp c'), and its outputs go to l' = j'' T + c' --
+        // what that transform's load phase would have written.
+        constexpr int T = Sh::T;
+        constexpr int R = 16 / T;
+#pragma unroll
+        for (int c0 = 0; c0 < R; ++c0) {
+          float2 t[T];
+#pragma unroll
+          for (int r = 0; r < T; ++r) t[r] = v[c0 + r * R];
+          small_dft<T, IO::NEXT_SIGN>(t);
+          const int jj = j + c0 * J;
+          const int rp = (jj * T) / J;
+#pragma unroll
+          for (int cp = 0; cp < T; ++cp) {
+            const float2 x = cp == 0 ? t[0] : cmulf(t[cp], __ldg(io.tw_next + rp * cp * (L / (16 * T))));
+            st_pair(re, im, Tl::off(g, jj * T + cp), x);
+          }
+        }
+      }
     } else if constexpr (LAST) {
       // final outputs X[j + c*J] of line line0 + g
       const long long line = line0 + g;
