@@ -150,6 +150,7 @@ tcfftStatus build_persistent(tcfftBatchImpl* b) {
   const int pr = b->precision == TCFFT_FP16 ? 0 : 1;
   const int lag = 2 * g_bk_ctas[pr][b->sign_idx];
   BatchSpec spec;
+  spec.fuse_conv_columns = b->precision == TCFFT_FP16;
   spec.count = b->count;
   spec.n = b->n.data();
   spec.in_off = b->in_off.data();

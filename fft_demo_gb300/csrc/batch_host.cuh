@@ -51,6 +51,7 @@ struct BatchSpec {
   const float* scale = nullptr;  // per transform (not null when count > 0)
   std::vector<BatchConv> convs;
   std::vector<char> conv_prep;
+  bool fuse_conv_columns = false;  // FP16: both column FFTs as one item kind (kItemConvMid)
 };
 
 struct Built {
@@ -195,7 +196,7 @@ inline Built build_items(const BatchSpec& b, int lag) {
     cv.x_off = static_cast<long long>(out.ws_elems);
     out.ws_elems += static_cast<size_t>(rows) * P;
     cv.y_off = static_cast<long long>(out.ws_elems);
-    out.ws_elems += static_cast<size_t>(P) * P;
+    if (!b.fuse_conv_columns) out.ws_elems += static_cast<size_t>(P) * P;
     const int obj = static_cast<int>(out.convs.size());
     const float inv_p = 1.0f / static_cast<float>(P);
     if (b.conv_prep[c]) {
@@ -205,12 +206,21 @@ inline Built build_items(const BatchSpec& b, int lag) {
       add_tiles(out.prep_items, kItemFiltCol, cv.logP, P, obj, 1.0f, fc, tiles_of(cv.logP, cv.fy), -1);
     }
     // the convolution
-    const int c1 = out.nctrs++, c2 = out.nctrs++, c3 = out.nctrs++;
-    Stages st(4);
-    add_tiles(st[0], kItemConvRow, cv.logP, cv.sy, obj, inv_p, -1, 0, c1);
-    add_tiles(st[1], kItemConvCol, cv.logP, P, obj, inv_p, c1, tiles_of(cv.logP, cv.sy), c2);
-    add_tiles(st[2], kItemConvInv, cv.logP, P, obj, 1.0f, c2, tiles_of(cv.logP, P), c3);
-    add_tiles(st[3], kItemConvOut, cv.logP, cv.oy, obj, 1.0f, c3, tiles_of(cv.logP, P), -1);
+    Stages st;
+    if (b.fuse_conv_columns) {
+      const int c1 = out.nctrs++, c2 = out.nctrs++;
+      st.resize(3);
+      add_tiles(st[0], kItemConvRow, cv.logP, cv.sy, obj, inv_p, -1, 0, c1);
+      add_tiles(st[1], kItemConvMid, cv.logP, P, obj, inv_p, c1, tiles_of(cv.logP, cv.sy), c2);
+      add_tiles(st[2], kItemConvOut, cv.logP, cv.oy, obj, 1.0f, c2, tiles_of(cv.logP, P), -1);
+    } else {
+      const int c1 = out.nctrs++, c2 = out.nctrs++, c3 = out.nctrs++;
+      st.resize(4);
+      add_tiles(st[0], kItemConvRow, cv.logP, cv.sy, obj, inv_p, -1, 0, c1);
+      add_tiles(st[1], kItemConvCol, cv.logP, P, obj, inv_p, c1, tiles_of(cv.logP, cv.sy), c2);
+      add_tiles(st[2], kItemConvInv, cv.logP, P, obj, 1.0f, c2, tiles_of(cv.logP, P), c3);
+      add_tiles(st[3], kItemConvOut, cv.logP, cv.oy, obj, 1.0f, c3, tiles_of(cv.logP, P), -1);
+    }
     out.convs.push_back(cv);
     jobs.push_back(std::move(st));
   }

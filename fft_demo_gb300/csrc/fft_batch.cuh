@@ -43,6 +43,7 @@ enum : int {
   kItemConvOut = 6,  // conv: row FFT, real part of the output window's columns
   kItemFiltRow = 7,  // filter spectrum: forward FFT of the (flipped) filter's rows
   kItemFiltCol = 8,  // filter spectrum: forward FFT of columns -> K
+  kItemConvMid = 9,  // conv (FP16): kItemConvCol and kItemConvInv on one tile, the product on chip
 };
 
 constexpr int kBatchMt = 512;
@@ -298,6 +299,34 @@ struct IoColMulConj : IoColMaskCrop<E> {
   }
 };
 
+// kItemConvMid's forward half: the column FFT's last stage multiplies by
+// the spectrum and 1/P, conjugates (the second column FFT is a forward one:
+// IDFT(y) = conj(DFT(conj y))) and hands the result to the planes, running
+// the second transform's radix-T stage there when P is not a power of 16.
+template <class E>
+struct IoColMulConjMid : IoColMaskCrop<E> {
+  static constexpr bool TO_PLANES = true;
+  static constexpr int NEXT_SIGN = -1;
+  const E* K;             // P x P filter spectrum (row stride P)
+  const float2* tw_next;  // W_P^e, forward (the second transform's twiddles)
+  __device__ __forceinline__ void product16(long long line, int j, int J, float2 (&v)[16]) const {
+    const long long col = line & ((1ll << this->lps_log2) - 1);
+    const E* k = K + col + static_cast<long long>(j) * this->P;
+    const float2 s2 = f2bcast(this->scale);
+#pragma unroll
+    for (int c = 0; c < 16; c += 2) {
+      const float2 k0 = from_elem(k[static_cast<long long>(c) * J * this->P]);
+      const float2 k1 = from_elem(k[static_cast<long long>(c + 1) * J * this->P]);
+      float2 yr, yi;
+      cmul_pair(make_float2(v[c].x, v[c + 1].x), make_float2(v[c].y, v[c + 1].y), twpair(k0, k1), yr, yi);
+      yr = f2mul(yr, s2);
+      yi = f2mul(yi, s2);
+      v[c] = make_float2(yr.x, -yi.x);
+      v[c + 1] = make_float2(yr.y, -yi.y);
+    }
+  }
+};
+
 template <class T>
 __device__ __forceinline__ T zeroed() {
   T t;
@@ -367,6 +396,41 @@ __device__ __noinline__ bool batch_conv_item(typename BatchPrec<SPLIT>::State& s
     io.nr = L;
     io.scale = 1.0f;
     return P::template tile<L, true, -1>(st, io, core, line0);
+  }
+  if constexpr (!SPLIT) {
+    if (it.kind == kItemConvMid) {
+      // both column FFTs of the convolution on one tile: X's columns (rows
+      // past the image zero) -> times K, 1/P, conjugated, on chip -> second
+      // forward column FFT -> the output window's rows, back into X (each
+      // tile reads and writes only its own columns)
+      constexpr int G = kBatchMt * 16 / L;
+      using Tl = Tile<L, G, true>;
+      auto fio = zeroed<IoColMulConjMid<E>>();
+      fio.in = ws + cv.x_off;
+      fio.total_lines = L;
+      fio.P = L;
+      fio.lps_log2 = cv.logP;
+      fio.valid_rows = cv.sy;
+      fio.r0 = 0;
+      fio.nr = L;
+      fio.scale = it.scale;
+      fio.K = static_cast<const E*>(cv.kspec);
+      fio.tw_next = core.tw;
+      auto iio = zeroed<IoColMaskCrop<E>>();
+      iio.out = ws + cv.x_off;
+      iio.total_lines = L;
+      iio.P = L;
+      iio.lps_log2 = cv.logP;
+      iio.valid_rows = L;
+      iio.r0 = cv.r0;
+      iio.nr = cv.oy;
+      iio.scale = 1.0f;
+      uint8_t* re = st.smem + kPlaneOffset;
+      uint8_t* im = re + Tl::PLANE;
+      if (!tile_load<L, G, true, -1, IoColMulConjMid<E>>(st, fio, core, line0, re, im)) return false;
+      if (!run_stages<L, G, true, -1, IoColMulConjMid<E>>(st, fio, core, line0, re, im, false)) return false;
+      return run_stages<L, G, true, -1, IoColMaskCrop<E>>(st, iio, core, line0, re, im, false);
+    }
   }
   if (it.kind == kItemConvInv) {
     auto io = zeroed<IoColMaskCrop<E>>();

@@ -276,6 +276,7 @@ tcfftStatus tcfft_queue_submit(tcfftQueue q, int count, const long long* n, cons
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   BatchSpec spec;
+  spec.fuse_conv_columns = q->precision == TCFFT_FP16;
   std::vector<float> ones;
   if (count > 0 && !scale) {
     ones.assign(static_cast<size_t>(count), 1.0f);
