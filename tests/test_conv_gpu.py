@@ -194,3 +194,30 @@ def test_one_filter_fused_column_pass(tc, orc, mode):
         err = orc.conv_scaled_err(got[None, None], ref[None, None], xh[b][None], w)
         assert err < CONV_SCALED_FP16, (b, err)
     conv.destroy()
+
+
+@pytest.mark.parametrize("side,padded", [(300, 512), (600, 1024), (1100, 2048)])
+def test_one_filter_fused_column_pass_radix_tail(tc, orc, side, padded):
+    """One filter at padded sizes with a radix-2/4/8 tail (P = 512, 1024,
+    2048): the inverse column transform's radix-T stage runs in the forward
+    transform's last-stage registers, so these too take three launches; a
+    batch of three images (one pair sharing a complex plane, one alone)."""
+    import torch
+    rng = np.random.default_rng(side)
+    f, B = 31, 3
+    img = rng.uniform(0, 1, (B, 1, side, side))
+    w = rng.standard_normal((1, 1, f, f))
+    w /= np.abs(w).sum()
+    conv = tc.Conv2d(1, 1, side, side, f, f, mode=tc.CONV_SAME, precision=tc.FP16, max_batch=B)
+    assert conv.padded == padded
+    conv.set_filters(torch.from_numpy(w).float().cuda())
+    out = conv.exec(torch.from_numpy(img).half().cuda())
+    assert tc.last_launch_count() == 3
+    conv.check()
+    xh = img.astype(np.float16).astype(np.float64)
+    for b in range(B):
+        ref = orc.conv2d_same(xh[b, 0], w[0, 0])
+        got = out.double().cpu().numpy()[b, 0]
+        err = orc.conv_scaled_err(got[None, None], ref[None, None], xh[b][None], w)
+        assert err < CONV_SCALED_FP16, (b, err)
+    conv.destroy()
