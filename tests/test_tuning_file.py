@@ -25,6 +25,7 @@ TABLES = {
     "register_split_rowt_kernels": {"tab": (SPLIT, ROWT)},
     "register_split_mid_kernels": {"row": (SPLIT, ROW), "col": (SPLIT, COL), "rowt": (SPLIT, ROWT)},
     "register_f16_narrow_kernels": {"row": (F16, ROW), "col": (F16, COL), "rowt": (F16, ROWT)},
+    "register_split_pf_kernels": {"row": (SPLIT, ROW), "col": (SPLIT, COL), "rowt": (SPLIT, ROWT)},
 }
 
 
@@ -41,7 +42,7 @@ def built_variants():
             if name not in TABLES:
                 continue
             seen.add(name)
-            for m in re.finditer(r"fill_(?:pf_|split_)?entry<(\d+),[^>]*>\((\w+), (kTile\w+)\)", body):
+            for m in re.finditer(r"fill_(?:pf_|split_pf_|split_)?entry<(\d+),[^>]*>\((\w+), (kTile\w+)\)", body):
                 prec, kind = TABLES[name][m.group(2)]
                 logl = int(m.group(1)).bit_length() - 1
                 out.setdefault((prec, kind, logl), set()).add(TILES[m.group(3)])
@@ -54,6 +55,7 @@ def test_registration_parsed():
     # spot checks against the kernel files
     assert 3 in b[(F16, ROW, 12)] and 2 in b[(F16, ROW, 13)] and 3 not in b.get((F16, ROW, 13), set())
     assert 2 in b[(SPLIT, ROW, 12)] and 2 in b[(SPLIT, COL, 9)] and 2 not in b.get((SPLIT, ROWT, 7), set())
+    assert 3 in b[(SPLIT, ROW, 10)] and 3 in b[(SPLIT, COL, 10)] and 3 not in b.get((SPLIT, ROWT, 7), set())
 
 
 def test_tuning_file_names_built_variants():
