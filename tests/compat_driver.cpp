@@ -199,6 +199,27 @@ int main(int argc, char** argv) {
     cudaFree(dr);
     dump(out + "/fast_fft.bin", fres.data(), fres.size() * sizeof(cufftComplex));
   }
+  // ---- full convolution at a padded size that is not a power of two ----
+  // fftRows = fftCols = 84 + 13 - 1 = 96 (a multiple of 32, as the
+  // reference's kernels assume): the convolution runs at the next power of
+  // two and is cropped; the spectra of a 96-point grid are not produced.
+  {
+    const int kernelCount = 16, f = 13, o = 84, fr = o + f - 1;
+    std::vector<float> sig(o * o), ker(f * f * kernelCount), res(fr * fr * kernelCount), res3(res.size());
+    for (auto& v : sig) v = static_cast<float>(next_val());
+    for (auto& v : ker) v = static_cast<float>(next_val() - 0.45);
+    dump(out + "/np2_sig.bin", sig.data(), sig.size() * 4);
+    dump(out + "/np2_ker.bin", ker.data(), ker.size() * 4);
+    convolve_direct_fft(sig.data(), ker.data(), kernelCount, o, o, f, f, res.data());
+    printf("np2 direct status %d\n", tcfft_get_last_error());
+    dump(out + "/np2_direct.bin", res.data(), res.size() * 4);
+    convolve_turbo_fft_v3(sig.data(), ker.data(), kernelCount, o, o, f, f, res3.data());
+    printf("np2 turbo_v3 status %d\n", tcfft_get_last_error());
+    dump(out + "/np2_v3.bin", res3.data(), res3.size() * 4);
+    std::vector<cufftComplex> spec((kernelCount / 2) * fr * fr);
+    direct_fft(ker.data(), kernelCount, o, o, f, f, spec.data());
+    printf("np2 direct_fft status %d\n", tcfft_get_last_error());
+  }
   printf("compat driver done\n");
   return 0;
 }

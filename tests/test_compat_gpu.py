@@ -112,8 +112,8 @@ def test_fftconvolve2d_family(driver_out, orc):
 
 def _status(d, what):
     for line in (d / "stdout.txt").read_text().splitlines():
-        if line.startswith(what + " status"):
-            return int(line.split()[2])
+        if line.startswith(what + " status "):
+            return int(line[len(what) + len(" status "):].split()[0])
     raise AssertionError("no status line for " + what)
 
 
@@ -151,3 +151,20 @@ def test_qd_route(driver_out, orc):
     fspec = load(driver_out, "fast_fft.bin", np.float32)
     fspec = (fspec[0::2] + 1j * fspec[1::2]).reshape(8, 256, 256)
     assert orc.rel_l2(fspec, orc.fft2d(packed, sign=-1)) < REL_SPLIT
+
+
+def test_full_convolution_non_power_of_two(driver_out, orc):
+    """convolve_direct_fft and convolve_turbo_fft_v3 at fftRows = fftCols = 96
+    (84 + 13 - 1; fftconvolve2d.cu:184,1516-1517 pad to nRows + kRows - 1 with
+    any extent): the linear convolution is computed at the next power of two
+    and cropped, so it equals the FP64 full convolution. direct_fft's spectra
+    on a 96-point grid are not produced: the call reports TCFFT_INVALID_SIZE."""
+    assert _status(driver_out, "np2 direct") == 0
+    assert _status(driver_out, "np2 turbo_v3") == 0
+    assert _status(driver_out, "np2 direct_fft") == 1  # TCFFT_INVALID_SIZE
+    sig = load(driver_out, "np2_sig.bin", np.float32).astype(np.float64).reshape(84, 84)
+    ker = load(driver_out, "np2_ker.bin", np.float32).astype(np.float64).reshape(16, 13, 13)
+    ref = orc.conv2d_full(sig, ker)
+    for name in ("np2_direct.bin", "np2_v3.bin"):
+        got = load(driver_out, name, np.float32).reshape(16, 96, 96)
+        assert orc.rel_l2(got, ref) < REL_SPLIT, name
