@@ -32,6 +32,7 @@ zero-mean filter is much smaller than that scale.
 """
 import argparse
 import collections
+import gc
 import json
 import math
 import os
@@ -274,77 +275,85 @@ def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, s
     t0 = time.perf_counter()
     busy_flops = 0.0
     waiting = {p: collections.deque() for p in lanes}
-    while done < nreq:
-        now = time.perf_counter() - t0
-        # retire finished batches
-        for p, lane in lanes.items():
-            while lane.inflight and lane.inflight[0][0].query():
-                ev, start, end, reqs = lane.inflight.popleft()
-                t_done = lane.e0.elapsed_time(ev) * 1e-3
-                for (i, off) in reqs:
-                    lat[i] = t_done - wl["arrival"][i]
-                done += len(reqs)
-        # arrivals -> per-precision waiting lines
-        while pending and wl["arrival"][pending[0]] <= now:
-            i = pending.popleft()
-            waiting[int(wl["prec"][i])].append(i)
-        for p, lane in lanes.items():
-            if not waiting[p] or len(lane.inflight) >= 2:
-                continue
-            # admit in arrival order while the output ring, the workspace
-            # and the staging slot (work items) allow
-            limit = lane_limit(lane, int(out_elems[waiting[p][0]]))
-            if limit is None:
-                continue
-            reqs, ws_used, nitems = [], 0, 0
-            pos = lane.head
-            while waiting[p] and len(reqs) < max_batch:
-                i = waiting[p][0]
-                need = int(out_elems[i])
-                if pos + need > limit or ws_used + ws_elems[i] * lane.eb > lane.ws_bytes or \
-                        nitems + items_est[i] > MAX_ITEMS:
-                    break
-                waiting[p].popleft()
-                reqs.append((i, pos))
-                pos += need
-                ws_used += ws_elems[i] * lane.eb
-                nitems += items_est[i]
-            start = lane.head
-            lane.head = pos
-            if not reqs:
-                continue
-            ffts = [(i, off) for (i, off) in reqs if not wl["conv"][i]]
-            cvs = [(i, off) for (i, off) in reqs if wl["conv"][i]]
-            # inputs host -> device, each to the offset of its output
-            es = lane.eb // 2
-            src = [lane.pool[("fft", int(wl["k"][i]), i % pool_per_size)][0] * es if not wl["conv"][i] else
-                   lane.pool[("img", int(wl["side"][i]), i % pool_per_size)][0] * es for i, _ in reqs]
-            tc.copy_inputs(lane.host_in, src, [int(out_elems_raw[i]) * es for i, _ in reqs], lane.in_ring,
-                           [off * es for _, off in reqs], stream=lane.stream)
-            n = [1 << int(wl["k"][i]) for i, _ in ffts]
-            io_off = [off // 2 for _, off in ffts]
-            convs = [(int(wl["side"][i]), int(wl["side"][i]), int(wl["fid"][i]), tc.CONV_SAME, off, off)
-                     for i, off in cvs]
-            lane.q.submit(n, io_off, io_off, convs, lane.in_ring, lane.ring, lane.in_ring, lane.ring,
-                          stream=lane.stream)
-            launches += tc.last_launch_count()
-            with torch.cuda.stream(lane.stream):
-                lane.host_out[start:lane.head].copy_(lane.ring[start:lane.head], non_blocking=True)
-                ev = torch.cuda.Event(enable_timing=True)
-                ev.record(lane.stream)
-                if sample_every:
-                    for i, off in reqs:
-                        n_ = int(out_elems_raw[i])
-                        if i % sample_every == 0 and len(sample_meta) < sample_max and \
-                                lane.sample_head + n_ <= SAMPLE_ELEMS:
-                            h = lane.sample_head
-                            lane.sample_dev[h:h + n_].copy_(lane.ring[off:off + n_], non_blocking=True)
-                            sample_meta.append((i, p, h, n_))
-                            lane.sample_head += n_
-            lane.inflight.append((ev, start, lane.head, reqs))
-            busy_flops += sum(request_flops(wl, i, filters) for i, _ in reqs)
-            if verbose:
-                print("t=%.4f p=%d batch=%d" % (now, p, len(reqs)), file=sys.stderr)
+    # no garbage collection inside the loop: a full collection over this
+    # process's heap takes milliseconds, which would show up as tail latency
+    gc_was_enabled = gc.isenabled()
+    gc.disable()
+    try:
+        while done < nreq:
+            now = time.perf_counter() - t0
+            # retire finished batches
+            for p, lane in lanes.items():
+                while lane.inflight and lane.inflight[0][0].query():
+                    ev, start, end, reqs = lane.inflight.popleft()
+                    t_done = lane.e0.elapsed_time(ev) * 1e-3
+                    for (i, off) in reqs:
+                        lat[i] = t_done - wl["arrival"][i]
+                    done += len(reqs)
+            # arrivals -> per-precision waiting lines
+            while pending and wl["arrival"][pending[0]] <= now:
+                i = pending.popleft()
+                waiting[int(wl["prec"][i])].append(i)
+            for p, lane in lanes.items():
+                if not waiting[p] or len(lane.inflight) >= 2:
+                    continue
+                # admit in arrival order while the output ring, the workspace
+                # and the staging slot (work items) allow
+                limit = lane_limit(lane, int(out_elems[waiting[p][0]]))
+                if limit is None:
+                    continue
+                reqs, ws_used, nitems = [], 0, 0
+                pos = lane.head
+                while waiting[p] and len(reqs) < max_batch:
+                    i = waiting[p][0]
+                    need = int(out_elems[i])
+                    if pos + need > limit or ws_used + ws_elems[i] * lane.eb > lane.ws_bytes or \
+                            nitems + items_est[i] > MAX_ITEMS:
+                        break
+                    waiting[p].popleft()
+                    reqs.append((i, pos))
+                    pos += need
+                    ws_used += ws_elems[i] * lane.eb
+                    nitems += items_est[i]
+                start = lane.head
+                lane.head = pos
+                if not reqs:
+                    continue
+                ffts = [(i, off) for (i, off) in reqs if not wl["conv"][i]]
+                cvs = [(i, off) for (i, off) in reqs if wl["conv"][i]]
+                # inputs host -> device, each to the offset of its output
+                es = lane.eb // 2
+                src = [lane.pool[("fft", int(wl["k"][i]), i % pool_per_size)][0] * es if not wl["conv"][i] else
+                       lane.pool[("img", int(wl["side"][i]), i % pool_per_size)][0] * es for i, _ in reqs]
+                tc.copy_inputs(lane.host_in, src, [int(out_elems_raw[i]) * es for i, _ in reqs], lane.in_ring,
+                               [off * es for _, off in reqs], stream=lane.stream)
+                n = [1 << int(wl["k"][i]) for i, _ in ffts]
+                io_off = [off // 2 for _, off in ffts]
+                convs = [(int(wl["side"][i]), int(wl["side"][i]), int(wl["fid"][i]), tc.CONV_SAME, off, off)
+                         for i, off in cvs]
+                lane.q.submit(n, io_off, io_off, convs, lane.in_ring, lane.ring, lane.in_ring, lane.ring,
+                              stream=lane.stream)
+                launches += tc.last_launch_count()
+                with torch.cuda.stream(lane.stream):
+                    lane.host_out[start:lane.head].copy_(lane.ring[start:lane.head], non_blocking=True)
+                    ev = torch.cuda.Event(enable_timing=True)
+                    ev.record(lane.stream)
+                    if sample_every:
+                        for i, off in reqs:
+                            n_ = int(out_elems_raw[i])
+                            if i % sample_every == 0 and len(sample_meta) < sample_max and \
+                                    lane.sample_head + n_ <= SAMPLE_ELEMS:
+                                h = lane.sample_head
+                                lane.sample_dev[h:h + n_].copy_(lane.ring[off:off + n_], non_blocking=True)
+                                sample_meta.append((i, p, h, n_))
+                                lane.sample_head += n_
+                lane.inflight.append((ev, start, lane.head, reqs))
+                busy_flops += sum(request_flops(wl, i, filters) for i, _ in reqs)
+                if verbose:
+                    print("t=%.4f p=%d batch=%d" % (now, p, len(reqs)), file=sys.stderr)
+    finally:
+        if gc_was_enabled:
+            gc.enable()
     t_end = max(lane.e0.elapsed_time(lane.inflight[-1][0]) * 1e-3 if lane.inflight else 0.0
                 for lane in lanes.values())
     torch.cuda.synchronize()
