@@ -141,31 +141,24 @@ __device__ __forceinline__ bool split_stage_epilogue(const SplitPlanes& P, const
     Tl::unpos(m, g, j);
     // Twiddles of the next stage, W_L^(e0 + c*de) for outputs c = 0..15 (see
     // below for e0, de); the stage's 2^-4 (exact) is applied to the products.
-    // Line-minor tiles: the G lanes of a line group share the address, so
-    // each output's exact table value is one broadcast load. Line-major tiles
-    // (32 distinct addresses per load): exact table values at c = 0, 4, 8, 12
-    // and the step W_L^de, read before the TMEM load so their latency
-    // overlaps it; the three values between two exact ones follow by
-    // multiplying with the step (at most three FP32 products from an exact
-    // value).
+    // Exact table values at c = 0, 4, 8, 12 and the step W_L^de, read before
+    // the wait and the TMEM load so their latency overlaps them; the three
+    // values between two exact ones follow by multiplying with the step (at
+    // most three FP32 products from an exact value). Five loads per row
+    // instead of one per output, whose latency sat between the TMEM load and
+    // the products.
     int e0_ = 0, de_ = 0;
     float2 wq[4] = {}, wstep = make_float2(1.f, 0.f);
     if constexpr (!LAST) {
       const int rp_ = ((j / Ns) * 16 * Ns + j % Ns) / J;
       e0_ = rp_ * (j % Ns) * (L / (256 * Ns));
       de_ = rp_ * (L / 256);
-      if constexpr (!LINE_MINOR) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q) wq[q] = __ldg(tw + e0_ + 4 * q * de_);
-        wstep = __ldg(tw + de_);
-      }
+      for (int q = 0; q < 4; ++q) wq[q] = __ldg(tw + e0_ + 4 * q * de_);
+      wstep = __ldg(tw + de_);
     }
     auto twiddle = [&](int c, float2& w) {
-      if constexpr (LINE_MINOR) {
-        w = __ldg(tw + e0_ + c * de_);
-      } else {
-        w = (c & 3) == 0 ? wq[c >> 2] : cmulf(w, wstep);
-      }
+      w = (c & 3) == 0 ? wq[c >> 2] : cmulf(w, wstep);
       return w;
     };
     if (!mbar_wait_bounded(mbar + grp, parity)) {
