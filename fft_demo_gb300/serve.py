@@ -17,9 +17,12 @@ area than the images' own transforms.
 Each loop turn, per precision, the requests that have arrived are admitted
 in arrival order while they fit the device budget (an output ring and the
 queue's workspace, all inside the HBM cap) and go to the GPU as one submit:
-one persistent launch (tcfft_queue_submit) plus one device-to-host copy.
-At most two submits per precision are in flight, so the host builds batch
-i+1 while the GPU runs batch i.
+the inputs' host-to-device copies on the lane's copy-in stream, one
+persistent launch (tcfft_queue_submit) on its compute stream, the outputs'
+device-to-host copy on its copy-out stream, ordered by events. So a lane
+copies batch i+1 in and batch i-1 out while batch i computes, and the host
+builds the next batch meanwhile; at most three submits per precision are in
+flight.
 
 Latency = completion (a CUDA event after the batch's output copy, on a
 clock aligned with the host's) minus arrival; reported as p50 / p99 with
@@ -184,13 +187,16 @@ class Lane:
         self.host_out = torch.empty(self.ring_elems, dtype=self.dt, pin_memory=True)
         self.head = 0       # next free real element of the ring
         self.inflight = collections.deque()  # (event, ring_start, ring_end, requests)
-        self.stream = torch.cuda.Stream()
+        self.stream = torch.cuda.Stream()   # the queue's launches
+        self.s_in = torch.cuda.Stream()     # inputs host -> device
+        self.s_out = torch.cuda.Stream()    # outputs device -> host
 
 
 def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, sample_every=97,
-        pool_per_size=2, max_batch=1024, verbose=False, max_side=IMAGE_SIDES[-1]):
+        pool_per_size=2, max_batch=1024, verbose=False, max_side=IMAGE_SIDES[-1], idle_sleep_s=0.0):
     """One Poisson stream; max_side limits the image sides drawn (the stated
-    mix is 64 .. 2048)."""
+    mix is 64 .. 2048). idle_sleep_s > 0: the loop sleeps that long in a turn
+    that neither retired nor submitted a batch (instead of polling on)."""
     import torch
     filters = make_filters(seed)
     sides = tuple(x for x in IMAGE_SIDES if x <= max_side)
@@ -282,9 +288,11 @@ def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, s
     try:
         while done < nreq:
             now = time.perf_counter() - t0
+            busy = False
             # retire finished batches
             for p, lane in lanes.items():
                 while lane.inflight and lane.inflight[0][0].query():
+                    busy = True
                     ev, start, end, reqs = lane.inflight.popleft()
                     t_done = lane.e0.elapsed_time(ev) * 1e-3
                     for (i, off) in reqs:
@@ -295,7 +303,7 @@ def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, s
                 i = pending.popleft()
                 waiting[int(wl["prec"][i])].append(i)
             for p, lane in lanes.items():
-                if not waiting[p] or len(lane.inflight) >= 2:
+                if not waiting[p] or len(lane.inflight) >= 3:
                     continue
                 # admit in arrival order while the output ring, the workspace
                 # and the staging slot (work items) allow
@@ -325,8 +333,14 @@ def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, s
                 es = lane.eb // 2
                 src = [lane.pool[("fft", int(wl["k"][i]), i % pool_per_size)][0] * es if not wl["conv"][i] else
                        lane.pool[("img", int(wl["side"][i]), i % pool_per_size)][0] * es for i, _ in reqs]
+                # the batch's ring region is its own (in-flight batches keep
+                # theirs until their output copy has completed), so its
+                # inputs may land while earlier batches still compute
                 tc.copy_inputs(lane.host_in, src, [int(out_elems_raw[i]) * es for i, _ in reqs], lane.in_ring,
-                               [off * es for _, off in reqs], stream=lane.stream)
+                               [off * es for _, off in reqs], stream=lane.s_in)
+                e_in = torch.cuda.Event()
+                e_in.record(lane.s_in)
+                lane.stream.wait_event(e_in)
                 n = [1 << int(wl["k"][i]) for i, _ in ffts]
                 io_off = [off // 2 for _, off in ffts]
                 convs = [(int(wl["side"][i]), int(wl["side"][i]), int(wl["fid"][i]), tc.CONV_SAME, off, off)
@@ -334,10 +348,11 @@ def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, s
                 lane.q.submit(n, io_off, io_off, convs, lane.in_ring, lane.ring, lane.in_ring, lane.ring,
                               stream=lane.stream)
                 launches += tc.last_launch_count()
-                with torch.cuda.stream(lane.stream):
+                e_k = torch.cuda.Event()
+                e_k.record(lane.stream)
+                lane.s_out.wait_event(e_k)
+                with torch.cuda.stream(lane.s_out):
                     lane.host_out[start:lane.head].copy_(lane.ring[start:lane.head], non_blocking=True)
-                    ev = torch.cuda.Event(enable_timing=True)
-                    ev.record(lane.stream)
                     if sample_every:
                         for i, off in reqs:
                             n_ = int(out_elems_raw[i])
@@ -347,10 +362,17 @@ def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, s
                                 lane.sample_dev[h:h + n_].copy_(lane.ring[off:off + n_], non_blocking=True)
                                 sample_meta.append((i, p, h, n_))
                                 lane.sample_head += n_
+                    # completion: the output copy (and any sample copy) done,
+                    # after which the batch's ring region may be reused
+                    ev = torch.cuda.Event(enable_timing=True)
+                    ev.record(lane.s_out)
                 lane.inflight.append((ev, start, lane.head, reqs))
+                busy = True
                 busy_flops += sum(request_flops(wl, i, filters) for i, _ in reqs)
                 if verbose:
                     print("t=%.4f p=%d batch=%d" % (now, p, len(reqs)), file=sys.stderr)
+            if not busy and idle_sleep_s > 0:
+                time.sleep(idle_sleep_s)
     finally:
         if gc_was_enabled:
             gc.enable()
