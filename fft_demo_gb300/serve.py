@@ -193,10 +193,9 @@ class Lane:
 
 
 def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, sample_every=97,
-        pool_per_size=2, max_batch=1024, verbose=False, max_side=IMAGE_SIDES[-1], idle_sleep_s=0.0):
+        pool_per_size=2, max_batch=1024, verbose=False, max_side=IMAGE_SIDES[-1]):
     """One Poisson stream; max_side limits the image sides drawn (the stated
-    mix is 64 .. 2048). idle_sleep_s > 0: the loop sleeps that long in a turn
-    that neither retired nor submitted a batch (instead of polling on)."""
+    mix is 64 .. 2048)."""
     import torch
     filters = make_filters(seed)
     sides = tuple(x for x in IMAGE_SIDES if x <= max_side)
@@ -288,11 +287,9 @@ def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, s
     try:
         while done < nreq:
             now = time.perf_counter() - t0
-            busy = False
             # retire finished batches
             for p, lane in lanes.items():
                 while lane.inflight and lane.inflight[0][0].query():
-                    busy = True
                     ev, start, end, reqs = lane.inflight.popleft()
                     t_done = lane.e0.elapsed_time(ev) * 1e-3
                     for (i, off) in reqs:
@@ -367,12 +364,9 @@ def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, s
                     ev = torch.cuda.Event(enable_timing=True)
                     ev.record(lane.s_out)
                 lane.inflight.append((ev, start, lane.head, reqs))
-                busy = True
                 busy_flops += sum(request_flops(wl, i, filters) for i, _ in reqs)
                 if verbose:
                     print("t=%.4f p=%d batch=%d" % (now, p, len(reqs)), file=sys.stderr)
-            if not busy and idle_sleep_s > 0:
-                time.sleep(idle_sleep_s)
     finally:
         if gc_was_enabled:
             gc.enable()
