@@ -2,15 +2,16 @@
 // into the persistent batch kernel (fft_batch.cuh), with everything a
 // request needs kept resident on the device: twiddle and DFT tables for
 // every supported size, a pool of filters and their spectra per padded size
-// (made on first use), a workspace arena and two staging slots for the work
+// (made on first use), a workspace arena and four staging slots for the work
 // lists, so that a submit allocates nothing except a new filter spectrum.
 //
 // A submit builds the work list on the host, copies it from pinned staging
 // memory with one cudaMemcpyAsync, and makes one launch (two when a filter
-// spectrum is new). Slot k's staging is rewritten only after the launch that
-// used it two submits ago has finished, so host work on submit i+1 overlaps
-// the GPU work of submit i. All submits of a queue share its workspace and
-// counters: use one stream per queue.
+// spectrum is new). A slot's staging is rewritten only after the launch that
+// used it four submits ago has finished, so the host builds later submits
+// while up to three earlier ones are on the GPU (a caller that pipelines
+// copies around the launches keeps that many in flight). All submits of a
+// queue share its workspace and counters: use one stream per queue.
 //
 // Convolutions whose own padded transform would be 2048 or more (P >= 2^11:
 // images of side 1024 and up; the persistent kernel's largest is 2048) run as
@@ -128,7 +129,8 @@ struct tcfftQueueImpl {
     cudaEvent_t ev = nullptr;
     bool pending = false;
   };
-  Slot slot[2];
+  static constexpr int kSlots = 4;
+  Slot slot[kSlots];
   int cur = 0;
   size_t slot_bytes = 0;
   struct Filter {
@@ -459,7 +461,7 @@ tcfftStatus tcfft_queue_submit(tcfftQueue q, int count, const long long* n, cons
   }
   if (cudaEventRecord(sl.ev, st) != cudaSuccess) return record_status(TCFFT_LAUNCH_FAILED, launches);
   sl.pending = true;
-  q->cur ^= 1;
+  q->cur = (q->cur + 1) % tcfftQueueImpl::kSlots;
   return record_status(TCFFT_OK, launches);
 }
 

@@ -206,12 +206,13 @@ def run(rate=20000.0, seconds=1.0, seed=5, conv_fraction=0.5, hbm_cap_gb=60.0, s
     # the input pools and filter spectra are counted against it too
     ws_bytes = min(6 << 30, cap // 8)
     ring_bytes = min(6 << 30, cap // 8)
-    lanes = {p: Lane(p, filters, seed + 10 * p, ring_bytes, ws_bytes, 16 << 20, pool_per_size, sides)
+    staging_bytes = 16 << 20  # per staging slot of a queue (four slots)
+    lanes = {p: Lane(p, filters, seed + 10 * p, ring_bytes, ws_bytes, staging_bytes, pool_per_size, sides)
              for p in (tc.FP16, tc.SPLIT_FP32)}
     spectra = sum(N_FILTERS * sum(max(p for _, p in conv_parts(s, 63)) ** 2 for s in sides) * l.eb
                   for l in lanes.values())
-    resident = spectra + sum(2 * ring_bytes + ws_bytes + (SAMPLE_ELEMS * l.eb // 2 if sample_every else 0)
-                             for l in lanes.values())
+    resident = spectra + sum(2 * ring_bytes + ws_bytes + 4 * staging_bytes +
+                             (SAMPLE_ELEMS * l.eb // 2 if sample_every else 0) for l in lanes.values())
     if resident > cap:
         raise RuntimeError("device budget %.1f GB exceeds the %.1f GB cap" % (resident / 1e9, cap / 1e9))
     # per-request device footprint: output + workspace

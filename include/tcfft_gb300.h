@@ -238,7 +238,7 @@ tcfftStatus tcfft_batch_destroy(tcfftBatch batch);
  * forward 1D FFTs (64 <= n <= 2^20) and 2D convolutions (filters from a
  * resident pool) into the persistent batch kernel.
  * Tables, the filter pool and its spectra (made per padded size on first
- * use), a workspace arena of workspace_bytes and two staging slots of
+ * use), a workspace arena of workspace_bytes and four staging slots of
  * staging_bytes stay resident; a submit builds the work list on the host,
  * copies it with one async copy and launches once (twice when a filter
  * spectrum is new). A convolution whose own padded size would be 2048 or
