@@ -392,14 +392,25 @@ def uneven(peak_gbs, count=10000, nconv=512, seed=4, precisions=((tc.SPLIT_FP32,
     return {"workload": "uneven batch: 10000 1D FFTs 2^6..2^16 + 512 same convs", **out}
 
 
-def serving(peak_gbs, rate=20000.0, seconds=1.0, sweep=(8000.0, 16000.0, 24000.0, 32000.0, 40000.0), sweep_seconds=0.5,
-            p99_bound_ms=50.0, max_side=2048):
+def serving(peak_gbs, rate=20000.0, seconds=1.0, sweep=(8000.0, 16000.0, 24000.0, 28000.0, 32000.0, 36000.0, 40000.0),
+            sweep_seconds=0.5,
+            p99_bound_ms=50.0, max_side=2048, repeats=3):
     """Config 5 at the offered 20k req/s (image sides 64 .. max_side), then a
     sweep of offered rates: the saturation rate is the largest achieved rate
-    whose p99 latency stays within p99_bound_ms."""
+    whose p99 latency stays within p99_bound_ms. The 20k stream runs
+    `repeats` times (same seed); the line reports the run with the median
+    p99 and lists every run: a pause of the shared host or its link now and
+    then delays one run's completions by hundreds of ms."""
     from fft_demo_gb300 import serve
-    res = serve.run(rate=rate, seconds=seconds, max_side=max_side)
-    out = serve.summarize(res, serve.errors(res))
+    runs = []
+    for k in range(repeats):
+        res = serve.run(rate=rate, seconds=seconds, max_side=max_side, sample_every=97 if k == 0 else 0)
+        runs.append(serve.summarize(res, serve.errors(res) if k == 0 else {}))
+    by_p99 = sorted(range(repeats), key=lambda k: runs[k]["p99_ms"])
+    med = runs[by_p99[repeats // 2]]
+    out = dict(runs[0])  # errors and sample counts from the first run
+    out.update({k: med[k] for k in ("req_per_s", "p50_ms", "p99_ms", "max_ms", "gflops", "launches")})
+    out["runs"] = [{"req_per_s": r["req_per_s"], "p50_ms": r["p50_ms"], "p99_ms": r["p99_ms"]} for r in runs]
     rates = []
     for r in sweep:
         rr = serve.run(rate=r, seconds=sweep_seconds, sample_every=0, max_side=max_side)
@@ -509,7 +520,7 @@ def extras(peak_gbs, ref_cases=None):
         for name, r in un.items() if isinstance(r, dict)}
     sv = serving(peak_gbs)
     out["config5_serving"] = {k: v for k, v in sv.items() if k != "workload"}
-    sv = serving(peak_gbs, sweep=(20000.0, 30000.0, 40000.0, 60000.0), max_side=1024)
+    sv = serving(peak_gbs, sweep=(20000.0, 30000.0, 40000.0, 60000.0, 80000.0), max_side=1024)
     out["config5_serving_sides_to_1024"] = {k: v for k, v in sv.items() if k != "workload"}
     if ref_cases:
         out["reference_sizes"] = reference_sizes(ref_cases)
