@@ -55,6 +55,7 @@ def _declare(L):
         "tcfft_workspace_bytes": (i, [vp, ctypes.POINTER(ctypes.c_size_t)]),
         "tcfft_plan_set_fused": (i, [vp, i]),
         "tcfft_tune_set": (i, [i, i, i, i]),
+        "tcfft_tune_prefer": (i, [i, i, i, i]),
         "tcfft_tune_get": (i, [i, i, i, ctypes.POINTER(i)]),
         "tcfft_tune_split": (i, [i, i, i]),
         "tcfft_pass_info": (i, [i, i, i, i, ctypes.POINTER(i), ctypes.POINTER(i), ctypes.POINTER(i)]),

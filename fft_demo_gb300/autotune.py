@@ -5,7 +5,9 @@ kind has tile variants (tcfft_pass_info: lines per tile, CTAs per SM). For a
 workload the tuner times every variant of every pass of the transform with
 CUDA events, keeps the fastest and writes the choices to a JSON cache keyed by
 device name, precision, pass kind and log2 of the pass length. Loading the
-cache re-applies the choices through tcfft_tune_set.
+cache re-applies the choices through tcfft_tune_prefer (a smaller FP16 batch
+than the tuner's may then take smaller tiles); the tuner itself times each
+variant through tcfft_tune_set, which forces it.
 
 For four-step sizes tune_split also searches the column/row split (the
 radix schedule of the two passes), tuning both passes' tiles per split.
@@ -183,7 +185,7 @@ def load(path=None):
         data = json.load(open(path)).get(_device_name(), {})
     except Exception:
         return 0
-    lib().tcfft_tune_set.argtypes = [ctypes.c_int] * 4
+    lib().tcfft_tune_prefer.argtypes = [ctypes.c_int] * 4
     n = 0
     for key, val in data.items():
         parts = key.split("/")
@@ -192,7 +194,8 @@ def load(path=None):
                 n += 1
             continue
         prec, kind, logl = (int(v) for v in parts)
-        if lib().tcfft_tune_set(prec, kind, logl, int(val)) == 0:
+        # preferred, not forced: small batches may take smaller tiles
+        if lib().tcfft_tune_prefer(prec, kind, logl, int(val)) == 0:
             n += 1
     return n
 

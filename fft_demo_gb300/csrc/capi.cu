@@ -43,8 +43,12 @@ std::once_flag g_once;
 cudaError_t g_init_err = cudaSuccess;
 int g_num_sms = 0;
 // Tile variant per (precision, pass kind, log2 length); -1 = built-in choice.
-// Written by tcfft_tune_set (the autotuner), read at every launch.
+// Written by tcfft_tune_set (exact: the autotuner's timing, the tile tests)
+// or tcfft_tune_prefer (a tuning file: the tuner measured on batches that
+// fill the GPU, so a batch too small for the variant may take another),
+// read at every launch.
 int g_tune[kNumPrec][kNumPassKinds][kMaxLogL + 1];
+bool g_tune_pref[kNumPrec][kNumPassKinds][kMaxLogL + 1];
 // Four-step split per (precision, log2 n): log2 of the column-pass length,
 // -1 = built-in choice. Written by tcfft_tune_split, read at plan creation.
 constexpr int kMaxLogN = 24;
@@ -54,6 +58,9 @@ void tune_reset() {
   for (auto& a : g_tune)
     for (auto& b : a)
       for (int& c : b) c = -1;
+  for (auto& a : g_tune_pref)
+    for (auto& b : a)
+      for (bool& c : b) c = false;
   for (auto& a : g_split)
     for (int& c : a) c = -1;
 }
@@ -319,12 +326,24 @@ tcfftStatus launch_pass(int prec, int kind, int logL, int tile, int sign_idx, co
 // small ones when big ones would leave SMs idle.
 int choose_tile(int prec, int kind, int logL, long long lines) {
   std::call_once(g_tune_once, tune_reset);
-  const int t = g_tune[prec][kind][logL];
-  if (t >= 0 && t < kNumTileSel && g_tab[prec][kind][logL][t][0].fn) return t;
   const PassKernel& small = g_tab[prec][kind][logL][kTileSmall][0];
   const PassKernel& big = g_tab[prec][kind][logL][kTileBig][0];
   const PassKernel& mid = g_tab[prec][kind][logL][kTileMid][0];
   const PassKernel& narrow = g_tab[prec][kind][logL][kTileNarrow][0];
+  const int t = g_tune[prec][kind][logL];
+  if (t >= 0 && t < kNumTileSel && g_tab[prec][kind][logL][t][0].fn) {
+    // A preferred (tuning-file) variant was measured on batches that fill
+    // the GPU. A batch that its FP16 tiles would spread over fewer than two
+    // tiles per SM runs faster on narrow tiles when they are smaller (more
+    // CTAs of 128 threads): N = 256 x 4096 forward + inverse 15.1 -> 14.0 us
+    // from a CUDA graph against the tuned 512-row tiles.
+    const int tg = g_tab[prec][kind][logL][t][0].G;
+    const bool underfilled = (lines + tg - 1) / tg < 2ll * g_num_sms;
+    if (g_tune_pref[prec][kind][logL] && prec == kPrecF16 && underfilled && narrow.fn && narrow.G < tg &&
+        (kind == kPassRow || narrow.G >= 8))
+      return kTileNarrow;
+    return t;
+  }
   // FP16 narrow tiles (256 rows on 128 threads, 6 CTAs/SM) when they fill
   // the GPU and column-layout rows of the tile stay >= 32 bytes (G >= 8):
   // the tuner's choice at every such length on GB300
@@ -814,7 +833,8 @@ tcfftStatus tcfft_set_wait_limit(long long polls) {
 
 int tcfft_last_launch_count(void) { return g_last_launches; }
 
-tcfftStatus tcfft_tune_set(int precision, int pass_kind, int log2_len, int tile) {
+namespace {
+tcfftStatus tune_store(int precision, int pass_kind, int log2_len, int tile, bool preferred) {
   if (precision < 0 || precision >= kNumPrec || pass_kind < 0 || pass_kind >= kNumPassKinds || log2_len < 0 ||
       log2_len > kMaxLogL || tile < -1 || tile >= kNumTileSel)
     return ret(TCFFT_INVALID_VALUE);
@@ -823,7 +843,17 @@ tcfftStatus tcfft_tune_set(int precision, int pass_kind, int log2_len, int tile)
   if (s != TCFFT_OK) return ret(s);
   if (tile >= 0 && !g_tab[precision][pass_kind][log2_len][tile][0].fn) return ret(TCFFT_UNSUPPORTED);
   g_tune[precision][pass_kind][log2_len] = tile;
+  g_tune_pref[precision][pass_kind][log2_len] = preferred;
   return ret(TCFFT_OK);
+}
+}  // namespace
+
+tcfftStatus tcfft_tune_set(int precision, int pass_kind, int log2_len, int tile) {
+  return tune_store(precision, pass_kind, log2_len, tile, false);
+}
+
+tcfftStatus tcfft_tune_prefer(int precision, int pass_kind, int log2_len, int tile) {
+  return tune_store(precision, pass_kind, log2_len, tile, true);
 }
 
 tcfftStatus tcfft_tune_split(int precision, int log2_n, int log2_n1) {

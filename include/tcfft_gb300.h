@@ -305,8 +305,13 @@ typedef enum tcfftTile {
   TCFFT_TILE_NARROW = 3  /* FP16 256 rows, next tile prefetched, 128 threads,
                             6 CTAs/SM */
 } tcfftTile;
-/* tile = -1 restores the built-in choice. */
+/* tile = -1 restores the built-in choice. tcfft_tune_set: every launch of
+ * the pass uses that variant. tcfft_tune_prefer (a tuning file's choice,
+ * measured on batches that fill the GPU): the same, except that an FP16
+ * batch the variant would spread over fewer than two tiles per SM takes
+ * the smaller narrow tiles. */
 tcfftStatus tcfft_tune_set(int precision, int pass_kind, int log2_len, int tile);
+tcfftStatus tcfft_tune_prefer(int precision, int pass_kind, int log2_len, int tile);
 tcfftStatus tcfft_tune_get(int precision, int pass_kind, int log2_len, int *tile);
 /* Four-step split for 1D plans of 2^log2_n points made after this call:
  * column passes of 2^log2_n1 points, then transposing passes of

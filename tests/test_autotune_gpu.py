@@ -68,3 +68,26 @@ def test_tune_split_four_step(tc, orc):
         assert orc.rel_l2(from_dev_f32(out), orc.fft1d(x)) < 1e-5
     finally:
         _reset(tc, tc.SPLIT_FP32, ch, logn)
+
+
+@pytest.mark.parametrize("batch", [64, 4096, 16384])
+def test_preferred_tile(tc, orc, batch):
+    """A tuning file's choice (tcfft_tune_prefer, mid 512-row tiles at
+    N = 256) gives the transform at every batch, including the small ones
+    that take the smaller narrow tiles instead."""
+    from gpu_util import f16_round, from_dev_f16, to_dev_f16
+    from fft_demo_gb300 import autotune
+    n, logn = 256, 8
+    assert tc.lib().tcfft_tune_prefer(tc.FP16, autotune.PASS_ROW, logn, autotune.TILE_MID) == 0
+    try:
+        rng = np.random.default_rng(batch)
+        x = f16_round(uniform_complex(rng, (batch, n)))
+        plan = tc.plan_1d(n, batch)
+        d = to_dev_f16(x)
+        plan.exec(d)
+        plan.check()
+        y = from_dev_f16(d)
+        assert orc.rel_l2(y, orc.fft1d(x)) < 2e-3
+        plan.destroy()
+    finally:
+        tc.lib().tcfft_tune_set(tc.FP16, autotune.PASS_ROW, logn, -1)
