@@ -492,6 +492,18 @@ __device__ __forceinline__ bool split_wait_prefetch(SplitState& st, const IO& io
 // NT: threads per CTA (256, or 128 for 256-row tiles run 4 CTAs per SM).
 // PF: prefetching kernel; the tile is in rawbuf (its copy is awaited here)
 // and the next one's copy is issued once the planes are written.
+//
+// Lane-bit destinations (remap_lane_bits over the NT * U items) of the
+// prefetching kernel's row-input items in line-minor tiles (the transposing
+// passes), from a CPU model of the shared-memory banks counting the raw
+// reads and the four planes' stores of a tile: L = 512 on 8-line tiles
+// 2560 -> 2048 wavefronts. Identity elsewhere.
+template <int L, int G, bool APPLY, int NITEMS>
+constexpr LaneBits split_pf_row_lane_bits() {
+  if constexpr (APPLY && L == 512 && G == 8 && NITEMS == 512) return LaneBits{{0, 2, 3, 4, 6}};
+  return LaneBits{{0, 1, 2, 3, 4}};
+}
+
 template <int L, int G, bool LINE_MINOR, int SIGN, class IO, bool TMA_IN = false, int NT = kPassThreads,
           bool PF = false>
 __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const PassCore& core, long long line0,
@@ -579,6 +591,16 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
       constexpr int QPL = (L / T) / 4;
       constexpr int ITEMS = G * QPL;
       static_assert(ITEMS <= NT * U, "one load batch per tile");
+      constexpr LaneBits LB = split_pf_row_lane_bits<L, G, PF && LINE_MINOR, NT * U>();
+      constexpr int B0 = LB.b[0], B1 = LB.b[1], B2 = LB.b[2], B3 = LB.b[3], B4 = LB.b[4];
+      constexpr bool REMAP = !(B0 == 0 && B1 == 1 && B2 == 2 && B3 == 3 && B4 == 4);
+      auto row_item = [&](int u) {
+        if constexpr (REMAP) {
+          return remap_lane_bits<NT * U, B0, B1, B2, B3, B4>(tid + u * NT);
+        } else {
+          return tid + u * NT;
+        }
+      };
       // item -> (line g, first of four consecutive butterflies j0): a warp's
       // loads run along one line
       auto item_g = [](int it) { return it / QPL; };
@@ -586,7 +608,7 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
       typename IO::Raw raw[U][T];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const int it = tid + u * NT;
+        const int it = row_item(u);
 #pragma unroll
         for (int r = 0; r < T; ++r) {
           if constexpr (PF) {
@@ -606,7 +628,7 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
       float lmax = 0.f;
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const int it = tid + u * NT;
+        const int it = row_item(u);
         const int g = item_g(it);
         const int j0 = item_j0(it);
 #pragma unroll
@@ -618,7 +640,7 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
       scales_from(lmax);
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const int it = tid + u * NT;
+        const int it = row_item(u);
         if (ITEMS % (NT * U) != 0 && it >= ITEMS) continue;
         const int g = item_g(it);
         const int j0 = item_j0(it);

@@ -635,7 +635,7 @@ struct LaneBits {
 template <int NT, int B0, int B1, int B2, int B3, int B4>
 __device__ __forceinline__ int remap_lane_bits(int tid) {
   constexpr int K = ilog2c(NT);
-  static_assert((1 << K) == NT && K >= 5 && K <= 8, "threads per CTA");
+  static_assert((1 << K) == NT && K >= 5 && K <= 10, "index range: a power of two, 32 to 1024");
   constexpr int B[5] = {B0, B1, B2, B3, B4};
   if constexpr (B0 == 0 && B1 == 1 && B2 == 2 && B3 == 3 && B4 == 4) {
     return tid;
