@@ -496,11 +496,11 @@ __device__ __forceinline__ bool split_wait_prefetch(SplitState& st, const IO& io
 // Lane-bit destinations (remap_lane_bits over the NT * U items) of the
 // prefetching kernel's row-input items in line-minor tiles (the transposing
 // passes), from a CPU model of the shared-memory banks counting the raw
-// reads and the four planes' stores of a tile: L = 512 on 8-line tiles
-// 2560 -> 2048 wavefronts. Identity elsewhere.
+// reads and the four planes' stores of a tile: 2560 -> 2048 wavefronts for
+// every 256-row tile (L = 256 .. 2048 on 16 .. 2 lines). Identity elsewhere.
 template <int L, int G, bool APPLY, int NITEMS>
 constexpr LaneBits split_pf_row_lane_bits() {
-  if constexpr (APPLY && L == 512 && G == 8 && NITEMS == 512) return LaneBits{{0, 2, 3, 4, 6}};
+  if constexpr (APPLY && L * G == 4096 && L >= 256 && NITEMS >= 128) return LaneBits{{0, 2, 3, 4, 6}};
   return LaneBits{{0, 1, 2, 3, 4}};
 }
 
