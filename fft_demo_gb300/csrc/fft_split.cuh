@@ -498,6 +498,17 @@ __device__ __forceinline__ bool split_wait_prefetch(SplitState& st, const IO& io
 // passes), from a CPU model of the shared-memory banks counting the raw
 // reads and the four planes' stores of a tile: 2560 -> 2048 wavefronts for
 // every 256-row tile (L = 256 .. 2048 on 16 .. 2 lines). Identity elsewhere.
+// The same for column input ([L][G] raw tiles: the four-step column
+// passes): 2^20's 1024-point pass on 4-line tiles 1536 -> 1024 wavefronts,
+// 65536's 128-point pass on 32-line tiles 1024 -> 768.
+template <int L, int G, bool APPLY, int NITEMS>
+constexpr LaneBits split_pf_col_lane_bits() {
+  if constexpr (APPLY && L == 1024 && G == 4 && NITEMS == 256) return LaneBits{{0, 1, 2, 4, 3}};
+  if constexpr (APPLY && ((L == 128 && G == 32) || (L == 512 && G == 8)) && NITEMS >= 64)
+    return LaneBits{{0, 1, 2, 5, 3}};
+  return LaneBits{{0, 1, 2, 3, 4}};
+}
+
 template <int L, int G, bool APPLY, int NITEMS>
 constexpr LaneBits split_pf_row_lane_bits() {
   if constexpr (APPLY && L * G == 4096 && L >= 256 && NITEMS >= 128) return LaneBits{{0, 2, 3, 4, 6}};
@@ -719,6 +730,16 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
       constexpr int GQ = G / 4;
       constexpr int ITEMS = GQ * (L / T);
       static_assert(ITEMS <= NT * U, "one load batch per tile");
+      constexpr LaneBits CB = split_pf_col_lane_bits<L, G, PF && ITEMS == NT * U, NT * U>();
+      constexpr int C0 = CB.b[0], C1 = CB.b[1], C2 = CB.b[2], C3 = CB.b[3], C4 = CB.b[4];
+      constexpr bool CREMAP = !(C0 == 0 && C1 == 1 && C2 == 2 && C3 == 3 && C4 == 4);
+      auto col_item = [&](int u) {
+        if constexpr (CREMAP) {
+          return remap_lane_bits<NT * U, C0, C1, C2, C3, C4>(tid + u * NT);
+        } else {
+          return tid + u * NT;
+        }
+      };
       typename IO::Raw raw[U][T];
       bool loaded = false;
       if constexpr (TMA_IN) {
@@ -737,7 +758,7 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
           const uint8_t* src = st.smem + kSplitPlaneOffset;
 #pragma unroll
           for (int u = 0; u < U; ++u) {
-            const int it = tid + u * NT;
+            const int it = col_item(u);
 #pragma unroll
             for (int r = 0; r < T; ++r) {
               raw[u][r] = typename IO::Raw{make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
@@ -756,7 +777,7 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
         // the prefetched [L][G] tile (past the last line: zero-filled)
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-          const int it = tid + u * NT;
+          const int it = col_item(u);
 #pragma unroll
           for (int r = 0; r < T; ++r) {
             raw[u][r] = typename IO::Raw{make_uint4(0, 0, 0, 0), make_uint4(0, 0, 0, 0)};
@@ -770,7 +791,7 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
       if (!loaded) {
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-          const int it = tid + u * NT;
+          const int it = col_item(u);
 #pragma unroll
           for (int r = 0; r < T; ++r)
             raw[u][r] = io.fetch_g(line0 + (it % GQ) * 4, it / GQ + r * (L / T), it < ITEMS);
@@ -780,7 +801,7 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
       float lmax = 0.f;
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const int it = tid + u * NT;
+        const int it = col_item(u);
         const int j = it / GQ;
         const int g0 = (it % GQ) * 4;
 #pragma unroll
@@ -792,7 +813,7 @@ __device__ __forceinline__ bool split_tile(SplitState& st, const IO& io, const P
       scales_from(lmax);
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        const int it = tid + u * NT;
+        const int it = col_item(u);
         if (ITEMS % (NT * U) != 0 && it >= ITEMS) continue;
         const int j = it / GQ;
         const int g0 = (it % GQ) * 4;
