@@ -73,7 +73,8 @@ def test_split_row_inverse_variants(tc, orc):
         tc.lib().tcfft_tune_set(SPLIT, PASS_ROW, 12, -1)
 
 
-@pytest.mark.parametrize("n,log_n1", [(1 << 16, 9), (1 << 16, 8), (1 << 16, 6), (1 << 20, 9), (1 << 20, 10)])
+@pytest.mark.parametrize("n,log_n1", [(1 << 16, 9), (1 << 16, 8), (1 << 16, 7), (1 << 16, 6), (1 << 20, 9),
+                                       (1 << 20, 10)])
 def test_split_four_step_tile_variants(tc, orc, n, log_n1):
     """Both passes of the two-pass path with every combination of the column
     and transposing-row variants, under the given column/row split."""
