@@ -394,7 +394,7 @@ def uneven(peak_gbs, count=10000, nconv=512, seed=4, precisions=((tc.SPLIT_FP32,
 
 def serving(peak_gbs, rate=20000.0, seconds=1.0, sweep=(8000.0, 16000.0, 24000.0, 28000.0, 32000.0, 36000.0, 40000.0),
             sweep_seconds=0.5,
-            p99_bound_ms=50.0, max_side=2048, repeats=3):
+            p99_bound_ms=50.0, max_side=2048, repeats=5):
     """Config 5 at the offered 20k req/s (image sides 64 .. max_side), then a
     sweep of offered rates: the saturation rate is the largest achieved rate
     whose p99 latency stays within p99_bound_ms. The 20k stream runs
